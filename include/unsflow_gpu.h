@@ -1,0 +1,120 @@
+/*
+ * unsflow_gpu.h -- C-ABI of libunsflow_gpu.so, the GB300 (sm_103a) drop-in for
+ * the residual-and-update hot path of UNSFlow2D.
+ *
+ * The reference hot-path subroutines take no arguments and work on Fortran
+ * module arrays.  Here each of them becomes one entry point that works on the
+ * device copy of those arrays held by an opaque handle; the caller (the
+ * Fortran main program through iso_c_binding, or the C++ driver in
+ * libunsflow_host.so) calls them in the same order as the reference main
+ * loop.  Every call returns a UNS_* status (unsflow_types.h) instead of
+ * printing and stopping.  One handle = one CUDA stream; calls on one handle
+ * must come from one host thread at a time; handles are independent.
+ *
+ * Citations are file:line in the UNSFlow2D sources.
+ */
+#ifndef UNSFLOW_GPU_H
+#define UNSFLOW_GPU_H
+#include "unsflow_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* uns_last_error(void);
+/* Library version string. */
+const char* uns_version(void);
+
+/* ============================================================ CCFVM =====*/
+typedef struct uns_cc_handle uns_cc_handle;
+
+/* Copies the preprocessed mesh (the `grid` module after geometric,
+ * CCFVM/geometric.F90:1-57) and the flo.inp parameters to the device and
+ * sets the freestream (CCFVM/read_input.F90:237-262).  The caller may free
+ * its arrays afterwards. */
+int uns_cc_create(const uns_cc_mesh* mesh, const uns_params* params, uns_cc_handle** out);
+int uns_cc_destroy(uns_cc_handle* h);
+
+/* initialize (CCFVM/read_input.F90:291-294): qc = freestream on every cell
+ * including ghosts, phi = 1, primitives 0. */
+int uns_cc_initialize(uns_cc_handle* h);
+/* Conserved state of all noc+nbf cells, [noc+nbf][4] row-major. */
+int uns_cc_set_state(uns_cc_handle* h, const double* qc);
+int uns_cc_get_state(uns_cc_handle* h, double* qc);
+/* Any UNS_CC_* field (unsflow_types.h) copied to host memory. */
+int uns_cc_get_field(uns_cc_handle* h, int field, double* out);
+
+/* con2prim over the interior cells (CCFVM/main.F90:62-67). */
+int uns_cc_con2prim(uns_cc_handle* h);
+/* avg_c2v (CCFVM/average.F90:1-39). */
+int uns_cc_avg_c2v(uns_cc_handle* h);
+/* time_step02 + spectral02 (CCFVM/timestep.F90:350-429); dtglobal may be NULL. */
+int uns_cc_time_step(uns_cc_handle* h, double cfl, double* dtglobal);
+/* save_old (CCFVM/solution.F90:331-345). */
+int uns_cc_save_old(uns_cc_handle* h);
+/* Gradient_GG / Gradient_GG_FC / Gradient_LSQR per params.grad_type,
+ * followed by limit when params.ilimit == 1 (CCFVM/gradient.F90:293-614). */
+int uns_cc_gradient(uns_cc_handle* h);
+/* limit -> limiter_VKN1 (CCFVM/limiter.F90:3-17,123-296). */
+int uns_cc_limit(uns_cc_handle* h);
+/* fvresidual (CCFVM/fvresidual.F90:4-187): boundary and interior convective
+ * fluxes, ghost states, viscous flux, implicit residual smoothing. */
+int uns_cc_fvresidual(uns_cc_handle* h);
+/* One RK3 stage update, irk = 1..3 (CCFVM/main.F90:90-101). */
+int uns_cc_rk_stage(uns_cc_handle* h, int irk);
+/* lusgs -> lusgs2 (CCFVM/lusgs.F90:5-10,207-379), level-scheduled. */
+int uns_cc_lusgs(uns_cc_handle* h);
+/* check_positivity (CCFVM/main.F90:358-414): UNS_ERR_NONPOSITIVE and the
+ * 0-based cell index in *bad_cell (-1 when none). */
+int uns_cc_check_positivity(uns_cc_handle* h, int* bad_cell);
+/* residue (CCFVM/solution.F90:349-372): sqrt(sum res^2 / noc / 4) before the
+ * first-iteration normalisation, which stays with the caller. */
+int uns_cc_residue(uns_cc_handle* h, double* fres_raw);
+/* Flux-based wall forces Fx1, Fy1 of the last fvresidual
+ * (CCFVM/fvresidual.F90:99-100, CCFVM/viscous_flux.F90:530-533). */
+int uns_cc_forces(uns_cc_handle* h, double* fx1, double* fy1);
+/* Fast path: `niter` whole iterations of the main loop body
+ * (CCFVM/main.F90:59-115) replayed from one captured CUDA graph.  cfl[k] is
+ * the CFL of iteration k; fres_raw[k] receives that iteration's raw residual
+ * norm.  When first_iter is non-zero the first iteration is iteration 1 of
+ * the run and its norm becomes the normalisation; iterations after the
+ * normalised norm drops to params.min_res are skipped on the device, as the
+ * reference loop stops there.  Returns the number of iterations executed in
+ * *done_iters (may be NULL). */
+int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
+                   int* done_iters);
+
+/* ============================================================ NCFVM =====*/
+typedef struct uns_nc_handle uns_nc_handle;
+
+/* Mesh and parameters of the vertex-centred solver (NCFVM/geometric.f90,
+ * NCFVM/common.f90:19-54). */
+int uns_nc_create(const uns_nc_mesh* mesh, const uns_params* params, uns_nc_handle** out);
+int uns_nc_destroy(uns_nc_handle* h);
+/* initialize (NCFVM/common.f90:50-52): qc = freestream; phi = 1e20. */
+int uns_nc_initialize(uns_nc_handle* h);
+int uns_nc_set_state(uns_nc_handle* h, const double* qc);
+int uns_nc_get_state(uns_nc_handle* h, double* qc);
+int uns_nc_get_field(uns_nc_handle* h, int field, double* out);
+/* save_old (NCFVM/common.f90:88-104): con2prim + qold. */
+int uns_nc_save_old(uns_nc_handle* h);
+/* fvresidual (NCFVM/fvresidual.f90:4-85): Gradient_LSQR, limiter, edge
+ * fluxes, wall and farfield closures, then time_step2 with this CFL. */
+int uns_nc_fvresidual(uns_nc_handle* h, double cfl);
+/* One RK3 stage update, irk = 1..3 (NCFVM/main.f90:321-342). */
+int uns_nc_rk_stage(uns_nc_handle* h, int irk);
+/* lusgs (NCFVM/lusgs.f90:4-157), level-scheduled; calls fvresidual. */
+int uns_nc_lusgs(uns_nc_handle* h, double cfl);
+/* residue (NCFVM/common.f90:108-154) before normalisation: L2 over nodes,
+ * Linf and its 0-based node (any output pointer may be NULL). */
+int uns_nc_residue(uns_nc_handle* h, double* fres_raw, double* fresi, int* iresi);
+/* Fast path as uns_cc_iterate for the loop body NCFVM/main.f90:315-348;
+ * fresi may be NULL. */
+int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
+                   double* fresi, int* done_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UNSFLOW_GPU_H */

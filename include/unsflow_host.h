@@ -1,0 +1,70 @@
+/*
+ * unsflow_host.h -- C-ABI of libunsflow_host.so, the caller side of the drop-in.
+ *
+ * The reference keeps the Fortran driver, flo.inp and geometry.inp as they
+ * are and replaces only the hot-path subroutines.  No Fortran compiler exists
+ * in this build environment, so the caller side is provided in C++ here:
+ * the geometry.inp readers and the geometric preprocessing restated from
+ * CCFVM/geometric.F90 and NCFVM/geometric.f90 (connectivity orders matter:
+ * they fix summation and LU-SGS sweep order), a flo.inp reader, an analytic
+ * airfoil O-mesh generator (the reference ships no meshes), and a driver that
+ * runs the reference main loop through the libunsflow_gpu.so entry points.
+ */
+#ifndef UNSFLOW_HOST_H
+#define UNSFLOW_HOST_H
+#include "unsflow_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct uns_host_cc uns_host_cc; /* raw + preprocessed CC mesh */
+typedef struct uns_host_nc uns_host_nc; /* raw + preprocessed NC mesh */
+
+const char* uns_host_last_error(void);
+
+/* Symmetric 4-digit-thickness airfoil O-mesh: ni circumferential x nj radial
+ * quads, each split into two triangles; farfield circle of radius rfar chords
+ * about mid-chord; geometric radial spacing from dwall at the wall. */
+int uns_host_cc_airfoil(int ni, int nj, double thickness, double rfar, double dwall, uns_host_cc** out);
+int uns_host_nc_airfoil(int ni, int nj, double thickness, double rfar, double dwall, uns_host_nc** out);
+/* geometry.inp readers (CCFVM/read_input.F90:123-213, NCFVM/read_input.f90:
+ * 479-512) followed by geometric. */
+int uns_host_cc_read(const char* path, uns_host_cc** out);
+int uns_host_nc_read(const char* path, uns_host_nc** out);
+/* Write the raw (file) form in the reference's geometry.inp layout. */
+int uns_host_cc_write(const uns_host_cc* m, const char* path);
+int uns_host_nc_write(const uns_host_nc* m, const char* path);
+/* Views of the preprocessed mesh (pointers valid until the free call). */
+int uns_host_cc_view(const uns_host_cc* m, uns_cc_mesh* view);
+int uns_host_nc_view(const uns_host_nc* m, uns_nc_mesh* view);
+/* Renumbering map: file index (0-based) -> index after geometric. */
+int uns_host_cc_newnum(const uns_host_cc* m, int32_t* out);  /* [noc] */
+int uns_host_nc_newnum(const uns_host_nc* m, int32_t* out);  /* [nop] */
+void uns_host_cc_free(uns_host_cc* m);
+void uns_host_nc_free(uns_host_nc* m);
+
+/* flo.inp readers.  `grid` receives the GridFile value (up to gridlen-1
+ * characters). */
+int uns_host_read_flo_cc(const char* path, uns_params* p, char* grid, int gridlen);
+int uns_host_read_flo_nc(const char* path, uns_params* p, char* grid, int gridlen);
+
+/* CFL schedules: cfl_number (CCFVM/main.F90:148-168; `prev` is the value kept
+ * when the ramp is over) and the fixed tanh ramp of NCFVM/main.f90:316. */
+double uns_host_cfl_cc(const uns_params* p, int iter, double prev);
+double uns_host_cfl_nc(const uns_params* p, int iter);
+
+/* The reference main program (CCFVM/main.F90:4-170, NCFVM/main.f90:266-374)
+ * on the GPU library: reads flo.inp, the geometry named there (relative to
+ * flo.inp's directory), runs to MaxIter / MinRes and writes FLO.RES into
+ * outdir.  mode 0 calls one entry point per reference subroutine each
+ * iteration; mode 1 uses the graph-replayed uns_*_iterate fast path.
+ * iters_out / fres_out (may be NULL) receive the iteration count and the
+ * final normalised residual. */
+int uns_host_cc_main(const char* flo_inp, const char* outdir, int mode, int* iters_out, double* fres_out);
+int uns_host_nc_main(const char* flo_inp, const char* outdir, int mode, int* iters_out, double* fres_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UNSFLOW_HOST_H */

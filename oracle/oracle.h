@@ -1,0 +1,68 @@
+/*
+ * oracle.h -- TEST INFRASTRUCTURE ONLY.  CPU oracle for the UNSFlow2D hot path.
+ *
+ * A serial C++ restatement of the reference Fortran routines on the
+ * residual-and-update path (CCFVM and NCFVM), written loop for loop in the
+ * reference's own order (face loops that scatter into cells/nodes).  Only the
+ * test-suite, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+ * always as the checker; the product library never links it.
+ *
+ * PARITY UNPINNED: the reference ships no tests, fixtures or golden vectors,
+ * and it cannot be compiled here (no Fortran compiler in this image; NCFVM
+ * also carries unresolved merge-conflict markers).  The oracle is checked
+ * against analytic known answers instead (freestream preservation, flux
+ * consistency, exact linear gradients, conservation) -- see tests/.
+ */
+#ifndef UNS_ORACLE_H
+#define UNS_ORACLE_H
+#include "unsflow_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_cc oracle_cc;
+typedef struct oracle_nc oracle_nc;
+
+/* ------------------------------------------------------------ CCFVM */
+oracle_cc* oracle_cc_create(const uns_cc_mesh* m, const uns_params* p);
+void oracle_cc_free(oracle_cc* o);
+int oracle_cc_initialize(oracle_cc* o);                 /* solution.F90:231-297 */
+int oracle_cc_set_state(oracle_cc* o, const double* qc);/* [noc+nbf][4]          */
+int oracle_cc_con2prim(oracle_cc* o);                   /* main.F90:62-67        */
+int oracle_cc_avg_c2v(oracle_cc* o);                    /* average.F90:1-39      */
+int oracle_cc_time_step(oracle_cc* o, double cfl, double* dtglobal); /* timestep.F90:28-107 */
+int oracle_cc_save_old(oracle_cc* o);                   /* solution.F90:331-345  */
+int oracle_cc_gradient(oracle_cc* o);                   /* gradient.F90 (+limit) */
+int oracle_cc_limit(oracle_cc* o);                      /* limiter.F90:3-17,123-296 */
+int oracle_cc_fvresidual(oracle_cc* o);                 /* fvresidual.F90:4-187  */
+int oracle_cc_rk_stage(oracle_cc* o, int irk);          /* main.F90:90-101       */
+int oracle_cc_lusgs(oracle_cc* o);                      /* lusgs.F90:207-379     */
+int oracle_cc_check_positivity(oracle_cc* o, int* bad); /* main.F90:358-414      */
+int oracle_cc_residue(oracle_cc* o, double* fres_raw);  /* solution.F90:349-393  */
+int oracle_cc_forces(oracle_cc* o, double* fx1, double* fy1);
+/* One full iteration of main.F90:57-117 (cfl given). */
+int oracle_cc_iteration(oracle_cc* o, double cfl, double* fres_raw);
+int oracle_cc_get(oracle_cc* o, int field, double* out);
+/* Test hook: overwrite QC, QP (all cells incl. ghosts), GRAD or PHI. */
+int oracle_cc_set(oracle_cc* o, int field, const double* in);
+
+/* ------------------------------------------------------------ NCFVM */
+oracle_nc* oracle_nc_create(const uns_nc_mesh* m, const uns_params* p);
+void oracle_nc_free(oracle_nc* o);
+int oracle_nc_initialize(oracle_nc* o);                 /* NCFVM/common.f90:19-54 */
+int oracle_nc_set_state(oracle_nc* o, const double* qc);
+int oracle_nc_save_old(oracle_nc* o);                   /* common.f90:88-104      */
+int oracle_nc_fvresidual(oracle_nc* o, double cfl);     /* fvresidual.f90:4-85    */
+int oracle_nc_rk_stage(oracle_nc* o, int irk);          /* main.f90:321-342       */
+int oracle_nc_lusgs(oracle_nc* o, double cfl);          /* lusgs.f90:4-157        */
+int oracle_nc_residue(oracle_nc* o, double* fres_raw, double* fresi, int* iresi); /* common.f90:108-154 */
+int oracle_nc_iteration(oracle_nc* o, double cfl, double* fres_raw, double* fresi);
+int oracle_nc_get(oracle_nc* o, int field, double* out);
+/* Test hook: overwrite QC, QP, GRAD or PHI. */
+int oracle_nc_set(oracle_nc* o, int field, const double* in);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,94 @@
+"""CCFVM hot path on the GPU vs the CPU oracle, routine by routine.
+
+Tolerance: 1e-12 of each field's max magnitude (FP64; the GPU fuses
+multiply-adds and sums faces in the same order as the reference, so the
+difference is a few ulps per operation).
+"""
+import numpy as np
+import pytest
+
+from unsflow2d_gb300 import abi, mesh
+from unsflow2d_gb300.solver import CCSolver
+from oracle import OracleCC
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+CASES = [
+    dict(flux="roe", grad="gg"),
+    dict(flux="rusanov", grad="gg"),
+    dict(flux="vanleer", grad="lsqr"),
+    dict(flux="ausm", grad="ggfc"),
+    dict(flux="roe", grad="gg", time="lusgs", cfl_max=5.0, cfl_type="ramp", cfl_min=0.5, cfl_ramp_steps=10),
+    dict(flux="roe", grad="ggfc", flow="laminar", iwall=0, rey=500.0, m_inf=0.5),
+    dict(flux="vanleer", grad="gg", flow="laminar", iwall=1, rey=5000.0),
+    dict(flux="roe", grad="lsqr", irs=1, ilimit=0),
+]
+
+
+@pytest.fixture(scope="module")
+def cc_mesh():
+    return mesh.CCMesh.airfoil(24, 12)
+
+
+@pytest.mark.parametrize("case", CASES, ids=[str(i) for i in range(len(CASES))])
+def test_cc_routine_parity(cc_mesh, case, assert_close):
+    p = abi.make_params(**case)
+    g, o = CCSolver(cc_mesh, p), OracleCC(cc_mesh, p)
+    cfl = 0.0
+    for it in range(1, 4):
+        cfl = mesh.cfl_schedule(p, it, 1, "cc", cfl)[0]
+        for s in (g, o):
+            s.con2prim()
+        assert_close("qp", g.get("qp"), o.get("qp"), RTOL)
+        for s in (g, o):
+            s.avg_c2v()
+        assert_close("ptprim", g.get("ptprim"), o.get("ptprim"), RTOL)
+        assert_close("fqp", g.get("fqp"), o.get("fqp"), RTOL)
+        for s in (g, o):
+            s.time_step(cfl)
+        assert_close("fla", g.get("fla"), o.get("fla"), RTOL)
+        assert_close("dt", g.get("dt"), o.get("dt"), RTOL)
+        for s in (g, o):
+            s.save_old()
+            s.gradient()
+        assert_close("grad", g.get("grad"), o.get("grad"), RTOL)
+        assert_close("phi", g.get("phi"), o.get("phi"), RTOL)
+        if p.time_mode == abi.TIME["rk3"]:
+            for irk in (1, 2, 3):
+                for s in (g, o):
+                    s.fvresidual()
+                assert_close(f"res it{it} st{irk}", g.get("res"), o.get("res"), RTOL)
+                assert_close("ghost qc", g.get("qc")[g.noc:], o.get("qc")[o.noc:], RTOL)
+                for s in (g, o):
+                    s.rk_stage(irk)
+                assert_close("qc", g.get("qc"), o.get("qc"), RTOL)
+        else:
+            for s in (g, o):
+                s.lusgs()
+            assert_close("res", g.get("res"), o.get("res"), RTOL)
+            assert_close("qc", g.get("qc"), o.get("qc"), RTOL)
+        assert g.check_positivity() == o.check_positivity() == -1
+        fg, fo = g.residue(), o.residue()
+        assert abs(fg - fo) <= RTOL * abs(fo)
+        if case.get("flow") == "laminar":
+            assert_close("fmu", g.get("fmu"), o.get("fmu"), RTOL)
+        fx, fy = g.forces()
+        ox, oy = o.forces()
+        assert abs(fx - ox) <= RTOL * (abs(ox) + 1e-300) and abs(fy - oy) <= RTOL * (abs(oy) + 1e-300)
+
+
+@pytest.mark.parametrize("case", [CASES[0], CASES[4]], ids=["rk3", "lusgs"])
+def test_cc_history_graph_vs_oracle(cc_mesh, case):
+    """FLO.RES residual history: graph-replayed iterations vs the oracle loop."""
+    p = abi.make_params(**case)
+    g, o = CCSolver(cc_mesh, p), OracleCC(cc_mesh, p)
+    n = 60
+    cfl = mesh.cfl_schedule(p, 1, n, "cc")
+    fg = g.iterate(cfl, first_iter=True)
+    fo = np.array([o.iteration(c) for c in cfl])
+    assert len(fg) == n
+    lg, lo = np.log10(fg / fg[0]), np.log10(fo / fo[0])
+    # the FLO.RES text (e16.6) agrees to its printed digits
+    assert np.max(np.abs(lg - lo)) < 1e-9
+    assert np.max(np.abs(g.get_state() - o.get_state())) <= 1e-10 * np.max(np.abs(o.get_state()))

@@ -1,0 +1,211 @@
+"""Caller-side host logic (no GPU): mesh generator, geometry.inp round trip,
+geometric invariants, flo.inp reader, CFL schedules, and the C-ABI surface."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from unsflow2d_gb300 import abi, mesh
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+@pytest.fixture(scope="module")
+def cc():
+    return mesh.CCMesh.airfoil(32, 16)
+
+
+@pytest.fixture(scope="module")
+def nc():
+    return mesh.NCMesh.airfoil(32, 16)
+
+
+def test_cc_counts_match_the_o_mesh_formula(cc):
+    I, J = 32, 16
+    assert cc["noc"] == 2 * I * J
+    assert cc["nop"] == I * (J + 1)
+    assert cc["nfi"] + cc["nbf"] == I * (J + 1) + 2 * I * J
+    assert cc["nbf"] == 2 * I
+
+
+def test_cc_geometry_invariants(cc):
+    m = cc.arrays
+    assert np.allclose(np.hypot(m["fnx"], m["fny"]), 1.0, atol=1e-14)
+    assert (m["cv"] > 0).all() and (m["cov"] > 0).all() and (m["farea"] > 0).all()
+    # normal points from `in` to `out` (ghosts included)
+    d = np.stack([m["cx"][m["fout"]] - m["cx"][m["fin"]], m["cy"][m["fout"]] - m["cy"][m["fin"]]], 1)
+    assert ((d[:, 0] * m["fnx"] + d[:, 1] * m["fny"]) > 0).all()
+    # every interior cell is closed: sum of n*A over its faces (signed) = 0
+    noc = m["noc"]
+    s = np.zeros((noc, 2))
+    for f in range(len(m["fin"])):
+        a = m["farea"][f] * np.array([m["fnx"][f], m["fny"][f]])
+        s[m["fin"][f]] += a
+        if m["fout"][f] < noc:
+            s[m["fout"][f]] -= a
+    assert np.abs(s).max() < 1e-12
+    # triangles: three faces each; ghost count = boundary faces
+    assert (np.diff(m["c2f_off"]) == 3).all()
+    assert (m["fout"][m["nfi"]:] == noc + np.arange(m["nbf"])).all()
+
+
+def test_cc_bfs_renumbering(cc):
+    """renumber (CCFVM/geometric.F90:247-356): a permutation starting at file cell 1,
+    and every renumbered cell >0 has an interior neighbour with a smaller number."""
+    nn = cc.newnum()
+    m = cc.arrays
+    assert sorted(nn.tolist()) == list(range(m["noc"]))
+    assert nn[0] == 0
+    nfi = m["nfi"]
+    lowest = np.full(m["noc"], m["noc"])
+    for a, b in zip(m["fin"][:nfi], m["fout"][:nfi]):
+        lowest[a] = min(lowest[a], b)
+        lowest[b] = min(lowest[b], a)
+    assert (lowest[1:] < np.arange(1, m["noc"])).all()
+
+
+def test_cc_pseudo_laplacian_weights_reproduce_linear_fields(cc):
+    m = cc.arrays
+    f = lambda x, y: 3.0 + 2.0 * x - 5.0 * y
+    vals = f(m["cx"], m["cy"])
+    off, idx, w = m["v2c_off"], m["v2c"], m["v2c_wt"]
+    avg = np.array([np.dot(w[off[i]:off[i + 1]], vals[idx[off[i]:off[i + 1]]]) / w[off[i]:off[i + 1]].sum()
+                    for i in range(m["nop"])])
+    assert np.abs(avg - f(m["px"], m["py"])).max() < 1e-9
+
+
+def test_nc_geometry_invariants(nc, cc):
+    m = nc.arrays
+    assert np.isclose(m["cv"].sum(), cc["cv"].sum(), rtol=1e-12)
+    assert (m["cv"] > 0).all()
+    assert np.allclose(np.hypot(m["fnx"], m["fny"]), 1.0, atol=1e-14)
+    # interior dual cells are closed
+    s = np.zeros((m["nop"], 2))
+    for f in range(m["nof"]):
+        a = m["farea"][f] * np.array([m["fnx"][f], m["fny"][f]])
+        s[m["fp1"][f]] += a
+        s[m["fp2"][f]] -= a
+    onb = np.zeros(m["nop"], bool)
+    onb[m["fp1"][m["fbc"] != 0]] = True
+    onb[m["fp2"][m["fbc"] != 0]] = True
+    assert np.abs(s[~onb]).max() < 1e-12
+    nn = nc.newnum()
+    assert sorted(nn.tolist()) == list(range(m["nop"])) and nn[0] == 0
+
+
+def test_geometry_inp_round_trip(cc, nc, tmp_path):
+    for m, cls in ((cc, mesh.CCMesh), (nc, mesh.NCMesh)):
+        path = tmp_path / f"{m.kind}.inp"
+        m.write(path)
+        r = cls.read(path)
+        for k, v in m.arrays.items():
+            if isinstance(v, np.ndarray):
+                assert np.array_equal(v, r.arrays[k]), (m.kind, k)
+
+
+def test_truncated_geometry_file_is_an_io_error(cc, tmp_path):
+    path = tmp_path / "g.inp"
+    cc.write(path)
+    lines = path.read_text().splitlines()
+    path.write_text("\n".join(lines[: len(lines) // 2]) + "\n")
+    with pytest.raises(abi.UnsError) as e:
+        mesh.CCMesh.read(path)
+    assert e.value.code == abi.UNS_ERR_IO
+
+
+def test_inverted_cell_is_a_mesh_error(cc, tmp_path):
+    path = tmp_path / "g.inp"
+    cc.write(path)
+    text = path.read_text().splitlines()
+    nop = int(text[0].split()[0])
+    # move point 1 far outside: its cells fold over
+    parts = text[1].split()
+    parts[1], parts[2] = "50.0", "50.0"
+    text[1] = " ".join(parts)
+    path.write_text("\n".join(text) + "\n")
+    with pytest.raises(abi.UnsError) as e:
+        mesh.CCMesh.read(path)
+    assert e.value.code == abi.UNS_ERR_MESH
+    assert nop > 0
+
+
+FLO_CC = """Start     1
+FlowType  {flow}  1 300
+Mach      0.5
+AOA       2.0
+Reynolds  5000
+CFL       {cfl_type}  0.1  {cfl} 500
+Timemode  {tm}
+GradType  gg
+LastIter  0
+MaxIter   20
+MinRes    1.0e-8
+SaveInt   1000
+ScrInt    100
+NoIso     30
+Flux      roe
+Limiter   1
+irs       0
+FarBC     0  0.0  0.0
+GridFile  "geometry.inp"
+"""
+
+
+def test_flo_inp_reader_and_validation(tmp_path):
+    f = tmp_path / "flo.inp"
+    f.write_text(FLO_CC.format(flow="inviscid", cfl_type="tanh", cfl=0.9, tm="rk3"))
+    p, grid = mesh.read_flo_inp(f)
+    assert grid == "geometry.inp" and p.m_inf == 0.5 and p.cfl_max == 0.9 and p.max_iter == 20
+    assert p.flux_type == abi.FLUX["roe"] and p.time_mode == abi.TIME["rk3"]
+    for bad in (dict(flow="turbulent", cfl_type="tanh", cfl=0.9, tm="rk3"),
+                dict(flow="inviscid", cfl_type="linear", cfl=0.9, tm="rk3"),
+                dict(flow="inviscid", cfl_type="tanh", cfl=1.0, tm="rk3"),   # rk3 needs CFL < 1
+                dict(flow="inviscid", cfl_type="tanh", cfl=0.9, tm="gmres")):
+        f.write_text(FLO_CC.format(**bad))
+        with pytest.raises(abi.UnsError) as e:
+            mesh.read_flo_inp(f)
+        assert e.value.code == abi.UNS_ERR_ARG
+    f.write_text("Start 1\nFlowType inviscid 1 300\n")
+    with pytest.raises(abi.UnsError) as e:
+        mesh.read_flo_inp(f)
+    assert e.value.code == abi.UNS_ERR_IO
+
+
+def test_cfl_schedules():
+    p = abi.make_params(cfl_type="tanh", cfl_max=0.9, cfl_ramp_steps=500)
+    c = mesh.cfl_schedule(p, 1, 600)
+    s = np.arange(1, 601) / 499.0
+    assert np.allclose(c, 0.5 * 0.9 * (1 + np.tanh(s * 7 - 3.5)), rtol=1e-15)
+    p = abi.make_params(cfl_type="ramp", cfl_min=0.1, cfl_max=5.0, cfl_ramp_steps=10, time="lusgs")
+    c = mesh.cfl_schedule(p, 1, 15)
+    assert np.isclose(c[9], 5.0) and (c[10:] == c[9]).all()
+    n = mesh.cfl_schedule(abi.make_params(cfl_max=50.0), 1, 3, kind="nc")
+    assert np.allclose(n, 0.5 * 50 * (1 + np.tanh(np.arange(1, 4) * 7 / 500 - 3.5)))
+
+
+def _declared(header: Path) -> set[str]:
+    text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+    return set(re.findall(r"^\s*(?:const\s+)?\w+[\s\*]+(uns_\w+)\s*\(", text, flags=re.M))
+
+
+def test_c_abi_exports_every_declared_symbol():
+    gpu, host = abi.gpu_lib(), abi.host_lib()
+    for header, lib in (("unsflow_gpu.h", gpu), ("unsflow_host.h", host)):
+        names = _declared(ROOT / "include" / header)
+        assert len(names) > 10
+        missing = [n for n in names if not hasattr(lib, n)]
+        assert not missing, (header, missing)
+
+
+def test_gpu_create_validates_mesh_on_the_host(cc):
+    """A corrupt index is rejected before any device call (works without a GPU)."""
+    lib = abi.gpu_lib()
+    arr = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in cc.arrays.items()}
+    arr["fin"][5] = arr["noc"] + 100
+    view, keep = abi.cc_view_from_arrays(arr)
+    h = C.c_void_p()
+    rc = lib.uns_cc_create(C.byref(view), C.byref(abi.make_params()), C.byref(h))
+    assert rc == abi.UNS_ERR_MESH and not h.value
+    assert b"out-of-range" in lib.uns_last_error()

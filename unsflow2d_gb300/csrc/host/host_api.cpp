@@ -1,0 +1,299 @@
+// host_api.cpp -- C-ABI of libunsflow_host.so (declared in unsflow_host.h):
+// mesh handles, flo.inp, CFL schedules and the C++ mirror of the reference
+// main programs driving libunsflow_gpu.so.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host_mesh.hpp"
+#include "unsflow_gpu.h"
+#include "unsflow_host.h"
+
+using namespace unshost;
+
+struct uns_host_cc { RawCC raw; MeshCC mesh; };
+struct uns_host_nc { RawNC raw; MeshNC mesh; };
+
+namespace {
+thread_local std::string g_err;
+int fail(int code, const std::string& msg) { g_err = msg; return code; }
+
+// Fortran Ew.d edit descriptor (e16.6): 0.dddddd mantissa, 2-digit exponent.
+std::string fort_e(double x, int w, int d) {
+    char buf[80];
+    if (std::isnan(x)) { std::snprintf(buf, sizeof buf, "%*s", w, "NaN"); return buf; }
+    if (std::isinf(x)) { std::snprintf(buf, sizeof buf, "%*s", w, x > 0 ? "Infinity" : "-Infinity"); return buf; }
+    std::string digits(d, '0');
+    int e = 0;
+    if (x != 0.0) {
+        char tmp[64];
+        std::snprintf(tmp, sizeof tmp, "%.*e", d - 1, std::fabs(x));  // d.ddddde+XX
+        digits.clear();
+        for (const char* c = tmp; *c && *c != 'e'; ++c)
+            if (*c >= '0' && *c <= '9') digits.push_back(*c);
+        e = std::atoi(std::strchr(tmp, 'e') + 1) + 1;
+    }
+    char body[64];
+    std::snprintf(body, sizeof body, "%s0.%sE%c%02d", x < 0 ? "-" : "", digits.c_str(), e < 0 ? '-' : '+', std::abs(e));
+    std::snprintf(buf, sizeof buf, "%*s", w, body);
+    return buf;
+}
+
+std::string dir_of(const std::string& p) {
+    size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string(".") : p.substr(0, k);
+}
+std::string join(const std::string& d, const std::string& f) {
+    if (!f.empty() && f[0] == '/') return f;
+    return d + "/" + f;
+}
+}  // namespace
+
+extern "C" {
+
+const char* uns_host_last_error(void) { return g_err.c_str(); }
+
+int uns_host_cc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns_host_cc** out) {
+    if (!out) return fail(UNS_ERR_ARG, "null out");
+    AirfoilSpec s{ni, nj, t, rfar, dwall};
+    auto* m = new uns_host_cc();
+    std::string err;
+    int rc = gen_airfoil_cc(s, m->raw, err);
+    if (!rc) rc = geometric_cc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_nc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns_host_nc** out) {
+    if (!out) return fail(UNS_ERR_ARG, "null out");
+    AirfoilSpec s{ni, nj, t, rfar, dwall};
+    auto* m = new uns_host_nc();
+    std::string err;
+    int rc = gen_airfoil_nc(s, m->raw, err);
+    if (!rc) rc = geometric_nc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_cc_read(const char* path, uns_host_cc** out) {
+    if (!path || !out) return fail(UNS_ERR_ARG, "null argument");
+    auto* m = new uns_host_cc();
+    std::string err;
+    int rc = read_geometry_cc(path, m->raw, err);
+    if (!rc) rc = geometric_cc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_nc_read(const char* path, uns_host_nc** out) {
+    if (!path || !out) return fail(UNS_ERR_ARG, "null argument");
+    auto* m = new uns_host_nc();
+    std::string err;
+    int rc = read_geometry_nc(path, m->raw, err);
+    if (!rc) rc = geometric_nc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_cc_write(const uns_host_cc* m, const char* path) {
+    if (!m || !path) return fail(UNS_ERR_ARG, "null argument");
+    std::string err;
+    int rc = write_geometry_cc(path, m->raw, err);
+    return rc ? fail(rc, err) : UNS_OK;
+}
+
+int uns_host_nc_write(const uns_host_nc* m, const char* path) {
+    if (!m || !path) return fail(UNS_ERR_ARG, "null argument");
+    std::string err;
+    int rc = write_geometry_nc(path, m->raw, err);
+    return rc ? fail(rc, err) : UNS_OK;
+}
+
+int uns_host_cc_view(const uns_host_cc* m, uns_cc_mesh* v) {
+    if (!m || !v) return fail(UNS_ERR_ARG, "null argument");
+    *v = m->mesh.view();
+    return UNS_OK;
+}
+
+int uns_host_nc_view(const uns_host_nc* m, uns_nc_mesh* v) {
+    if (!m || !v) return fail(UNS_ERR_ARG, "null argument");
+    *v = m->mesh.view();
+    return UNS_OK;
+}
+
+int uns_host_cc_newnum(const uns_host_cc* m, int32_t* out) {
+    if (!m || !out) return fail(UNS_ERR_ARG, "null argument");
+    std::copy(m->mesh.newnum.begin(), m->mesh.newnum.end(), out);
+    return UNS_OK;
+}
+
+int uns_host_nc_newnum(const uns_host_nc* m, int32_t* out) {
+    if (!m || !out) return fail(UNS_ERR_ARG, "null argument");
+    std::copy(m->mesh.newnum.begin(), m->mesh.newnum.end(), out);
+    return UNS_OK;
+}
+
+void uns_host_cc_free(uns_host_cc* m) { delete m; }
+void uns_host_nc_free(uns_host_nc* m) { delete m; }
+
+int uns_host_read_flo_cc(const char* path, uns_params* p, char* grid, int gridlen) {
+    if (!path || !p) return fail(UNS_ERR_ARG, "null argument");
+    std::string g, err;
+    int rc = read_flo_inp_cc(path, *p, g, err);
+    if (rc) return fail(rc, err);
+    if (grid && gridlen > 0) { std::strncpy(grid, g.c_str(), gridlen - 1); grid[gridlen - 1] = 0; }
+    return UNS_OK;
+}
+
+int uns_host_read_flo_nc(const char* path, uns_params* p, char* grid, int gridlen) {
+    if (!path || !p) return fail(UNS_ERR_ARG, "null argument");
+    std::string g, err;
+    int rc = read_flo_inp_nc(path, *p, g, err);
+    if (rc) return fail(rc, err);
+    if (grid && gridlen > 0) { std::strncpy(grid, g.c_str(), gridlen - 1); grid[gridlen - 1] = 0; }
+    return UNS_OK;
+}
+
+double uns_host_cfl_cc(const uns_params* p, int iter, double prev) {
+    if (p->cfl_type == UNS_CFL_TANH) {
+        double s = (double)iter / (double)(p->cfl_ramp_steps - 1);
+        return 0.5 * p->cfl_max * (1.0 + std::tanh(s * 7.0 - 3.5));
+    }
+    if (iter <= p->cfl_ramp_steps) {
+        double ef = 0.5;
+        double s = (double)iter / (double)p->cfl_ramp_steps;
+        return p->cfl_min + (p->cfl_max - p->cfl_min) * (1.0 - std::exp(-(s * ef))) / (1.0 - std::exp(-ef));
+    }
+    return prev;
+}
+
+double uns_host_cfl_nc(const uns_params* p, int iter) {
+    return 0.5 * p->cfl_max * (1.0 + std::tanh((double)iter * 7.0 / 500.0 - 3.5));
+}
+
+int uns_host_cc_main(const char* flo_inp, const char* outdir, int mode, int* iters_out, double* fres_out) {
+    if (!flo_inp || !outdir) return fail(UNS_ERR_ARG, "null argument");
+    uns_params P;
+    std::string grid, err;
+    int rc = read_flo_inp_cc(flo_inp, P, grid, err);
+    if (rc) return fail(rc, err);
+    RawCC raw;
+    MeshCC mesh;
+    if ((rc = read_geometry_cc(join(dir_of(flo_inp), grid), raw, err)) || (rc = geometric_cc(raw, mesh, err))) return fail(rc, err);
+    uns_cc_mesh view = mesh.view();
+    uns_cc_handle* h = nullptr;
+    if ((rc = uns_cc_create(&view, &P, &h))) return fail(rc, uns_last_error());
+    std::string res_path = std::string(outdir) + "/FLO.RES";
+    FILE* fo = std::fopen(res_path.c_str(), "w");
+    if (!fo) { uns_cc_destroy(h); return fail(UNS_ERR_IO, "cannot write " + res_path); }
+    int iter = 0;
+    double fres = 1.0, fres1 = 0.0, cfl = 0.0;
+    const double eps = 2.220446049250313e-16;
+    while (iter < P.max_iter && fres > P.min_res) {
+        if (mode == 0) {
+            ++iter;
+            cfl = uns_host_cfl_cc(&P, iter, cfl);
+            double raw_f;
+            int bad;
+            if ((rc = uns_cc_con2prim(h)) || (rc = uns_cc_avg_c2v(h)) || (rc = uns_cc_time_step(h, cfl, nullptr)) ||
+                (rc = uns_cc_save_old(h)) || (rc = uns_cc_gradient(h)))
+                break;
+            if (P.time_mode == UNS_TIME_RK3) {
+                for (int irk = 1; irk <= 3 && !rc; ++irk)
+                    if (!(rc = uns_cc_fvresidual(h))) rc = uns_cc_rk_stage(h, irk);
+            } else {
+                rc = uns_cc_lusgs(h);
+            }
+            if (rc || (rc = uns_cc_check_positivity(h, &bad)) || (rc = uns_cc_residue(h, &raw_f))) break;
+            if (iter == 1) fres1 = raw_f;
+            fres = (fres1 >= eps) ? raw_f / fres1 : raw_f;
+            std::fprintf(fo, "%6d%s%s\n", iter, fort_e(std::log10(fres), 16, 6).c_str(), fort_e(cfl, 16, 6).c_str());
+        } else {
+            int chunk = std::min(200, P.max_iter - iter);
+            std::vector<double> cf(chunk), fr(chunk);
+            double c = cfl;
+            for (int k = 0; k < chunk; ++k) { c = uns_host_cfl_cc(&P, iter + 1 + k, c); cf[k] = c; }
+            int done = 0;
+            rc = uns_cc_iterate(h, chunk, cf.data(), iter == 0 ? 1 : 0, fr.data(), &done);
+            for (int k = 0; k < done; ++k) {
+                ++iter;
+                cfl = cf[k];
+                if (iter == 1) fres1 = fr[k];
+                fres = (fres1 >= eps) ? fr[k] / fres1 : fr[k];
+                std::fprintf(fo, "%6d%s%s\n", iter, fort_e(std::log10(fres), 16, 6).c_str(), fort_e(cfl, 16, 6).c_str());
+            }
+            if (rc || done < chunk) break;
+        }
+    }
+    std::fclose(fo);
+    std::string e = rc ? std::string(uns_last_error()) : std::string();
+    uns_cc_destroy(h);
+    if (iters_out) *iters_out = iter;
+    if (fres_out) *fres_out = fres;
+    return rc ? fail(rc, e) : UNS_OK;
+}
+
+int uns_host_nc_main(const char* flo_inp, const char* outdir, int mode, int* iters_out, double* fres_out) {
+    if (!flo_inp || !outdir) return fail(UNS_ERR_ARG, "null argument");
+    uns_params P;
+    std::string grid, err;
+    int rc = read_flo_inp_nc(flo_inp, P, grid, err);
+    if (rc) return fail(rc, err);
+    RawNC raw;
+    MeshNC mesh;
+    if ((rc = read_geometry_nc(join(dir_of(flo_inp), grid), raw, err)) || (rc = geometric_nc(raw, mesh, err))) return fail(rc, err);
+    uns_nc_mesh view = mesh.view();
+    uns_nc_handle* h = nullptr;
+    if ((rc = uns_nc_create(&view, &P, &h))) return fail(rc, uns_last_error());
+    std::string res_path = std::string(outdir) + "/FLO.RES";
+    FILE* fo = std::fopen(res_path.c_str(), "w");
+    if (!fo) { uns_nc_destroy(h); return fail(UNS_ERR_IO, "cannot write " + res_path); }
+    int iter = 0;
+    double fres = 1.0, fres1 = 0.0;
+    while (iter < P.max_iter && fres > P.min_res) {
+        if (mode == 0) {
+            ++iter;
+            double cfl = uns_host_cfl_nc(&P, iter), raw_f, fresi;
+            if ((rc = uns_nc_save_old(h))) break;
+            if (P.time_mode == UNS_TIME_RK3) {
+                for (int irk = 1; irk <= 3 && !rc; ++irk)
+                    if (!(rc = uns_nc_fvresidual(h, cfl))) rc = uns_nc_rk_stage(h, irk);
+            } else {
+                rc = uns_nc_lusgs(h, cfl);
+            }
+            if (rc || (rc = uns_nc_residue(h, &raw_f, &fresi, nullptr))) break;
+            if (iter == 1) fres1 = raw_f;
+            fres = (fres1 != 0.0) ? raw_f / fres1 : raw_f;
+            std::fprintf(fo, "%6d%s%s%s\n", iter, fort_e(std::log10(fres), 16, 6).c_str(),
+                         fort_e(std::log10(fresi), 16, 6).c_str(), fort_e(cfl, 16, 6).c_str());
+        } else {
+            int chunk = std::min(200, P.max_iter - iter);
+            std::vector<double> cf(chunk), fr(chunk), fi(chunk);
+            for (int k = 0; k < chunk; ++k) cf[k] = uns_host_cfl_nc(&P, iter + 1 + k);
+            int done = 0;
+            rc = uns_nc_iterate(h, chunk, cf.data(), iter == 0 ? 1 : 0, fr.data(), fi.data(), &done);
+            for (int k = 0; k < done; ++k) {
+                ++iter;
+                if (iter == 1) fres1 = fr[k];
+                fres = (fres1 != 0.0) ? fr[k] / fres1 : fr[k];
+                std::fprintf(fo, "%6d%s%s%s\n", iter, fort_e(std::log10(fres), 16, 6).c_str(),
+                             fort_e(std::log10(fi[k]), 16, 6).c_str(), fort_e(cf[k], 16, 6).c_str());
+            }
+            if (rc || done < chunk) break;
+        }
+    }
+    std::fclose(fo);
+    std::string e = rc ? std::string(uns_last_error()) : std::string();
+    uns_nc_destroy(h);
+    if (iters_out) *iters_out = iter;
+    if (fres_out) *fres_out = fres;
+    return rc ? fail(rc, e) : UNS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,926 @@
+// host_mesh.cpp -- caller-side mesh handling of the UNSFlow2D drop-in:
+//   * an analytic symmetric-airfoil O-mesh generator (quads split into two
+//     triangles) that writes the same data a CCFVM or NCFVM geometry.inp holds;
+//   * geometry.inp readers / writers for both formats;
+//   * the reference's geometric preprocessing, restated step by step so that
+//     normals, renumbering and connectivity orders match the Fortran driver's
+//     (CCFVM/geometric.F90, NCFVM/geometric.f90).  The hot path depends on these
+//     orders (summation order, LU-SGS sweep order), so each loop keeps the
+//     reference's traversal order.
+//
+// Built with -ffp-contract=off so that x86 and Arm hosts produce identical bits.
+#include "host_mesh.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace unshost {
+
+namespace {
+
+// Symmetric 4-digit thickness distribution with the closed-trailing-edge
+// coefficient (published formula; t = thickness / chord).
+double thickness_4digit(double x, double t) {
+    if (x < 0.0) x = 0.0;
+    if (x > 1.0) x = 1.0;
+    return 5.0 * t *
+           (0.2969 * std::sqrt(x) - 0.1260 * x - 0.3516 * x * x + 0.2843 * x * x * x -
+            0.1036 * x * x * x * x);
+}
+
+// Geometric growth ratio q with d0*(q^n-1)/(q-1) = L (bisection).
+double stretch_ratio(double d0, double L, int n) {
+    if (d0 * n >= L) return 1.0;
+    double lo = 1.0 + 1e-14, hi = 4.0;
+    auto f = [&](double q) { return d0 * (std::pow(q, n) - 1.0) / (q - 1.0) - L; };
+    while (f(hi) < 0.0) hi *= 2.0;
+    for (int it = 0; it < 200; ++it) {
+        double mid = 0.5 * (lo + hi);
+        if (f(mid) < 0.0) lo = mid; else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+struct OGrid {
+    int I, J;
+    std::vector<double> x, y;  // (J+1)*I, index j*I+i
+};
+
+int build_ogrid(const AirfoilSpec& s, OGrid& g, std::string& err) {
+    if (s.ni < 4 || s.nj < 1 || s.thickness <= 0.0 || s.rfar <= 1.0 || s.dwall <= 0.0) {
+        err = "airfoil: bad spec";
+        return UNS_ERR_ARG;
+    }
+    const int I = s.ni, J = s.nj;
+    g.I = I; g.J = J;
+    g.x.assign((size_t)(J + 1) * I, 0.0);
+    g.y.assign((size_t)(J + 1) * I, 0.0);
+    const double pi = 4.0 * std::atan(1.0);
+    for (int i = 0; i < I; ++i) {
+        // Surface parameter: TE (s=0) -> upper surface -> LE (s=pi) -> lower.
+        double sp = 2.0 * pi * (double)i / (double)I;
+        double xw = 0.5 * (1.0 + std::cos(sp));
+        double yw = thickness_4digit(xw, s.thickness);
+        if (sp > pi) yw = -yw;
+        if (i == 0) yw = 0.0;
+        // Farfield point at the same surface parameter: uniform in angle
+        // about mid-chord, so lines of constant i never cross.
+        double xf = 0.5 + s.rfar * std::cos(sp);
+        double yf = s.rfar * std::sin(sp);
+        double L = std::hypot(xf - xw, yf - yw);
+        double q = stretch_ratio(s.dwall, L, J);
+        double qJ = (q == 1.0) ? (double)J : (std::pow(q, J) - 1.0) / (q - 1.0);
+        for (int j = 0; j <= J; ++j) {
+            double frac;
+            if (j == J) frac = 1.0;
+            else if (q == 1.0) frac = (double)j / (double)J;
+            else frac = ((std::pow(q, j) - 1.0) / (q - 1.0)) / qJ;
+            g.x[(size_t)j * I + i] = xw + (xf - xw) * frac;
+            g.y[(size_t)j * I + i] = yw + (yf - yw) * frac;
+        }
+    }
+    return UNS_OK;
+}
+
+inline double tri_area2(double ax, double ay, double bx, double by, double cx, double cy) {
+    return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+}
+
+// Triangles and edges of the split O-grid.  Quad (i,j) has corners
+// a=(i,j) b=(i+1,j) c=(i+1,j+1) d=(i,j+1); T1=(a,b,c) is cell 2q, T2=(a,c,d)
+// is cell 2q+1 with q=j*I+i.
+struct TriTopo {
+    int nop, noc;
+    std::vector<double> px, py, cx, cy, cv;
+    std::vector<int> pbc;
+    struct Edge { int p1, p2, c1, c2, bc; };
+    std::vector<Edge> interior, wall, farfield;
+};
+
+int build_topology(const OGrid& g, TriTopo& t, std::string& err) {
+    const int I = g.I, J = g.J;
+    auto pid = [&](int i, int j) { return j * I + ((i % I) + I) % I; };
+    t.nop = I * (J + 1);
+    t.noc = 2 * I * J;
+    t.px = g.x; t.py = g.y;
+    t.pbc.assign(t.nop, 0);
+    for (int i = 0; i < I; ++i) { t.pbc[pid(i, 0)] = 1001; t.pbc[pid(i, J)] = 2001; }
+    t.cx.resize(t.noc); t.cy.resize(t.noc); t.cv.resize(t.noc);
+    for (int j = 0; j < J; ++j)
+        for (int i = 0; i < I; ++i) {
+            int a = pid(i, j), b = pid(i + 1, j), c = pid(i + 1, j + 1), d = pid(i, j + 1);
+            int q = j * I + i;
+            const int tri[2][3] = {{a, b, c}, {a, c, d}};
+            for (int k = 0; k < 2; ++k) {
+                int p0 = tri[k][0], p1 = tri[k][1], p2 = tri[k][2];
+                double ar = 0.5 * std::fabs(tri_area2(t.px[p0], t.py[p0], t.px[p1], t.py[p1], t.px[p2], t.py[p2]));
+                if (!(ar > 0.0)) { err = "airfoil: degenerate triangle"; return UNS_ERR_MESH; }
+                t.cv[2 * q + k] = ar;
+                t.cx[2 * q + k] = (t.px[p0] + t.px[p1] + t.px[p2]) / 3.0;
+                t.cy[2 * q + k] = (t.py[p0] + t.py[p1] + t.py[p2]) / 3.0;
+            }
+            // Orientation consistency: both triangles must have the same sign.
+            double s1 = tri_area2(t.px[a], t.py[a], t.px[b], t.py[b], t.px[c], t.py[c]);
+            double s2 = tri_area2(t.px[a], t.py[a], t.px[c], t.py[c], t.px[d], t.py[d]);
+            if (!(s1 * s2 > 0.0)) { err = "airfoil: folded quad"; return UNS_ERR_MESH; }
+        }
+    auto T1 = [&](int i, int j) { return 2 * (j * I + ((i % I) + I) % I); };
+    auto T2 = [&](int i, int j) { return 2 * (j * I + ((i % I) + I) % I) + 1; };
+    for (int j = 0; j < J; ++j)
+        for (int i = 0; i < I; ++i) {
+            if (j >= 1) t.interior.push_back({pid(i, j), pid(i + 1, j), T1(i, j), T2(i, j - 1), 0});
+            t.interior.push_back({pid(i, j), pid(i, j + 1), T2(i, j), T1(i - 1, j), 0});
+            t.interior.push_back({pid(i, j), pid(i + 1, j + 1), T1(i, j), T2(i, j), 0});
+        }
+    for (int i = 0; i < I; ++i) t.wall.push_back({pid(i, 0), pid(i + 1, 0), T1(i, 0), -1, 1001});
+    for (int i = 0; i < I; ++i) t.farfield.push_back({pid(i, J), pid(i + 1, J), T2(i, J - 1), -1, 2001});
+    // Boundary edges: p1 -> p2 with the interior cell on the left, so the
+    // file normal (dy,-dx) points out of the domain.
+    auto orient = [&](TriTopo::Edge& e) {
+        double s = tri_area2(t.px[e.p1], t.py[e.p1], t.px[e.p2], t.py[e.p2], t.cx[e.c1], t.cy[e.c1]);
+        if (s < 0.0) std::swap(e.p1, e.p2);
+    };
+    for (auto& e : t.wall) orient(e);
+    for (auto& e : t.farfield) orient(e);
+    // Interior edges: c1 (`in`) on the left of p1 -> p2, c2 (`out`) on the
+    // right.  CCFVM's cell_face_norm (geometric.F90:90-102) "repairs" the
+    // other orientation by swapping the cells and the end points together,
+    // which leaves such a face mis-oriented, so its meshes must already be
+    // written this way.
+    for (auto& e : t.interior) orient(e);
+    return UNS_OK;
+}
+
+}  // namespace
+
+int gen_airfoil_cc(const AirfoilSpec& s, RawCC& m, std::string& err) {
+    OGrid g;
+    int rc = build_ogrid(s, g, err);
+    if (rc) return rc;
+    TriTopo t;
+    rc = build_topology(g, t, err);
+    if (rc) return rc;
+    m = RawCC();
+    m.nop = t.nop; m.noc = t.noc;
+    m.px = t.px; m.py = t.py; m.pbc = t.pbc;
+    m.cx = t.cx; m.cy = t.cy; m.cv = t.cv;
+    m.nfi = (int)t.interior.size();
+    m.nbf = (int)(t.wall.size() + t.farfield.size());
+    auto push = [&](const TriTopo::Edge& e, bool bnd) {
+        m.fp1.push_back(e.p1); m.fp2.push_back(e.p2);
+        m.fin.push_back(e.c1); m.fout.push_back(bnd ? -1 : e.c2);
+        m.fbc.push_back(e.bc);
+        m.fnx.push_back(t.py[e.p2] - t.py[e.p1]);
+        m.fny.push_back(-(t.px[e.p2] - t.px[e.p1]));
+    };
+    for (auto& e : t.interior) push(e, false);
+    for (auto& e : t.wall) push(e, true);
+    for (auto& e : t.farfield) push(e, true);
+    return UNS_OK;
+}
+
+int gen_airfoil_nc(const AirfoilSpec& s, RawNC& m, std::string& err) {
+    OGrid g;
+    int rc = build_ogrid(s, g, err);
+    if (rc) return rc;
+    TriTopo t;
+    rc = build_topology(g, t, err);
+    if (rc) return rc;
+    m = RawNC();
+    m.nop = t.nop; m.noc = t.noc;
+    m.px = t.px; m.py = t.py; m.pbc = t.pbc;
+    m.cx = t.cx; m.cy = t.cy; m.cv = t.cv;
+    auto push = [&](int p1, int p2, int in, int out, int bc) {
+        m.fp1.push_back(p1); m.fp2.push_back(p2);
+        m.fin.push_back(in); m.fout.push_back(out); m.fbc.push_back(bc);
+        m.fsx.push_back(t.py[p2] - t.py[p1]);
+        m.fsy.push_back(-(t.px[p2] - t.px[p1]));
+    };
+    for (auto& e : t.interior) push(e.p1, e.p2, e.c1, e.c2, 0);
+    // Same convention as MeshGen/SolverInputMESH.f90:106-115: the wall edge
+    // keeps its cell as `in`, the farfield edge as `out`.
+    for (auto& e : t.wall) push(e.p1, e.p2, e.c1, -1, 1001);
+    // The farfield cell is `out`, so it has to sit on the right of p1 -> p2.
+    for (auto& e : t.farfield) push(e.p2, e.p1, -1, e.c1, 2001);
+    m.nof = (int)m.fp1.size();
+    return UNS_OK;
+}
+
+// ---------------------------------------------------------------- file I/O
+namespace {
+struct Tok {
+    std::ifstream f;
+    std::string line;
+    std::istringstream ss;
+    bool next_line() {
+        if (!std::getline(f, line)) return false;
+        ss.clear(); ss.str(line);
+        return true;
+    }
+};
+}  // namespace
+
+int read_geometry_cc(const std::string& path, RawCC& m, std::string& err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open " + path; return UNS_ERR_IO; }
+    m = RawCC();
+    if (!(f >> m.nop >> m.noc >> m.nfi >> m.nbf) || m.nop <= 0 || m.noc <= 0 || m.nfi < 0 || m.nbf < 0) {
+        err = "bad geometry header"; return UNS_ERR_IO;
+    }
+    m.px.resize(m.nop); m.py.resize(m.nop); m.pbc.resize(m.nop);
+    for (int i = 0; i < m.nop; ++i) { int id; if (!(f >> id >> m.px[i] >> m.py[i] >> m.pbc[i])) { err = "truncated points"; return UNS_ERR_IO; } }
+    m.cx.resize(m.noc); m.cy.resize(m.noc); m.cv.resize(m.noc);
+    for (int i = 0; i < m.noc; ++i) { int id; if (!(f >> id >> m.cx[i] >> m.cy[i] >> m.cv[i])) { err = "truncated cells"; return UNS_ERR_IO; } }
+    int nf = m.nfi + m.nbf;
+    m.fp1.resize(nf); m.fp2.resize(nf); m.fin.resize(nf); m.fout.assign(nf, -1);
+    m.fbc.resize(nf); m.fnx.resize(nf); m.fny.resize(nf);
+    for (int i = 0; i < m.nfi; ++i) {
+        int id;
+        if (!(f >> id >> m.fp1[i] >> m.fp2[i] >> m.fin[i] >> m.fout[i] >> m.fnx[i] >> m.fny[i] >> m.fbc[i])) { err = "truncated faces"; return UNS_ERR_IO; }
+        m.fp1[i]--; m.fp2[i]--; m.fin[i]--; m.fout[i]--;
+    }
+    for (int i = m.nfi; i < nf; ++i) {
+        int id;
+        if (!(f >> id >> m.fp1[i] >> m.fp2[i] >> m.fin[i] >> m.fnx[i] >> m.fny[i] >> m.fbc[i])) { err = "truncated boundary faces"; return UNS_ERR_IO; }
+        m.fp1[i]--; m.fp2[i]--; m.fin[i]--;
+    }
+    for (int i = 0; i < nf; ++i) {
+        if (m.fp1[i] < 0 || m.fp1[i] >= m.nop || m.fp2[i] < 0 || m.fp2[i] >= m.nop) { err = "face point out of range"; return UNS_ERR_MESH; }
+        if (m.fin[i] < -1 || m.fin[i] >= m.noc) { err = "face cell out of range"; return UNS_ERR_MESH; }
+        if (i < m.nfi && (m.fout[i] < -1 || m.fout[i] >= m.noc)) { err = "face cell out of range"; return UNS_ERR_MESH; }
+    }
+    return UNS_OK;
+}
+
+int write_geometry_cc(const std::string& path, const RawCC& m, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) { err = "cannot write " + path; return UNS_ERR_IO; }
+    std::fprintf(f, "%d %d %d %d\n", m.nop, m.noc, m.nfi, m.nbf);
+    for (int i = 0; i < m.nop; ++i) std::fprintf(f, "%d %.17g %.17g %d\n", i + 1, m.px[i], m.py[i], m.pbc[i]);
+    for (int i = 0; i < m.noc; ++i) std::fprintf(f, "%d %.17g %.17g %.17g\n", i + 1, m.cx[i], m.cy[i], m.cv[i]);
+    for (int i = 0; i < m.nfi; ++i)
+        std::fprintf(f, "%d %d %d %d %d %.17g %.17g %d\n", i + 1, m.fp1[i] + 1, m.fp2[i] + 1, m.fin[i] + 1, m.fout[i] + 1, m.fnx[i], m.fny[i], m.fbc[i]);
+    for (int i = m.nfi; i < m.nfi + m.nbf; ++i)
+        std::fprintf(f, "%d %d %d %d %.17g %.17g %d\n", i + 1, m.fp1[i] + 1, m.fp2[i] + 1, m.fin[i] + 1, m.fnx[i], m.fny[i], m.fbc[i]);
+    std::fclose(f);
+    return UNS_OK;
+}
+
+int read_geometry_nc(const std::string& path, RawNC& m, std::string& err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open " + path; return UNS_ERR_IO; }
+    m = RawNC();
+    if (!(f >> m.nop >> m.noc >> m.nof) || m.nop <= 0 || m.noc <= 0 || m.nof <= 0) { err = "bad geometry header"; return UNS_ERR_IO; }
+    m.px.resize(m.nop); m.py.resize(m.nop); m.pbc.resize(m.nop);
+    for (int i = 0; i < m.nop; ++i) { int id; if (!(f >> id >> m.px[i] >> m.py[i] >> m.pbc[i])) { err = "truncated points"; return UNS_ERR_IO; } }
+    m.cx.resize(m.noc); m.cy.resize(m.noc); m.cv.resize(m.noc);
+    for (int i = 0; i < m.noc; ++i) { int id; if (!(f >> id >> m.cx[i] >> m.cy[i] >> m.cv[i])) { err = "truncated cells"; return UNS_ERR_IO; } }
+    m.fp1.resize(m.nof); m.fp2.resize(m.nof); m.fin.resize(m.nof); m.fout.resize(m.nof);
+    m.fbc.resize(m.nof); m.fsx.resize(m.nof); m.fsy.resize(m.nof);
+    for (int i = 0; i < m.nof; ++i) {
+        int id;
+        if (!(f >> id >> m.fp1[i] >> m.fp2[i] >> m.fin[i] >> m.fout[i] >> m.fsx[i] >> m.fsy[i] >> m.fbc[i])) { err = "truncated faces"; return UNS_ERR_IO; }
+        m.fp1[i]--; m.fp2[i]--; m.fin[i]--; m.fout[i]--;
+        if (m.fp1[i] < 0 || m.fp1[i] >= m.nop || m.fp2[i] < 0 || m.fp2[i] >= m.nop) { err = "face point out of range"; return UNS_ERR_MESH; }
+        if (m.fin[i] < -1 || m.fin[i] >= m.noc || m.fout[i] < -1 || m.fout[i] >= m.noc) { err = "face cell out of range"; return UNS_ERR_MESH; }
+    }
+    return UNS_OK;
+}
+
+int write_geometry_nc(const std::string& path, const RawNC& m, std::string& err) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) { err = "cannot write " + path; return UNS_ERR_IO; }
+    std::fprintf(f, "%d %d %d\n", m.nop, m.noc, m.nof);
+    for (int i = 0; i < m.nop; ++i) std::fprintf(f, "%d %.17g %.17g %d\n", i + 1, m.px[i], m.py[i], m.pbc[i]);
+    for (int i = 0; i < m.noc; ++i) std::fprintf(f, "%d %.17g %.17g %.17g\n", i + 1, m.cx[i], m.cy[i], m.cv[i]);
+    for (int i = 0; i < m.nof; ++i)
+        std::fprintf(f, "%d %d %d %d %d %.17g %.17g %d\n", i + 1, m.fp1[i] + 1, m.fp2[i] + 1, m.fin[i] + 1, m.fout[i] + 1, m.fsx[i], m.fsy[i], m.fbc[i]);
+    std::fclose(f);
+    return UNS_OK;
+}
+
+// ------------------------------------------------------- CC geometric
+namespace {
+
+// dotprod (CCFVM/solution.F90:576-597): cosine between the unit normal
+// (dy,-dx)/ds of p1->p2 and the unit vector from p1 to (xc,yc).
+double dotprod(const std::vector<double>& px, const std::vector<double>& py, int n1, int n2, double xc, double yc) {
+    double x1 = px[n1], y1 = py[n1], x2 = px[n2], y2 = py[n2];
+    double dx = x2 - x1, dy = y2 - y1;
+    double ds = std::sqrt(dx * dx + dy * dy);
+    double nx = dy / ds, ny = -dx / ds;
+    dx = xc - x1; dy = yc - y1;
+    ds = std::sqrt(dx * dx + dy * dy);
+    double rx = dx / ds, ry = dy / ds;
+    return rx * nx + ry * ny;
+}
+
+// triarea (CCFVM/geometric.F90:676-693): polygon area by the trapezoid sum.
+bool triarea(const double xy[2][3], double& area) {
+    area = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        int ip1 = (i == 2) ? 0 : i + 1;
+        double dx = 0.5 * (xy[0][ip1] + xy[0][i]);
+        double dy = xy[1][ip1] - xy[1][i];
+        area = area + dx * dy;
+    }
+    return area > 0.0;
+}
+
+void append_unique(std::vector<int>& v, int x) {
+    for (int y : v) if (y == x) return;
+    v.push_back(x);
+}
+
+template <class VV>
+void to_csr(const VV& lists, std::vector<int>& off, std::vector<int>& idx) {
+    off.assign(lists.size() + 1, 0);
+    for (size_t i = 0; i < lists.size(); ++i) off[i + 1] = off[i] + (int)lists[i].size();
+    idx.resize(off.back());
+    for (size_t i = 0; i < lists.size(); ++i) std::copy(lists[i].begin(), lists[i].end(), idx.begin() + off[i]);
+}
+
+}  // namespace
+
+int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
+    m = MeshCC();
+    const int nop = raw.nop, noc = raw.noc, nfi = raw.nfi, nbf = raw.nbf;
+    const int nof = nfi + nbf, ntot = noc + nbf;
+    m.nop = nop; m.noc = noc; m.nfi = nfi; m.nbf = nbf;
+    m.px = raw.px; m.py = raw.py; m.pbc = raw.pbc;
+    m.cx.assign(ntot, 0.0); m.cy.assign(ntot, 0.0);
+    std::vector<double> cv(raw.cv);
+    for (int i = 0; i < noc; ++i) { m.cx[i] = raw.cx[i]; m.cy[i] = raw.cy[i]; }
+    m.fp1 = raw.fp1; m.fp2 = raw.fp2; m.fin = raw.fin; m.fout = raw.fout; m.fbc = raw.fbc;
+    m.fnx = raw.fnx; m.fny = raw.fny;
+    const auto& px = m.px;
+    const auto& py = m.py;
+
+    // read_grid ghost cells (CCFVM/read_input.F90:179-203): ghost k of
+    // boundary face nfi+k is the mirror image of its cell's centroid.
+    for (int k = 0; k < nbf; ++k) {
+        int i = nfi + k;
+        int in = m.fin[i];
+        m.fout[i] = noc + k;
+        int p1 = m.fp1[i], p2 = m.fp2[i];
+        double sx = px[p1], sy = py[p1], ex = px[p2], ey = py[p2];
+        double qx = m.cx[in], qy = m.cy[in];
+        double dx = ex - sx, dy = ey - sy;
+        double x = sx - qx, y = sy - qy;
+        double r = 1.0 / (dx * dx + dy * dy);
+        m.cx[noc + k] = qx + 2.0 * (x - x * dx * dx * r - y * dx * dy * r);
+        m.cy[noc + k] = qy + 2.0 * (y - y * dy * dy * r - x * dx * dy * r);
+    }
+    // geometric.F90:9-27 sanity checks.
+    for (int i = 0; i < nfi; ++i)
+        if (m.fin[i] < 0 || m.fout[i] < 0) { err = "Inside faces in/out==0"; return UNS_ERR_MESH; }
+    for (int i = nfi; i < nof; ++i)
+        if (m.fin[i] < 0) { err = "BC faces in/out==0"; return UNS_ERR_MESH; }
+
+    // cell_face_norm (geometric.F90:62-198).
+    m.fcx.assign(nof, 0.0); m.fcy.assign(nof, 0.0);
+    for (int i = 0; i < nfi; ++i) {
+        int in = m.fin[i], out = m.fout[i], p1 = m.fp1[i], p2 = m.fp2[i];
+        double xc = m.cx[out], yc = m.cy[out];
+        double x1 = px[p1], y1 = py[p1], x2 = px[p2], y2 = py[p2];
+        double dx = x2 - x1, dy = y2 - y1;
+        m.fnx[i] = dy; m.fny[i] = -dx;
+        double check = dotprod(px, py, p1, p2, xc, yc);
+        if (check < 0.0) {
+            m.fin[i] = out; m.fout[i] = in; m.fp1[i] = p2; m.fp2[i] = p1;
+            x1 = px[p2]; y1 = py[p2]; x2 = px[p1]; y2 = py[p1];
+            dx = x2 - x1; dy = y2 - y1;
+            m.fnx[i] = dy; m.fny[i] = -dx;
+        }
+        m.fcx[i] = 0.5 * (px[p1] + px[p2]);
+        m.fcy[i] = 0.5 * (py[p1] + py[p2]);
+    }
+    for (int i = nfi; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i];
+        if (m.fbc[i] == 2001 || m.fbc[i] == 1001) {
+            double check = dotprod(px, py, p1, p2, m.cx[in], m.cy[in]);
+            if (check > 0.0) {
+                m.fp1[i] = p2; m.fp2[i] = p1;
+                double x1 = px[p2], y1 = py[p2], x2 = px[p1], y2 = py[p1];
+                double dx = x2 - x1, dy = y2 - y1;
+                m.fnx[i] = dy; m.fny[i] = -dx;
+            }
+        }
+        m.fcx[i] = 0.5 * (px[p1] + px[p2]);
+        m.fcy[i] = 0.5 * (py[p1] + py[p2]);
+    }
+    m.farea.assign(nof, 0.0);
+    for (int i = 0; i < nof; ++i) {
+        double dx = m.fnx[i], dy = m.fny[i];
+        m.farea[i] = std::sqrt(dx * dx + dy * dy);
+        m.fnx[i] = m.fnx[i] / m.farea[i];
+        m.fny[i] = m.fny[i] / m.farea[i];
+    }
+
+    // cell_2_cell (geometric.F90:200-245): interior faces only, face order.
+    std::vector<std::vector<int>> c2c(noc);
+    for (int i = 0; i < nfi; ++i) {
+        int in = m.fin[i], out = m.fout[i];
+        append_unique(c2c[in], out);
+        append_unique(c2c[out], in);
+    }
+
+    // renumber (geometric.F90:247-356): breadth-first from cell 1.
+    std::vector<int> oldnum(noc, -1), newnum(noc, -1);
+    int c = 0;
+    oldnum[0] = 0; newnum[0] = 0;
+    for (int i = 0; i < noc; ++i) {
+        int it = oldnum[i];
+        if (it < 0) { err = "renumber: mesh is not connected"; return UNS_ERR_MESH; }
+        for (int t1 : c2c[it])
+            if (t1 >= 0 && t1 < noc && newnum[t1] < 0) { ++c; oldnum[c] = t1; newnum[t1] = c; }
+    }
+    if (c + 1 != noc) { err = "renumber: count does not match no. of cells"; return UNS_ERR_MESH; }
+    for (int i = 0; i < nof; ++i) {
+        if (m.fin[i] >= 0 && m.fin[i] < noc) m.fin[i] = newnum[m.fin[i]];
+        if (m.fout[i] >= 0 && m.fout[i] < noc) m.fout[i] = newnum[m.fout[i]];
+    }
+    {
+        std::vector<double> ncx(m.cx), ncy(m.cy), ncv(noc);
+        std::vector<std::vector<int>> nc2c(noc);
+        for (int i = 0; i < noc; ++i) {
+            int it = oldnum[i];
+            ncx[i] = m.cx[it]; ncy[i] = m.cy[it]; ncv[i] = cv[it];
+            for (int t1 : c2c[it]) nc2c[i].push_back((t1 >= 0 && t1 < noc) ? newnum[t1] : t1);
+        }
+        m.cx.swap(ncx); m.cy.swap(ncy); cv.swap(ncv); c2c.swap(nc2c);
+    }
+    m.newnum = newnum;
+    m.cv = cv;
+    m.nc2c.resize(noc);
+    for (int i = 0; i < noc; ++i) m.nc2c[i] = (int)c2c[i].size();
+    to_csr(c2c, m.c2c_off, m.c2c);
+
+    // cell_2_face (geometric.F90:425-457).
+    std::vector<std::vector<int>> c2f(noc);
+    for (int i = 0; i < nof; ++i) {
+        int in = m.fin[i], out = m.fout[i];
+        if (in >= 0) c2f[in].push_back(i);
+        if (out >= 0 && out < noc) c2f[out].push_back(i);
+    }
+
+    // vertex_2_cell (geometric.F90:459-531): ghosts included.
+    std::vector<std::vector<int>> v2c(nop);
+    for (int i = 0; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
+        if (in < 0) { err = "v2c:in"; return UNS_ERR_MESH; }
+        append_unique(v2c[p1], in);
+        append_unique(v2c[p2], in);
+        if (out < 0) { err = "v2c:out"; return UNS_ERR_MESH; }
+        append_unique(v2c[p1], out);
+        append_unique(v2c[p2], out);
+    }
+
+    // cell_2_vertex (geometric.F90:533-616): walks the faces of each cell and
+    // reorders its c2f list as it goes (LU-SGS later loops over c2f).
+    std::vector<std::vector<int>> c2v(noc);
+    for (int i = 0; i < noc; ++i) {
+        double xc = m.cx[i], yc = m.cy[i];
+        auto& F = c2f[i];
+        auto& V = c2v[i];
+        int nf = (int)F.size();
+        int p1 = m.fp1[F[0]], p2 = m.fp2[F[0]];
+        if (dotprod(px, py, p1, p2, xc, yc) < 0.0) { V.push_back(p1); V.push_back(p2); }
+        else { V.push_back(p2); V.push_back(p1); }
+        for (int k = 1; k < nf - 1; ++k) {
+            int last = V.back();
+            for (int j = k; j < nf; ++j) {
+                int m1 = m.fp1[F[j]], m2 = m.fp2[F[j]];
+                if (m1 == last || m2 == last) {
+                    if (dotprod(px, py, m1, m2, xc, yc) < 0.0) V.push_back(m2);
+                    else V.push_back(m1);
+                    std::swap(F[j], F[k]);
+                }
+            }
+        }
+        V.push_back(V[0]);
+    }
+    to_csr(c2f, m.c2f_off, m.c2f);
+    to_csr(c2v, m.c2v_off, m.c2v);
+
+    // face_co_volume (geometric.F90:619-674).
+    m.fcov.assign(nof, 0.0);
+    m.cov.assign(ntot, 0.0);
+    for (int i = 0; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
+        double xy[2][3] = {{px[p1], px[p2], m.cx[in]}, {py[p1], py[p2], m.cy[in]}};
+        double a1, a2;
+        if (!triarea(xy, a1)) { err = "geom,triarea, -ve area"; return UNS_ERR_MESH; }
+        double xy2[2][3] = {{px[p1], m.cx[out], px[p2]}, {py[p1], m.cy[out], py[p2]}};
+        if (!triarea(xy2, a2)) { err = "geom,triarea, -ve area"; return UNS_ERR_MESH; }
+        m.fcov[i] = a1;
+        m.fcov[i] = m.fcov[i] + a2;
+        if (m.fcov[i] <= 0.0) { err = "-ve face co-volume"; return UNS_ERR_MESH; }
+        m.cov[in] = m.cov[in] + m.fcov[i];
+        m.cov[out] = m.cov[out] + m.fcov[i];
+    }
+    for (int i = 0; i < noc; ++i)
+        if (m.cov[i] <= 0.0) { err = "-ve cell co-volume"; return UNS_ERR_MESH; }
+
+    // LSQR_Coeff (geometric.F90:898-960), ds = 1.
+    m.r11.assign(noc, 0.0); m.r12.assign(noc, 0.0); m.r22.assign(noc, 0.0);
+    std::vector<double> R11(ntot, 0.0), R12(ntot, 0.0), R22(ntot, 0.0);
+    const double ds = 1.0;
+    for (int i = 0; i < nfi; ++i) {
+        int in = m.fin[i], out = m.fout[i];
+        double xi = m.cx[in], yi = m.cy[in], xo = m.cx[out], yo = m.cy[out];
+        double dx = xo - xi, dy = yo - yi;
+        R11[in] = R11[in] + ds * dx * dx; R12[in] = R12[in] + ds * dx * dy; R22[in] = R22[in] + ds * dy * dy;
+        dx = xi - xo; dy = yi - yo;
+        R11[out] = R11[out] + ds * dx * dx; R12[out] = R12[out] + ds * dx * dy; R22[out] = R22[out] + ds * dy * dy;
+    }
+    for (int i = nfi; i < nof; ++i) {
+        int in = m.fin[i], out = m.fout[i];
+        double dx = m.cx[out] - m.cx[in], dy = m.cy[out] - m.cy[in];
+        R11[in] = R11[in] + ds * dx * dx; R12[in] = R12[in] + ds * dx * dy; R22[in] = R22[in] + ds * dy * dy;
+    }
+    for (int i = 0; i < noc; ++i) {
+        double r11 = std::sqrt(R11[i]);
+        double r12 = R12[i] / r11;
+        m.r11[i] = r11; m.r12[i] = r12;
+        m.r22[i] = std::sqrt(R22[i] - r12 * r12);
+    }
+
+    // pseudo_Laplacian (geometric.F90:962-1013).
+    to_csr(v2c, m.v2c_off, m.v2c);
+    m.v2c_wt.assign(m.v2c.size(), 0.0);
+    for (int i = 0; i < nop; ++i) {
+        double ixx = 0, iyy = 0, ixy = 0, rx = 0, ry = 0;
+        for (int k = m.v2c_off[i]; k < m.v2c_off[i + 1]; ++k) {
+            int cc = m.v2c[k];
+            double dx = m.cx[cc] - px[i], dy = m.cy[cc] - py[i];
+            rx = rx + dx; ry = ry + dy;
+            ixx = ixx + dx * dx; iyy = iyy + dy * dy; ixy = ixy + dx * dy;
+        }
+        double det = ixx * iyy - ixy * ixy;
+        if (det < 0.0) { err = "Determinant -ve @ pseudo_Laplacian"; return UNS_ERR_MESH; }
+        double gx = (ixy * ry - iyy * rx) / det;
+        double gy = (ixy * rx - ixx * ry) / det;
+        for (int k = m.v2c_off[i]; k < m.v2c_off[i + 1]; ++k) {
+            int cc = m.v2c[k];
+            double dx = m.cx[cc] - px[i], dy = m.cy[cc] - py[i];
+            m.v2c_wt[k] = 1.0 + gx * dx + gy * dy;
+        }
+    }
+    return UNS_OK;
+}
+
+uns_cc_mesh MeshCC::view() const {
+    uns_cc_mesh v;
+    std::memset(&v, 0, sizeof(v));
+    v.nop = nop; v.noc = noc; v.nfi = nfi; v.nbf = nbf;
+    v.px = px.data(); v.py = py.data();
+    v.cx = cx.data(); v.cy = cy.data();
+    v.cv = cv.data(); v.cov = cov.data();
+    v.fp1 = fp1.data(); v.fp2 = fp2.data(); v.fin = fin.data(); v.fout = fout.data(); v.fbc = fbc.data();
+    v.fnx = fnx.data(); v.fny = fny.data(); v.farea = farea.data(); v.fcx = fcx.data(); v.fcy = fcy.data();
+    v.r11 = r11.data(); v.r12 = r12.data(); v.r22 = r22.data();
+    v.nc2c = nc2c.data();
+    v.c2f_off = c2f_off.data(); v.c2f = c2f.data();
+    v.v2c_off = v2c_off.data(); v.v2c = v2c.data(); v.v2c_wt = v2c_wt.data();
+    return v;
+}
+
+// ------------------------------------------------------- NC geometric
+int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
+    m = MeshNC();
+    const int nop = raw.nop, noc = raw.noc, nof = raw.nof;
+    m.nop = nop; m.noc = noc; m.nof = nof;
+    m.px = raw.px; m.py = raw.py; m.pbc = raw.pbc;
+    m.cx = raw.cx; m.cy = raw.cy; m.ccv = raw.cv;
+    m.fp1 = raw.fp1; m.fp2 = raw.fp2; m.fin = raw.fin; m.fout = raw.fout; m.fbc = raw.fbc;
+
+    // vertex_2_vertex (NCFVM/geometric.f90:52-81): face order, no dedup.
+    std::vector<std::vector<int>> v2v(nop);
+    for (int i = 0; i < nof; ++i) {
+        v2v[m.fp1[i]].push_back(m.fp2[i]);
+        v2v[m.fp2[i]].push_back(m.fp1[i]);
+    }
+    // renumber (NCFVM/geometric.f90:85-180): breadth-first from node 1.
+    std::vector<int> oldnum(nop, -1), newnum(nop, -1);
+    int c = 0;
+    oldnum[0] = 0; newnum[0] = 0;
+    for (int i = 0; i < nop; ++i) {
+        int it = oldnum[i];
+        if (it < 0) { err = "renumber: mesh is not connected"; return UNS_ERR_MESH; }
+        for (int t1 : v2v[it])
+            if (t1 >= 0 && newnum[t1] < 0) { ++c; oldnum[c] = t1; newnum[t1] = c; }
+    }
+    if (c + 1 != nop) { err = "renumber: count does not match nt"; return UNS_ERR_MESH; }
+    {
+        std::vector<double> nx(nop), ny(nop);
+        std::vector<int> nbc(nop);
+        std::vector<std::vector<int>> nv(nop);
+        for (int i = 0; i < nop; ++i) {
+            int it = oldnum[i];
+            nx[i] = raw.px[it]; ny[i] = raw.py[it]; nbc[i] = raw.pbc[it];
+            for (int t1 : v2v[it]) nv[i].push_back(t1 >= 0 ? newnum[t1] : t1);
+        }
+        m.px.swap(nx); m.py.swap(ny); m.pbc.swap(nbc); v2v.swap(nv);
+    }
+    for (int i = 0; i < nof; ++i) { m.fp1[i] = newnum[m.fp1[i]]; m.fp2[i] = newnum[m.fp2[i]]; }
+    m.newnum = newnum;
+    const auto& px = m.px;
+    const auto& py = m.py;
+
+    // cell_face_norm_c2f_dist (NCFVM/geometric.f90:184-345): dual-face normal
+    // = sum of the two median segments, each oriented along p1->p2.
+    m.fnx.assign(nof, 0.0); m.fny.assign(nof, 0.0); m.farea.assign(nof, 0.0);
+    m.fcx.assign(nof, 0.0); m.fcy.assign(nof, 0.0);
+    for (int i = 0; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i];
+        double xm = 0.5 * (px[p1] + px[p2]), ym = 0.5 * (py[p1] + py[p2]);
+        double dx = (px[p2] - px[p1]), dy = (py[p2] - py[p1]);
+        m.fcx[i] = xm; m.fcy[i] = ym;
+        int in = m.fin[i], out = m.fout[i];
+        if (in >= 0) {
+            double xc = m.cx[in], yc = m.cy[in];
+            double sx = yc - ym, sy = -(xc - xm);
+            double vprod = sx * dx + sy * dy;
+            if (vprod < 0.0) { sx = -sx; sy = -sy; }
+            m.fnx[i] = sx; m.fny[i] = sy;
+        }
+        if (out >= 0) {
+            double xc = m.cx[out], yc = m.cy[out];
+            double sx = (ym - yc), sy = -(xm - xc);
+            double vprod = sx * dx + sy * dy;
+            if (vprod < 0.0) { sx = -sx; sy = -sy; }
+            m.fnx[i] = m.fnx[i] + sx; m.fny[i] = m.fny[i] + sy;
+        }
+    }
+    for (int i = 0; i < nof; ++i) {
+        double sx = m.fnx[i], sy = m.fny[i];
+        double ds = std::sqrt(sx * sx + sy * sy);
+        m.fnx[i] = m.fnx[i] / ds; m.fny[i] = m.fny[i] / ds;
+        m.farea[i] = ds;
+    }
+    // Dual volumes (NCFVM/geometric.f90:263-315).
+    m.cv.assign(nop, 0.0);
+    for (int i = 0; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
+        double xm = m.fcx[i], ym = m.fcy[i];
+        double dx, dy;
+        if (in >= 0) {
+            double xc = m.cx[in], yc = m.cy[in];
+            dy = yc - ym; dx = 0.5 * (xc + xm);
+            m.cv[p1] = m.cv[p1] + dx * dy; m.cv[p2] = m.cv[p2] - dx * dy;
+        } else {
+            double xc = px[p1], yc = py[p1];
+            dy = yc - ym; dx = 0.5 * (xc + xm);
+            m.cv[p1] = m.cv[p1] + dx * dy;
+            xc = px[p2]; yc = py[p2];
+            dy = yc - ym; dx = 0.5 * (xc + xm);
+            m.cv[p2] = m.cv[p2] - dx * dy;
+        }
+        if (out >= 0) {
+            double xc = m.cx[out], yc = m.cy[out];
+            dy = ym - yc; dx = 0.5 * (xc + xm);
+            m.cv[p1] = m.cv[p1] + dx * dy; m.cv[p2] = m.cv[p2] - dx * dy;
+        } else {
+            double xc = px[p1], yc = py[p1];
+            dy = ym - yc; dx = 0.5 * (xc + xm);
+            m.cv[p1] = m.cv[p1] + dx * dy;
+            xc = px[p2]; yc = py[p2];
+            dy = ym - yc; dx = 0.5 * (xc + xm);
+            m.cv[p2] = m.cv[p2] - dx * dy;
+        }
+    }
+    for (int i = 0; i < nop; ++i)
+        if (!(m.cv[i] > 0.0)) { err = "non-positive dual volume"; return UNS_ERR_MESH; }
+
+    // vertex_2_face (NCFVM/geometric.f90:347-379): face order.
+    std::vector<std::vector<int>> v2f(nop);
+    for (int i = 0; i < nof; ++i) { v2f[m.fp1[i]].push_back(i); v2f[m.fp2[i]].push_back(i); }
+
+    // face_co_volume (NCFVM/geometric.f90:657-758): consistency check only.
+    m.fcov.assign(nof, 0.0);
+    for (int i = 0; i < nof; ++i) {
+        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
+        double cov = 0.0;
+        auto seg = [&](double x1, double y1, double x2, double y2) { cov = cov + 0.5 * (x2 + x1) * (y2 - y1); };
+        if (in >= 0 && out >= 0) {
+            seg(px[p1], py[p1], m.cx[out], m.cy[out]);
+            seg(m.cx[out], m.cy[out], px[p2], py[p2]);
+            seg(px[p2], py[p2], m.cx[in], m.cy[in]);
+            seg(m.cx[in], m.cy[in], px[p1], py[p1]);
+        }
+        if (in < 0 && out >= 0) {
+            seg(px[p1], py[p1], m.cx[out], m.cy[out]);
+            seg(m.cx[out], m.cy[out], px[p2], py[p2]);
+            seg(px[p2], py[p2], px[p1], py[p1]);
+        }
+        if (out < 0 && in >= 0) {
+            seg(px[p1], py[p1], px[p2], py[p2]);
+            seg(px[p2], py[p2], m.cx[in], m.cy[in]);
+            seg(m.cx[in], m.cy[in], px[p1], py[p1]);
+        }
+        m.fcov[i] = cov;
+        if (cov <= 0.0) { err = "-ve face co-volume"; return UNS_ERR_MESH; }
+    }
+
+    // LSQR_Coeff (NCFVM/geometric.f90:760-806): weights per v2v entry.
+    to_csr(v2v, m.v2v_off, m.v2v);
+    m.wx.assign(m.v2v.size(), 0.0); m.wy.assign(m.v2v.size(), 0.0);
+    for (int i = 0; i < nop; ++i) {
+        double xc = px[i], yc = py[i];
+        double r11 = 0, r12 = 0, r22 = 0;
+        for (int k = m.v2v_off[i]; k < m.v2v_off[i + 1]; ++k) {
+            int cc = m.v2v[k];
+            double dx = px[cc] - xc, dy = py[cc] - yc;
+            r11 = r11 + dx * dx; r12 = r12 + dx * dy; r22 = r22 + dy * dy;
+        }
+        r11 = std::sqrt(r11);
+        r12 = r12 / r11;
+        r22 = std::sqrt(r22 - r12 * r12);
+        for (int k = m.v2v_off[i]; k < m.v2v_off[i + 1]; ++k) {
+            int cc = m.v2v[k];
+            double dx = px[cc] - xc, dy = py[cc] - yc;
+            double alfa1 = dx / r11 / r11;
+            double alfa2 = (dy - dx * r12 / r11) / r22 / r22;
+            m.wx[k] = alfa1 - alfa2 * r12 / r11;
+            m.wy[k] = alfa2;
+        }
+    }
+    to_csr(v2f, m.v2f_off, m.v2f);
+    return UNS_OK;
+}
+
+uns_nc_mesh MeshNC::view() const {
+    uns_nc_mesh v;
+    std::memset(&v, 0, sizeof(v));
+    v.nop = nop; v.noc = noc; v.nof = nof;
+    v.px = px.data(); v.py = py.data(); v.cv = cv.data();
+    v.fp1 = fp1.data(); v.fp2 = fp2.data(); v.fbc = fbc.data();
+    v.fnx = fnx.data(); v.fny = fny.data(); v.farea = farea.data();
+    v.v2v_off = v2v_off.data(); v.v2v = v2v.data();
+    v.wx = wx.data(); v.wy = wy.data();
+    v.v2f_off = v2f_off.data(); v.v2f = v2f.data();
+    return v;
+}
+
+// ------------------------------------------------------------- flo.inp
+namespace {
+
+// One positional line of a list-directed Fortran read: label then values.
+bool flo_line(std::ifstream& f, std::vector<std::string>& tok) {
+    std::string line;
+    while (std::getline(f, line)) {
+        tok.clear();
+        std::istringstream ss(line);
+        std::string t;
+        while (ss >> t) {
+            if (t.size() >= 2 && (t.front() == '"' || t.front() == '\'')) t = t.substr(1, t.size() - 2);
+            tok.push_back(t);
+        }
+        if (!tok.empty()) return true;
+    }
+    return false;
+}
+
+int need(const std::vector<std::string>& t, size_t n, const char* what, std::string& err) {
+    if (t.size() < n) { err = std::string("flo.inp: missing values on line ") + what; return UNS_ERR_IO; }
+    return UNS_OK;
+}
+
+}  // namespace
+
+int read_flo_inp_cc(const std::string& path, uns_params& p, std::string& grid, std::string& err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open " + path; return UNS_ERR_IO; }
+    std::memset(&p, 0, sizeof(p));
+    std::vector<std::string> t;
+    int rc;
+    const char* names[] = {"Start", "FlowType", "Mach", "AOA", "Reynolds", "CFL", "Timemode", "GradType",
+                           "LastIter", "MaxIter", "MinRes", "SaveInt", "ScrInt", "NoIso", "Flux", "Limiter",
+                           "irs", "FarBC", "GridFile"};
+    const size_t nval[] = {2, 4, 2, 2, 2, 5, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 4, 2};
+    std::vector<std::vector<std::string>> L;
+    for (int k = 0; k < 19; ++k) {
+        if (!flo_line(f, t)) { err = std::string("flo.inp: missing line ") + names[k]; return UNS_ERR_IO; }
+        if ((rc = need(t, nval[k], names[k], err))) return rc;
+        L.push_back(t);
+    }
+    try {
+        int istart = std::stoi(L[0][1]);
+        std::string flow = L[1][1];
+        p.iwall = std::stoi(L[1][2]);
+        p.t_wall = std::stod(L[1][3]);
+        p.m_inf = std::stod(L[2][1]);
+        p.aoa_deg = std::stod(L[3][1]);
+        p.rey = std::stod(L[4][1]);
+        std::string cfl_type = L[5][1];
+        p.cfl_min = std::stod(L[5][2]);
+        p.cfl_max = std::stod(L[5][3]);
+        p.cfl_ramp_steps = std::stoi(L[5][4]);
+        std::string tm = L[6][1], gt = L[7][1];
+        p.max_iter = std::stoi(L[9][1]);
+        p.min_res = std::stod(L[10][1]);
+        p.scr_interval = std::stoi(L[12][1]);
+        std::string flux = L[14][1];
+        p.ilimit = std::stoi(L[15][1]);
+        p.irs = std::stoi(L[16][1]);
+        int vortex = std::stoi(L[17][1]);
+        grid = L[18][1];
+        // Validation as CCFVM/read_input.F90:53-119.
+        if (istart != 1 && istart != 2) { err = "Unknown start option"; return UNS_ERR_ARG; }
+        if (flow == "inviscid") p.flow_type = UNS_FLOW_INVISCID;
+        else if (flow == "laminar") p.flow_type = UNS_FLOW_LAMINAR;
+        else if (flow == "rans") { err = "RANS not available"; return UNS_ERR_ARG; }
+        else { err = "Unknown flow type " + flow; return UNS_ERR_ARG; }
+        if (p.iwall != 0 && p.iwall != 1) { err = "Unknown wall conditions"; return UNS_ERR_ARG; }
+        if (tm == "rk3") p.time_mode = UNS_TIME_RK3;
+        else if (tm == "lusgs") p.time_mode = UNS_TIME_LUSGS;
+        else { err = "Unknown time integration scheme " + tm; return UNS_ERR_ARG; }
+        if (cfl_type == "tanh") p.cfl_type = UNS_CFL_TANH;
+        else if (cfl_type == "ramp") p.cfl_type = UNS_CFL_RAMP;
+        else { err = "Unknown cfl type " + cfl_type; return UNS_ERR_ARG; }
+        if (gt == "gg") p.grad_type = UNS_GRAD_GG;
+        else if (gt == "ggfc") p.grad_type = UNS_GRAD_GGFC;
+        else if (gt == "lsqr") p.grad_type = UNS_GRAD_LSQR;
+        else { err = "Unknown gradient type " + gt; return UNS_ERR_ARG; }
+        if (flux == "roe") p.flux_type = UNS_FLUX_ROE;
+        else if (flux == "ausm") p.flux_type = UNS_FLUX_AUSM;
+        else if (flux == "vanleer") p.flux_type = UNS_FLUX_VANLEER;
+        else if (flux == "rusanov") p.flux_type = UNS_FLUX_RUSANOV;
+        else { err = "Unknown flux " + flux; return UNS_ERR_ARG; }
+        if (p.irs != 0 && p.irs != 1) { err = "Unknown Implicit Residual Smoothening option"; return UNS_ERR_ARG; }
+        if (p.ilimit != 0 && p.ilimit != 1) { err = "Unknown limiter option"; return UNS_ERR_ARG; }
+        if (vortex != 0 && vortex != 1) { err = "Unknown vortex option"; return UNS_ERR_ARG; }
+        // main.F90:32-45 accepts rk3 only below CFL 1; CFL exactly 1 leaves the
+        // stage coefficients unset there, so it is rejected too.
+        if (p.time_mode == UNS_TIME_RK3 && !(p.cfl_max < 1.0)) { err = "CFL should be less than 1 for rk3"; return UNS_ERR_ARG; }
+        p.precision = UNS_PREC_FP64;
+        if (L[15].size() >= 3 && L[15][2] == "mixed") p.precision = UNS_PREC_MIXED;
+    } catch (...) {
+        err = "flo.inp: unparsable value";
+        return UNS_ERR_IO;
+    }
+    return UNS_OK;
+}
+
+int read_flo_inp_nc(const std::string& path, uns_params& p, std::string& grid, std::string& err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open " + path; return UNS_ERR_IO; }
+    std::memset(&p, 0, sizeof(p));
+    std::vector<std::string> t;
+    std::vector<std::vector<std::string>> L;
+    const char* names[] = {"Start", "FlowType", "Mach", "AOA", "Reynolds", "CFL", "Timemode", "GMRES",
+                           "LastIter", "MaxIter", "MinRes", "SaveInt", "ScrInt", "NoIso", "Flux", "Limiter",
+                           "FarBC", "GridFile"};
+    const size_t nval[] = {2, 2, 2, 2, 2, 2, 2, 4, 2, 2, 2, 2, 2, 2, 2, 2, 4, 2};
+    int rc;
+    for (int k = 0; k < 18; ++k) {
+        if (!flo_line(f, t)) { err = std::string("flo.inp: missing line ") + names[k]; return UNS_ERR_IO; }
+        if ((rc = need(t, nval[k], names[k], err))) return rc;
+        L.push_back(t);
+    }
+    try {
+        int istart = std::stoi(L[0][1]);
+        std::string flow = L[1][1];
+        p.m_inf = std::stod(L[2][1]);
+        p.aoa_deg = std::stod(L[3][1]);
+        p.rey = std::stod(L[4][1]);
+        p.cfl_max = std::stod(L[5][1]);
+        std::string tm = L[6][1];
+        p.max_iter = std::stoi(L[9][1]);
+        p.min_res = std::stod(L[10][1]);
+        p.scr_interval = std::stoi(L[12][1]);
+        std::string flux = L[14][1];
+        p.ilimit = std::stoi(L[15][1]);
+        int vortex = std::stoi(L[16][1]);
+        grid = L[17][1];
+        if (istart != 1 && istart != 2) { err = "Unknown start option"; return UNS_ERR_ARG; }
+        if (flow == "inviscid") p.flow_type = UNS_FLOW_INVISCID;
+        else if (flow == "laminar" || flow == "rans") { err = "NCFVM hot path is inviscid"; return UNS_ERR_ARG; }
+        else { err = "Unknown flow type " + flow; return UNS_ERR_ARG; }
+        if (tm == "rk3") p.time_mode = UNS_TIME_RK3;
+        else if (tm == "lusgs") p.time_mode = UNS_TIME_LUSGS;
+        else { err = "Unknown time integration scheme " + tm; return UNS_ERR_ARG; }
+        // The reference NCFVM ignores the Flux and Limiter lines and always
+        // runs van Leer + Venkatakrishnan (NCFVM/fvresidual.f90:34-64).  This
+        // build selects AUSM+-up with "Flux ausm" and the Barth-Jespersen
+        // limiter with a third token "Limiter 1 barth"; anything else keeps
+        // the reference behaviour.
+        p.flux_type = (flux == "ausm") ? UNS_FLUX_AUSM : UNS_FLUX_VANLEER;
+        p.limiter_type = (L[15].size() >= 3 && L[15][2] == "barth") ? UNS_LIM_BARTH : UNS_LIM_VKN;
+        if (L[15].size() >= 4 && L[15][3] == "mixed") p.precision = UNS_PREC_MIXED;
+        if (p.ilimit != 0 && p.ilimit != 1) { err = "Unknown limiter option"; return UNS_ERR_ARG; }
+        if (vortex != 0 && vortex != 1) { err = "Unknown vortex option"; return UNS_ERR_ARG; }
+        if (p.time_mode == UNS_TIME_RK3 && !(p.cfl_max < 1.0)) { err = "CFL should be less than 1 for rk3"; return UNS_ERR_ARG; }
+    } catch (...) {
+        err = "flo.inp: unparsable value";
+        return UNS_ERR_IO;
+    }
+    return UNS_OK;
+}
+
+}  // namespace unshost

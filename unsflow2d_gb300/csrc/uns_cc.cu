@@ -1,0 +1,1496 @@
+// uns_cc.cu -- cell-centred (CCFVM) residual-and-update hot path on GB300.
+//
+// Design (see the design doc for the roofline per kernel):
+//   * structure-of-arrays in HBM with small per-entity vectors: double4 for
+//     the four conserved / primitive / gradient / limiter values of a cell,
+//     so a gathered neighbour costs one 32-byte sector;
+//   * face kernels compute every per-face quantity once (flux, spectral
+//     radius, face gradient) and write it to a face array; cell kernels then
+//     gather their faces from an index-sorted face list.  That is atomic-free
+//     and deterministic, and the per-cell summation order is exactly the
+//     reference's face-loop order (boundary faces, then interior faces, then
+//     the viscous loop), so there is no colour pass and no reordering error;
+//   * cell kernels fuse what the reference runs as separate cell loops
+//     (con2prim + save_old + the limiter's global min/max; spectral radius
+//     gather + dt + gradient + limiter; residual gather + RK stage + norm);
+//   * LU-SGS forward/backward sweeps are level-scheduled on the cell DAG of
+//     the reference ordering inside one cooperative launch with a bounded
+//     grid barrier, which reproduces the sequential sweep exactly;
+//   * one iteration of the main loop is captured once as a CUDA graph and
+//     replayed; iteration number, CFL schedule and the convergence stop live
+//     in device memory.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "uns_common.cuh"
+#include "uns_phys.cuh"
+#include "unsflow_gpu.h"
+
+using namespace uns;
+
+namespace {
+
+constexpr int SIDE_BIT = 1 << 30;  // cell is the `out` side of this face
+constexpr int FACE_MASK = SIDE_BIT - 1;
+
+struct CCView {
+    int nop, noc, nfi, nbf, nof, ntot;
+    // geometry (read-only)
+    const double2* pxy;
+    const double2* cen;
+    const double* cv;
+    const double* cov;
+    const int2* fnb;      // (in, out)
+    const int2* fpt;      // (p1, p2)
+    const double2* fn;    // unit normal
+    const double* farea;
+    const double2* fcen;
+    const int* fbc;
+    const double4* lsw;   // LSQ weights (wx0, wy0, wx1, wy1) per face
+    const int* nc2c;
+    const int* cf_off;    // index-sorted faces per cell, SIDE_BIT for `out`
+    const int* cf;
+    const int* rc2f_off;  // reference c2f order (LU-SGS)
+    const int* rc2f;
+    const int* v2c_off;
+    const int* v2c;
+    const double* v2c_wt;
+    // state
+    double4* qc;  // [ntot] E, rho, rho u, rho v
+    double4* qp;  // [ntot] rho, u, v, p
+    double* qT;   // [ntot] T
+    double4* qold;
+    double4* res;
+    double4* res0;
+    double4* restmp;
+    double4* gx;
+    double4* gy;
+    double4* phi;
+    double* dt;
+    double* la;
+    double* mul;
+    double4* pp;
+    double* ppT;
+    double4* fq;
+    double* fqT;
+    double* fla;
+    double* fmu;
+    double4* fF;   // convective face flux (boundary: flux into `in`)
+    double4* fV;   // viscous flux * area
+    double4* fgx;  // diamond-path face gradient, rho,u,v,p
+    double4* fgy;
+    double2* fgT;  // face gradient of T
+    double* fasum; // a1 + a2
+    double2* fwall;   // per boundary face: wall convective (flux3, flux4)
+    double2* fwallv;  // per boundary face: wall viscous (-flux3*A, -flux4*A)
+    double4* lower;
+    double4* upper;
+    unsigned long long* minmax;  // encoded qmax[4], qmin[4]
+    unsigned long long* dtmin;   // encoded dtglobal
+    double* partial;
+    DevErr* err;
+    // iteration control (graph fast path)
+    const double* cfl_sched;
+    int* iter;
+    int* done;
+    double* fres_hist;
+    double* fres1;
+    Gas g;
+    int grad_type, ilimit, irs, laminar, first_iter;
+    double cfl_max, min_res;
+};
+
+__device__ __forceinline__ bool stopped(const CCView& v) { return v.done != nullptr && *((volatile int*)v.done) != 0; }
+__device__ __forceinline__ double cur_cfl(const CCView& v, double cfl) {
+    return v.cfl_sched ? v.cfl_sched[*v.iter] : cfl;
+}
+
+// ---------------------------------------------------------------- kernels
+// con2prim (main.F90:62-67) + save_old (solution.F90:331-345) + the global
+// min/max of every cell's primitives incl. ghosts (limiter.F90:146-149) +
+// the positivity check of main.F90:384-411, fused over one pass of the cells.
+enum { BEGIN_PRIM = 1, BEGIN_OLD = 2, BEGIN_MINMAX = 4, BEGIN_POS = 8 };
+
+__global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long emx[4] = {0ULL, 0ULL, 0ULL, 0ULL};
+    unsigned long long emn[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
+    if (i < v.noc) {
+        double4 q = v.qc[i];
+        if (flags & BEGIN_PRIM) {
+            Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
+            v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
+            v.qT[i] = P.t;
+            if ((flags & BEGIN_POS) && (P.rho <= 0.0 || P.p <= 0.0)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
+        }
+        if (flags & BEGIN_OLD) v.qold[i] = q;
+    }
+    if (flags & BEGIN_MINMAX) {
+        if (i < v.ntot) {
+            double4 p = v.qp[i];
+            double a[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { emx[j] = enc_ord(a[j]); emn[j] = emx[j]; }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                unsigned long long t = __shfl_xor_sync(0xffffffffu, emx[j], o);
+                emx[j] = t > emx[j] ? t : emx[j];
+                t = __shfl_xor_sync(0xffffffffu, emn[j], o);
+                emn[j] = t < emn[j] ? t : emn[j];
+            }
+        }
+        __shared__ unsigned long long smx[kBlock / 32][4], smn[kBlock / 32][4];
+        int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+        if (l == 0)
+            for (int j = 0; j < 4; ++j) { smx[w][j] = emx[j]; smn[w][j] = emn[j]; }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            int j = threadIdx.x;
+            unsigned long long a = smx[0][j], b = smn[0][j];
+            for (int k = 1; k < kBlock / 32; ++k) { a = smx[k][j] > a ? smx[k][j] : a; b = smn[k][j] < b ? smn[k][j] : b; }
+            atomicMax(&v.minmax[j], a);
+            atomicMin(&v.minmax[4 + j], b);
+        }
+    }
+}
+
+// avg_c2v vertex part (average.F90:263-281): pseudo-Laplacian weighted mean.
+__global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nop) return;
+    double wt = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0;
+    for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
+        int c = __ldg(&v.v2c[k]);
+        double w = __ldg(&v.v2c_wt[k]);
+        wt = wt + w;
+        double4 q = v.qp[c];
+        c0 = c0 + q.x * w;
+        c1 = c1 + q.y * w;
+        c2 = c2 + q.z * w;
+        c3 = c3 + q.w * w;
+        c4 = c4 + v.qT[c] * w;
+    }
+    v.pp[i] = make_double4(c0 / wt, c1 / wt, c2 / wt, c3 / wt);
+    v.ppT[i] = c4 / wt;
+}
+
+// avg_c2v face part (average.F90:284-288) + spectral02 face radius
+// (timestep.F90:399-423).
+__global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
+    if (stopped(v)) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nof) return;
+    int2 p = v.fpt[f];
+    double4 a = v.pp[p.x], b = v.pp[p.y];
+    double4 q = make_double4(0.5 * (a.x + b.x), 0.5 * (a.y + b.y), 0.5 * (a.z + b.z), 0.5 * (a.w + b.w));
+    v.fq[f] = q;
+    v.fqT[f] = 0.5 * (v.ppT[p.x] + v.ppT[p.y]);
+    double2 n = v.fn[f];
+    double a0 = sqrt(v.g.gamma * q.w / q.x);
+    double un = q.y * n.x + q.z * n.y;
+    double ll = v.farea[f] * (fabs(un) + a0);
+    ll = ll + v.g.vll * v.fmu[f] / q.x;
+    v.fla[f] = ll;
+}
+
+// Diamond-path face gradient (gradient.F90:474-556, gradtrixy :572-612).
+__device__ __forceinline__ bool gradtri(const double* pr0, const double* pr1, const double* pr2, double x0, double y0,
+                                        double x1, double y1, double x2, double y2, double gxo[5], double gyo[5],
+                                        double& tarea) {
+    const double xs[3] = {x0, x1, x2}, ys[3] = {y0, y1, y2};
+    const double* prs[3] = {pr0, pr1, pr2};
+    tarea = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        int ip1 = (i == 2) ? 0 : i + 1;
+        double dx = 0.5 * (xs[ip1] + xs[i]);
+        double dy = ys[ip1] - ys[i];
+        tarea = tarea + dx * dy;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { gxo[k] = 0.0; gyo[k] = 0.0; }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        int ip1 = (i == 2) ? 0 : i + 1;
+        double dx = ys[ip1] - ys[i];
+        double dy = -(xs[ip1] - xs[i]);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            double var = 0.5 * (prs[i][k] + prs[ip1][k]);
+            gxo[k] = gxo[k] + var * dx;
+            gyo[k] = gyo[k] + var * dy;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) { gxo[k] = gxo[k] / tarea; gyo[k] = gyo[k] / tarea; }
+    return tarea > 0.0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_face_ggfc(CCView v) {
+    if (stopped(v)) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nof) return;
+    int2 nb = v.fnb[f];
+    int2 p = v.fpt[f];
+    double2 X1 = v.pxy[p.x], X2 = v.pxy[p.y], Ci = v.cen[nb.x], Co = v.cen[nb.y];
+    double4 a = v.pp[p.x], b = v.pp[p.y], qi = v.qp[nb.x], qo = v.qp[nb.y];
+    double P1[5] = {a.x, a.y, a.z, a.w, v.ppT[p.x]};
+    double P2[5] = {b.x, b.y, b.z, b.w, v.ppT[p.y]};
+    double QI[5] = {qi.x, qi.y, qi.z, qi.w, v.qT[nb.x]};
+    double QO[5] = {qo.x, qo.y, qo.z, qo.w, v.qT[nb.y]};
+    double g1x[5], g1y[5], g2x[5], g2y[5], a1, a2;
+    bool ok1 = gradtri(P1, QO, P2, X1.x, X1.y, Co.x, Co.y, X2.x, X2.y, g1x, g1y, a1);
+    bool ok2 = gradtri(P1, P2, QI, X1.x, X1.y, X2.x, X2.y, Ci.x, Ci.y, g2x, g2y, a2);
+    if (!(ok1 && ok2)) set_err(v.err, UNS_ERR_MESH, f);
+    double s = a1 + a2;
+    double gx[5], gy[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        gx[k] = (a1 * g1x[k] + a2 * g2x[k]) / s;
+        gy[k] = (a1 * g1y[k] + a2 * g2y[k]) / s;
+    }
+    v.fgx[f] = make_double4(gx[0], gx[1], gx[2], gx[3]);
+    v.fgy[f] = make_double4(gy[0], gy[1], gy[2], gy[3]);
+    v.fgT[f] = make_double2(gx[4], gy[4]);
+    v.fasum[f] = s;
+}
+
+__device__ __forceinline__ void d4get(const double4& q, double o[4]) { o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.w; }
+__device__ __forceinline__ double4 d4(const double o[4]) { return make_double4(o[0], o[1], o[2], o[3]); }
+
+// Per-cell gather over the index-sorted face list: spectral radius + dt
+// (timestep.F90:364-371, 424-425), the cell gradient (Gradient_GG
+// gradient.F90:399-443, Gradient_GG_FC :511-564, Gradient_LSQR :308-377) and
+// limiter_VKN1 (limiter.F90:146-279).  Face order is the reference's loop
+// order (interior faces, then boundary faces).
+enum { CG_DT = 1, CG_GRAD = 2, CG_LIM = 4 };
+
+__global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, double cfl_in) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+    if (flags & CG_DT) {
+        double la = 0.0;
+        for (int k = k0; k < k1; ++k) la = la + v.fla[v.cf[k] & FACE_MASK];
+        v.la[i] = la;
+        double cfl = cur_cfl(v, cfl_in);
+        double dt = cfl * v.cv[i] / la;
+        v.dt[i] = dt;
+        atomicMin(v.dtmin, enc_ord(dt));
+    }
+    double gx[4], gy[4];
+    if (flags & CG_GRAD) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { gx[j] = 0.0; gy[j] = 0.0; }
+        if (v.grad_type == UNS_GRAD_GG) {
+            for (int k = k0; k < k1; ++k) {
+                int e = v.cf[k], f = e & FACE_MASK;
+                double2 n = v.fn[f];
+                double area = v.farea[f];
+                double q[4];
+                d4get(v.fq[f], q);
+                if (f < v.nfi) {
+                    double dx = n.x * area, dy = n.y * area;
+                    if (e & SIDE_BIT) {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) { gx[j] = gx[j] - q[j] * dx; gy[j] = gy[j] - q[j] * dy; }
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + q[j] * dx; gy[j] = gy[j] + q[j] * dy; }
+                    }
+                } else {
+                    double dx = -n.x * area, dy = -n.y * area;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + q[j] * dx; gy[j] = gy[j] + q[j] * dy; }
+                }
+            }
+            double var = v.cv[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { gx[j] = gx[j] / var; gy[j] = gy[j] / var; }
+        } else if (v.grad_type == UNS_GRAD_GGFC) {
+            for (int k = k0; k < k1; ++k) {
+                int f = v.cf[k] & FACE_MASK;
+                double s = v.fasum[f];
+                double a[4], b[4];
+                d4get(v.fgx[f], a);
+                d4get(v.fgy[f], b);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + a[j] * s; gy[j] = gy[j] + b[j] * s; }
+            }
+            double var = v.cov[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { gx[j] = gx[j] / var; gy[j] = gy[j] / var; }
+        } else {  // LSQR
+            double qi[4];
+            d4get(v.qp[i], qi);
+            for (int k = k0; k < k1; ++k) {
+                int e = v.cf[k], f = e & FACE_MASK;
+                double4 w = v.lsw[f];
+                int2 nb = v.fnb[f];
+                double qa[4], qb[4];
+                d4get(v.qp[nb.x], qa);
+                d4get(v.qp[nb.y], qb);
+                if (f < v.nfi && (e & SIDE_BIT)) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        double var = qb[j] - qa[j];
+                        gx[j] = gx[j] - var * w.z;
+                        gy[j] = gy[j] - var * w.w;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        double var = qb[j] - qa[j];
+                        gx[j] = gx[j] + var * w.x;
+                        gy[j] = gy[j] + var * w.y;
+                    }
+                }
+            }
+            (void)qi;
+        }
+        v.gx[i] = d4(gx);
+        v.gy[i] = d4(gy);
+    } else {
+        d4get(v.gx[i], gx);
+        d4get(v.gy[i], gy);
+    }
+    if (flags & CG_LIM) {
+        double qmax[4], qmin[4], tol[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            qmax[j] = dec_ord(v.minmax[j]);
+            qmin[j] = dec_ord(v.minmax[4 + j]);
+            tol[j] = 0.05 * (qmax[j] - qmin[j]);
+        }
+        double qi[4], umax[4], umin[4], ph[4];
+        d4get(v.qp[i], qi);
+        d4get(v.phi[i], ph);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { umax[j] = qi[j]; umin[j] = qi[j]; }
+        for (int k = k0; k < k1; ++k) {
+            int e = v.cf[k], f = e & FACE_MASK;
+            double u[4];
+            if (f < v.nfi) {
+                int2 nb = v.fnb[f];
+                d4get(v.qp[(e & SIDE_BIT) ? nb.x : nb.y], u);
+            } else {
+                int2 p = v.fpt[f];
+                double4 a = v.pp[p.x], b = v.pp[p.y];
+                u[0] = 0.5 * (a.x + b.x); u[1] = 0.5 * (a.y + b.y); u[2] = 0.5 * (a.z + b.z); u[3] = 0.5 * (a.w + b.w);
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { umax[j] = rmax(umax[j], u[j]); umin[j] = rmin(umin[j], u[j]); }
+        }
+        double2 c = v.cen[i];
+        for (int k = k0; k < k1; ++k) {
+            int f = v.cf[k] & FACE_MASK;
+            double2 fc = v.fcen[f];
+            double d0 = fc.x - c.x, d1 = fc.y - c.y;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                double D_L = gx[j] * d0 + gy[j] * d1;
+                double phi0 = 1.0;
+                if (D_L > 0.0) phi0 = vk_limit(umax[j] - qi[j], D_L, tol[j]);
+                else if (D_L < 0.0) phi0 = vk_limit(umin[j] - qi[j], D_L, tol[j]);
+                ph[j] = rmin(ph[j], phi0);
+            }
+        }
+        v.phi[i] = d4(ph);
+    }
+}
+
+// Convective face flux (fvresidual.F90:27-171).  Boundary faces also write
+// their ghost cell (farfield: Riemann state; wall: slip / no-slip mirror).
+// R = double for the FP64 form, float for FP32 face arithmetic.
+template <class R>
+__device__ __forceinline__ bool flux_dispatch(const CCView& v, R nx, R ny, R area, V4<R>& ql, V4<R>& qr, V4<R>& F) {
+    const R G = (R)v.g.gamma, G1 = (R)v.g.gamma1;
+    bool ok = true;
+    R hl, hr;
+    switch (v.g.flux) {
+        case UNS_FLUX_ROE: ok = roe_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
+        case UNS_FLUX_RUSANOV: rusanov_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
+        case UNS_FLUX_VANLEER:
+            vanleer_core<R>(G, G1, nx, ny, ql, qr, F, hl, hr);
+            for (int k = 0; k < 4; ++k) F[k] = F[k] * area;
+            break;
+        default: {  // AUSM+-up: the reference scales by |n| of the unit normal
+            ausm_core<R>(G, G1, nx, ny, (R)v.g.mref, ql, qr, F, hl, hr);
+            R an = sqrt(nx * nx + ny * ny);
+            for (int k = 0; k < 4; ++k) F[k] = F[k] * an;
+        }
+    }
+    return ok;
+}
+
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
+    if (stopped(v)) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nof) return;
+    int2 nb = v.fnb[f];
+    int in = nb.x, out = nb.y;
+    double2 n = v.fn[f];
+    double area = v.farea[f];
+    double2 fc = v.fcen[f];
+    double2 ci = v.cen[in];
+    double qi[4], gxi[4], gyi[4], phi_i[4];
+    d4get(v.qp[in], qi);
+    d4get(v.gx[in], gxi);
+    d4get(v.gy[in], gyi);
+    d4get(v.phi[in], phi_i);
+    V4<R> ql, qr, F;
+    if (f < v.nfi) {
+        double2 co = v.cen[out];
+        double qo[4], gxo[4], gyo[4], phi_o[4];
+        d4get(v.qp[out], qo);
+        d4get(v.gx[out], gxo);
+        d4get(v.gy[out], gyo);
+        d4get(v.phi[out], phi_o);
+        const double zhi = 1.0 / 3.0;
+        double dl0 = fc.x - ci.x, dl1 = fc.y - ci.y;
+        double dr0 = fc.x - co.x, dr1 = fc.y - co.y;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
+            double alfa = gxi[j] * dl0 + gyi[j] * dl1;
+            double beta = qo[j] - qi[j];
+            ql[j] = (R)(qi[j] + 0.5 * phi_i[j] * (zhi * beta + (1.0 - zhi) * alfa));
+            alfa = gxo[j] * dr0 + gyo[j] * dr1;
+            beta = qi[j] - qo[j];
+            qr[j] = (R)(qo[j] + 0.5 * phi_o[j] * (zhi * beta + (1.0 - zhi) * alfa));
+        }
+        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
+        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
+        return;
+    }
+    // boundary face
+    int bc = v.fbc[f];
+    double d0 = fc.x - ci.x, d1 = fc.y - ci.y;
+    double qcl[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) qcl[j] = qi[j] + phi_i[j] * (gxi[j] * d0 + gyi[j] * d1);
+    const Gas& g = v.g;
+    double4 Fd = make_double4(0.0, 0.0, 0.0, 0.0);
+    if (bc == 2001) {
+        V4<double> L = {qcl[0], qcl[1], qcl[2], qcl[3]};
+        V4<double> B = farfield_state<double>(g.gamma, g.gamma1, n.x, n.y, g.r_inf, g.u_inf, g.v_inf, g.p_inf, L);
+        for (int j = 0; j < 4; ++j) { ql[j] = (R)L[j]; qr[j] = (R)B[j]; }
+        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
+        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        Fd = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
+        // Ghost state = prim2con of the right state the flux routine left
+        // behind (Rusanov leaves it in conserved form, as in the reference).
+        V4<double> R4 = B;
+        if (g.flux == UNS_FLUX_RUSANOV) for (int j = 0; j < 4; ++j) R4[j] = (double)qr[j];
+        V4<double> C = prim2con<double>(g.gamma, R4);
+        v.qc[out] = make_double4(C[0], C[1], C[2], C[3]);
+        Prim P = con2prim(g, C[0], C[1], C[2], C[3]);
+        v.qp[out] = make_double4(P.rho, P.u, P.v, P.p);
+        v.qT[out] = P.t;
+    } else if (bc == 1001) {
+        double4 c = v.qc[in];
+        Prim P = con2prim(g, c.x, c.y, c.z, c.w);
+        double4 gq;
+        double4 gp;
+        double gT;
+        if (g.flow == UNS_FLOW_INVISCID) {  // slip_wall (boundCond.F90:46-81)
+            double un = P.u * n.x + P.v * n.y;
+            gq = make_double4(c.x, c.y, P.rho * P.u - 2.0 * un * n.x, P.rho * P.v - 2.0 * un * n.y);
+            Prim Q = con2prim(g, gq.x, gq.y, gq.z, gq.w);
+            gp = make_double4(Q.rho, Q.u, Q.v, Q.p);
+            gT = Q.t;
+        } else if (g.iwall == 0) {  // isothermal NoSlip_wall (boundCond.F90:19-30)
+            double tg = 2.0 * g.t_wall - P.t;
+            if (tg <= 0.0) tg = 0.01 * g.t_wall;
+            double rhog = P.p / (P.rho * g.znd);
+            gp = make_double4(rhog, -P.u, -P.v, P.p);
+            gT = tg;
+            V4<double> pr = {gp.x, gp.y, gp.z, gp.w};
+            V4<double> C = prim2con<double>(g.gamma, pr);
+            gq = make_double4(C[0], C[1], C[2], C[3]);
+        } else {  // adiabatic NoSlip_wall (boundCond.F90:31-37)
+            gq = make_double4(c.x, c.y, -c.z, -c.w);
+            Prim Q = con2prim(g, gq.x, gq.y, gq.z, gq.w);
+            gp = make_double4(Q.rho, Q.u, Q.v, Q.p);
+            gT = Q.t;
+        }
+        v.qc[out] = gq;
+        v.qp[out] = gp;
+        v.qT[out] = gT;
+        for (int j = 0; j < 4; ++j) ql[j] = (R)qcl[j];
+        qr[0] = (R)gp.x; qr[1] = (R)gp.y; qr[2] = (R)gp.z; qr[3] = (R)gp.w;
+        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
+        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        Fd = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
+        v.fwall[f - v.nfi] = make_double2(Fd.z, Fd.w);
+    }
+    v.fF[f] = Fd;
+}
+
+// Sutherland viscosity of every interior cell (viscous_flux.F90:478-480,585-597).
+__global__ void __launch_bounds__(kBlock) k_cell_mul(CCView v) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    double4 c = v.qc[i];
+    Prim P = con2prim(v.g, c.x, c.y, c.z, c.w);
+    double num = 1.0 + v.g.T_infd / v.g.SCONST;
+    double den = P.t + v.g.T_infd / v.g.SCONST;
+    v.mul[i] = (num / den) * pow(P.t, 1.5);
+}
+
+// Laminar viscous face flux (viscous_flux.F90:488-534), stored as flux*area.
+__global__ void __launch_bounds__(kBlock) k_face_visc(CCView v) {
+    if (stopped(v)) return;
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nof) return;
+    int2 nb = v.fnb[f];
+    double2 n = v.fn[f];
+    double area = v.farea[f];
+    double mu = (nb.y < v.noc) ? 0.5 * (v.mul[nb.x] + v.mul[nb.y]) : v.mul[nb.x];
+    v.fmu[f] = mu;
+    double4 q = v.fq[f];
+    double4 a = v.fgx[f], b = v.fgy[f];
+    double2 t = v.fgT[f];
+    double uvel = q.y, vvel = q.z;
+    double ux = a.y, uy = b.y, vx = a.z, vy = b.z, tx = t.x, ty = t.y;
+    const double two = 2.0, two_third = two / 3.0;
+    double tauxx = two_third * (two * ux - vy);
+    double tauxy = (uy + vx);
+    double tauyy = two_third * (two * vy - ux);
+    double factor = (v.g.gamma - 1.0) * v.g.m_inf * v.g.m_inf * v.g.prandtl;
+    double qx = -(tx / factor), qy = -(ty / factor);
+    double mr = mu / v.g.rey;
+    double f1 = mr * ((uvel * tauxx + vvel * tauxy - qx) * n.x + (uvel * tauxy + vvel * tauyy - qy) * n.y);
+    double f3 = mr * (tauxx * n.x + tauxy * n.y);
+    double f4 = mr * (tauxy * n.x + tauyy * n.y);
+    v.fV[f] = make_double4(f1 * area, 0.0 * area, f3 * area, f4 * area);
+    if (f >= v.nfi) v.fwallv[f - v.nfi] = (v.fbc[f] == 1001) ? make_double2(f3 * area, f4 * area) : make_double2(0.0, 0.0);
+}
+
+// Residual gather in the reference's accumulation order, optionally fused
+// with one RK3 stage (main.F90:92-101) and the block partials of the norm.
+__device__ __forceinline__ void add4(double r[4], const double4& a) { r[0] = r[0] + a.x; r[1] = r[1] + a.y; r[2] = r[2] + a.z; r[3] = r[3] + a.w; }
+__device__ __forceinline__ void sub4(double r[4], const double4& a) { r[0] = r[0] - a.x; r[1] = r[1] - a.y; r[2] = r[2] - a.z; r[3] = r[3] - a.w; }
+
+__global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int partial) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0;
+    if (i < v.noc) {
+        const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+        double r[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = k0; k < k1; ++k) {  // boundary faces first
+            int f = v.cf[k] & FACE_MASK;
+            if (f >= v.nfi) add4(r, v.fF[f]);
+        }
+        for (int k = k0; k < k1; ++k) {  // then interior faces
+            int e = v.cf[k], f = e & FACE_MASK;
+            if (f < v.nfi) { if (e & SIDE_BIT) sub4(r, v.fF[f]); else add4(r, v.fF[f]); }
+        }
+        if (v.laminar) {
+            for (int k = k0; k < k1; ++k) {
+                int e = v.cf[k], f = e & FACE_MASK;
+                if (f < v.nfi && (e & SIDE_BIT)) add4(r, v.fV[f]); else sub4(r, v.fV[f]);
+            }
+        }
+        v.res[i] = d4(r);
+        if (irk > 0) {
+            const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
+            double a = A[irk - 1], b = B[irk - 1];
+            double dtbyarea = v.dt[i] / v.cv[i];
+            double o[4], c[4], q[4];
+            d4get(v.qold[i], o);
+            d4get(v.qc[i], c);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) q[j] = a * o[j] + b * (c[j] - dtbyarea * r[j]);
+            v.qc[i] = d4(q);
+        }
+        rr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+    }
+    if (partial) {
+        __shared__ double s[kBlock / 32];
+        rr = warp_sum(rr);
+        if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = rr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int k = 0; k < kBlock / 32; ++k) t = t + s[k];
+            v.partial[blockIdx.x] = t;
+        }
+    }
+}
+
+// One Jacobi sweep of cirs (ImpResiSmoothening.F90:626-643).
+__global__ void __launch_bounds__(kBlock) k_cirs(CCView v, const double4* src, double4* dst, double eps) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    double s[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = v.cf_off[i]; k < v.cf_off[i + 1]; ++k) {
+        int e = v.cf[k], f = e & FACE_MASK;
+        if (f >= v.nfi) continue;
+        int2 nb = v.fnb[f];
+        add4(s, src[(e & SIDE_BIT) ? nb.x : nb.y]);
+    }
+    double den = 1.0 / (1.0 + eps * (double)v.nc2c[i]);
+    double o[4];
+    d4get(v.res0[i], o);
+    double r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) r[j] = (s[j] * eps + o[j]) * den;
+    dst[i] = d4(r);
+}
+
+__global__ void __launch_bounds__(kBlock) k_rk_stage(CCView v, int irk) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
+    double a = A[irk - 1], b = B[irk - 1];
+    double dtbyarea = v.dt[i] / v.cv[i];
+    double o[4], c[4], r[4], q[4];
+    d4get(v.qold[i], o);
+    d4get(v.qc[i], c);
+    d4get(v.res[i], r);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[j] = a * o[j] + b * (c[j] - dtbyarea * r[j]);
+    v.qc[i] = d4(q);
+}
+
+__global__ void __launch_bounds__(kBlock) k_res_partial(CCView v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0;
+    if (i < v.noc) {
+        double4 r = v.res[i];
+        rr = r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w;
+    }
+    __shared__ double s[kBlock / 32];
+    rr = warp_sum(rr);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = rr;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < kBlock / 32; ++k) t = t + s[k];
+        v.partial[blockIdx.x] = t;
+    }
+}
+
+// Deterministic final sum of the block partials; in the graph path it also
+// records the history, the first-iteration normalisation and the stop flag
+// (solution.F90:365-379, main.F90:57).
+__global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, double* out) {
+    if (stopped(v)) return;
+    __shared__ double s[kBlock];
+    double t = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) t = t + v.partial[k];
+    s[threadIdx.x] = t;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) s[threadIdx.x] = s[threadIdx.x] + s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double fres = sqrt(s[0] / (double)v.noc / 4.0);
+        if (out) *out = fres;
+        if (v.iter) {
+            int it = *v.iter;
+            v.fres_hist[it] = fres;
+            if (it == 0 && v.first_iter) *v.fres1 = fres;
+            double f1 = *v.fres1;
+            double nf = (f1 >= 2.220446049250313e-16) ? fres / f1 : fres;
+            if (!(nf > v.min_res) || v.err->code != 0) {
+                *v.done = 1;
+                if (v.err->code != 0) v.err->iter = it;
+            }
+            *v.iter = it + 1;
+            // reset the encoded reductions for the next iteration
+            for (int j = 0; j < 4; ++j) { v.minmax[j] = 0ULL; v.minmax[4 + j] = ~0ULL; }
+            *v.dtmin = ~0ULL;
+        }
+    }
+}
+
+__global__ void k_reset_minmax(CCView v) {
+    if (stopped(v)) return;
+    if (threadIdx.x < 4) { v.minmax[threadIdx.x] = 0ULL; v.minmax[4 + threadIdx.x] = ~0ULL; }
+    if (threadIdx.x == 0) *v.dtmin = ~0ULL;
+}
+
+// Sequential wall-force sums in face order (fvresidual.F90:99-100 then
+// viscous_flux.F90:530-533).
+__global__ void k_forces(CCView v, double* out) {
+    double fx = 0.0, fy = 0.0;
+    for (int k = 0; k < v.nbf; ++k)
+        if (v.fbc[v.nfi + k] == 1001) { fx = fx + v.fwall[k].x; fy = fy + v.fwall[k].y; }
+    if (v.laminar)
+        for (int k = 0; k < v.nbf; ++k)
+            if (v.fbc[v.nfi + k] == 1001) { fx = fx - v.fwallv[k].x; fy = fy - v.fwallv[k].y; }
+    out[0] = fx;
+    out[1] = fy;
+}
+
+__global__ void k_check_pos(CCView v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    double4 p = v.qp[i];
+    if (p.x <= 0.0 || p.w <= 0.0) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
+}
+
+__global__ void k_initialize(CCView v, double4 qinf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < v.ntot) { v.qc[i] = qinf; v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0; }
+    if (i < v.noc) v.phi[i] = make_double4(1.0, 1.0, 1.0, 1.0);
+}
+
+// lusgs2 sweeps (lusgs.F90:245-318), one level of the dependency DAG per
+// grid-barrier phase.  The per-cell neighbour sum keeps the reference c2f
+// order, so the result equals the sequential sweep.
+__device__ __forceinline__ void normal_flux_d(const Gas& g, const double4& qo, const double4& dq, double nx, double ny,
+                                              double area, double out[4]) {
+    Prim P = con2prim(g, qo.x, qo.y, qo.z, qo.w);
+    double et = P.e * P.rho;
+    double un = P.u * nx + P.v * ny;
+    double f1[4] = {(et + P.p) * un, P.rho * un, 0.0, 0.0};
+    f1[2] = f1[1] * P.u + P.p * nx;
+    f1[3] = f1[1] * P.v + P.p * ny;
+    Prim Q = con2prim(g, qo.x + dq.x, qo.y + dq.y, qo.z + dq.z, qo.w + dq.w);
+    et = Q.e * Q.rho;
+    un = Q.u * nx + Q.v * ny;
+    double f2[4] = {(et + Q.p) * un, Q.rho * un, 0.0, 0.0};
+    f2[2] = f2[1] * Q.u + Q.p * nx;
+    f2[3] = f2[1] * Q.v + Q.p * ny;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[k] = area * (f2[k] - f1[k]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_lusgs(CCView v, const int* __restrict__ lf_off, const int* __restrict__ lf,
+                                                  int nlf, const int* __restrict__ lb_off, const int* __restrict__ lb,
+                                                  int nlb, GridSync* gs) {
+    const double omega = 1.5;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    if (stopped(v)) return;
+    for (int pass = 0; pass < 2; ++pass) {
+        const int* off = pass == 0 ? lf_off : lb_off;
+        const int* cells = pass == 0 ? lf : lb;
+        int nl = pass == 0 ? nlf : nlb;
+        for (int L = 0; L < nl; ++L) {
+            for (int t = off[L] + tid; t < off[L + 1]; t += nth) {
+                int it = cells[t];
+                double cres[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int k = v.rc2f_off[it]; k < v.rc2f_off[it + 1]; ++k) {
+                    int c = v.rc2f[k];
+                    double2 n = v.fn[c];
+                    double nx = n.x, ny = n.y;
+                    int2 nb = v.fnb[c];
+                    int out = nb.y;
+                    if (out == it) { out = nb.x; nx = -n.x; ny = -n.y; }
+                    bool take = (pass == 0) ? (out < it && out >= 0 && out < v.noc) : (out > it && out >= 0 && out < v.noc);
+                    if (!take) continue;
+                    double4 dq = pass == 0 ? v.lower[out] : v.upper[out];
+                    double df[4];
+                    normal_flux_d(v.g, v.qold[out], dq, nx, ny, v.farea[c], df);
+                    double lam = v.fla[c];
+                    double d[4] = {dq.x, dq.y, dq.z, dq.w};
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + (df[iv] - omega * lam * d[iv]);
+                }
+                double diag = v.cv[it] / v.dt[it] + 0.5 * omega * v.la[it];
+                double r[4];
+                if (pass == 0) {
+                    d4get(v.res[it], r);
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) r[iv] = (-r[iv] - 0.5 * cres[iv]) / diag;
+                    v.lower[it] = d4(r);
+                } else {
+                    double lo[4], o[4], q[4];
+                    d4get(v.lower[it], lo);
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) r[iv] = lo[iv] - 0.5 * cres[iv] / diag;
+                    v.upper[it] = d4(r);
+                    d4get(v.qold[it], o);
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) q[iv] = o[iv] + r[iv];
+                    v.qc[it] = d4(q);
+                }
+            }
+            __threadfence();
+            if (!grid_barrier(gs, v.err)) return;
+        }
+    }
+}
+
+}  // namespace
+
+// ====================================================================== handle
+struct uns_cc_handle {
+    uns_params P;
+    Gas g;
+    CCView v;
+    cudaStream_t stream = nullptr;
+    std::vector<void*> allocs;
+    int nparts = 0;
+    // LU-SGS levels
+    int* lf_off = nullptr; int* lf = nullptr; int nlf = 0;
+    int* lb_off = nullptr; int* lb = nullptr; int nlb = 0;
+    GridSync* gs = nullptr;
+    int coop_blocks = 0;
+    double4 qinf;
+    // graph fast path
+    cudaGraphExec_t graph = nullptr;
+    double* d_cfl = nullptr;
+    int cfl_cap = 0;
+    int* d_iter = nullptr;
+    int* d_done = nullptr;
+    double* d_hist = nullptr;
+    double* d_fres1 = nullptr;
+    double* d_scalar = nullptr;  // [4] scratch for host-visible scalars
+    int graph_first = -1;
+    double cfl_cur = 0.0;  // CFL passed to the last time_step call
+
+    template <class T>
+    int alloc(T*& p, size_t n) {
+        void* q = nullptr;
+        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        UNS_CUDA(cudaMalloc(&q, bytes));
+        UNS_CUDA(cudaMemsetAsync(q, 0, bytes, stream));
+        allocs.push_back(q);
+        p = (T*)q;
+        return UNS_OK;
+    }
+    template <class T>
+    int upload(T*& p, const T* src, size_t n) {
+        int rc = alloc(p, n);
+        if (rc) return rc;
+        if (n) UNS_CUDA(cudaMemcpyAsync(p, src, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+        return UNS_OK;
+    }
+};
+
+namespace {
+
+int check_dev_err(uns_cc_handle* h) {
+    DevErr e;
+    UNS_CUDA(cudaMemcpyAsync(&e, h->v.err, sizeof(DevErr), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    if (e.code != 0) {
+        const char* what = e.code == UNS_ERR_NEG_SOUND_SPEED ? "Roe scheme: sonic speed is negative at face "
+                           : e.code == UNS_ERR_NONPOSITIVE  ? "Density/pressure is negative at cell "
+                           : e.code == UNS_ERR_MESH         ? "ggfc,gradtrixy: -ve area at face "
+                           : e.code == UNS_ERR_TIMEOUT      ? "bounded device wait timed out in block "
+                                                            : "device error at ";
+        set_last_error(std::string(what) + std::to_string(e.index));
+        int code = e.code;
+        DevErr z = {0, 0, 0, 0};
+        UNS_CUDA(cudaMemcpyAsync(h->v.err, &z, sizeof(DevErr), cudaMemcpyHostToDevice, h->stream));
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+        return code;
+    }
+    return UNS_OK;
+}
+
+// Build the forward/backward level schedules of the lusgs2 sweeps: a cell
+// waits for every interior neighbour that precedes it in sweep order.
+void build_levels(int noc, const std::vector<int>& c2f_off, const std::vector<int>& c2f, const int* fin,
+                  const int* fout, bool forward, std::vector<int>& off, std::vector<int>& cells) {
+    std::vector<int> lev(noc, 0);
+    int maxl = 0;
+    for (int s = 0; s < noc; ++s) {
+        int it = forward ? s : noc - 1 - s;
+        int l = 0;
+        for (int k = c2f_off[it]; k < c2f_off[it + 1]; ++k) {
+            int c = c2f[k];
+            int nb = fin[c] == it ? fout[c] : fin[c];
+            if (nb < 0 || nb >= noc || nb == it) continue;
+            if (forward ? nb < it : nb > it) l = std::max(l, lev[nb] + 1);
+        }
+        lev[it] = l;
+        maxl = std::max(maxl, l);
+    }
+    off.assign(maxl + 2, 0);
+    for (int i = 0; i < noc; ++i) off[lev[i] + 1]++;
+    for (int l = 0; l <= maxl; ++l) off[l + 1] += off[l];
+    cells.assign(noc, 0);
+    std::vector<int> pos(off.begin(), off.end() - 1);
+    for (int i = 0; i < noc; ++i) cells[pos[lev[i]]++] = i;
+}
+
+void launch_cfg(int n, dim3& g, dim3& b) { b = dim3(kBlock); g = dim3(std::max(1, nblocks(n))); }
+
+#define LAUNCH(kern, n, ...)                                                         \
+    do {                                                                             \
+        dim3 g_, b_;                                                                 \
+        launch_cfg((n), g_, b_);                                                     \
+        kern<<<g_, b_, 0, h->stream>>>(__VA_ARGS__);                                 \
+        UNS_CUDA(cudaGetLastError());                                                \
+    } while (0)
+
+int enqueue_minmax(uns_cc_handle* h, CCView& v) {
+    k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
+    UNS_CUDA(cudaGetLastError());
+    LAUNCH(k_begin, v.ntot, v, (int)BEGIN_MINMAX);
+    return UNS_OK;
+}
+
+int enqueue_gradient(uns_cc_handle* h, CCView& v, int extra_flags, double cfl, bool do_reduce) {
+    if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
+    int flags = CG_GRAD | extra_flags | (v.ilimit ? CG_LIM : 0);
+    if (v.ilimit && do_reduce) { int rc = enqueue_minmax(h, v); if (rc) return rc; }
+    LAUNCH(k_cell_grad, v.noc, v, flags, cfl);
+    return UNS_OK;
+}
+
+double epsirs_of(const uns_cc_handle* h, double cfl) {
+    double r = cfl / h->P.cfl_max;
+    return std::max(0.25 * (r * r - 1.0), 0.0);
+}
+
+// fvresidual as a kernel sequence; irk > 0 fuses that RK stage into the
+// residual gather (only when no smoothing sweep sits in between).
+int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int partial, bool* fused) {
+    if (h->P.precision == UNS_PREC_MIXED) LAUNCH(k_face_conv<float>, v.nof, v);
+    else LAUNCH(k_face_conv<double>, v.nof, v);
+    if (v.laminar) {
+        LAUNCH(k_cell_mul, v.noc, v);
+        if (v.grad_type != UNS_GRAD_GGFC) {
+            CCView w = v;
+            w.grad_type = UNS_GRAD_GGFC;
+            int rc = enqueue_gradient(h, w, 0, cfl, true);
+            if (rc) return rc;
+        }
+        LAUNCH(k_face_visc, v.nof, v);
+    }
+    double eps = v.irs ? epsirs_of(h, cfl) : 0.0;
+    // With eps == 0 both smoothing sweeps reproduce the residual exactly
+    // ((0*x + r) * 1 == r for finite x), so they are launched only for eps > 0.
+    bool smooth = v.irs && eps > 0.0;
+    *fused = !smooth && irk > 0;
+    LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    if (smooth) {
+        UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
+        LAUNCH(k_cirs, v.noc, v, (const double4*)v.res0, v.restmp, eps);
+        LAUNCH(k_cirs, v.noc, v, (const double4*)v.restmp, v.res, eps);
+        if (partial) LAUNCH(k_res_partial, v.noc, v);
+    }
+    return UNS_OK;
+}
+
+int enqueue_lusgs(uns_cc_handle* h, CCView& v) {
+    UNS_CUDA(cudaMemsetAsync(v.lower, 0, sizeof(double4) * v.noc, h->stream));
+    UNS_CUDA(cudaMemsetAsync(v.upper, 0, sizeof(double4) * v.noc, h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GridSync), h->stream));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(h->coop_blocks);
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = h->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_lusgs, v, (const int*)h->lf_off, (const int*)h->lf, h->nlf,
+                                (const int*)h->lb_off, (const int*)h->lb, h->nlb, h->gs));
+    return UNS_OK;
+}
+
+// The main-loop body (main.F90:60-115) as one kernel sequence.
+int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
+    int rc;
+    k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
+    UNS_CUDA(cudaGetLastError());
+    int bflags = BEGIN_PRIM | BEGIN_OLD | BEGIN_POS | (v.ilimit ? BEGIN_MINMAX : 0);
+    LAUNCH(k_begin, v.ntot, v, bflags);
+    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH(k_face_prim_spec, v.nof, v);
+    if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
+    LAUNCH(k_cell_grad, v.noc, v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.0);
+    if (h->P.time_mode == UNS_TIME_RK3) {
+        for (int irk = 1; irk <= 3; ++irk) {
+            bool fused = false;
+            if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, irk, irk == 3, &fused))) return rc;
+            if (!fused) LAUNCH(k_rk_stage, v.noc, v, irk);
+        }
+    } else {
+        bool fused = false;
+        if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 0, 1, &fused))) return rc;
+        if ((rc = enqueue_lusgs(h, v))) return rc;
+    }
+    k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, nullptr);
+    UNS_CUDA(cudaGetLastError());
+    return UNS_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C-ABI
+extern "C" {
+
+int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out) {
+    if (!m || !p || !out) { set_last_error("uns_cc_create: null argument"); return UNS_ERR_ARG; }
+    *out = nullptr;
+    if (m->nop <= 0 || m->noc <= 0 || m->nfi < 0 || m->nbf < 0) { set_last_error("uns_cc_create: bad sizes"); return UNS_ERR_ARG; }
+    if (p->flux_type < 0 || p->flux_type > 3 || p->grad_type < 0 || p->grad_type > 2 || p->flow_type < 0 ||
+        p->flow_type > 1 || p->time_mode < 0 || p->time_mode > 1 || !(p->m_inf > 0.0)) {
+        set_last_error("uns_cc_create: bad parameters");
+        return UNS_ERR_ARG;
+    }
+    const int nop = m->nop, noc = m->noc, nfi = m->nfi, nbf = m->nbf, nof = nfi + nbf, ntot = noc + nbf;
+    // Validate indices on the host before anything reaches the device.
+    for (int f = 0; f < nof; ++f) {
+        bool ok = m->fin[f] >= 0 && m->fin[f] < noc && m->fp1[f] >= 0 && m->fp1[f] < nop && m->fp2[f] >= 0 && m->fp2[f] < nop;
+        ok = ok && (f < nfi ? (m->fout[f] >= 0 && m->fout[f] < noc) : (m->fout[f] == noc + (f - nfi)));
+        if (!ok) { set_last_error("uns_cc_create: face " + std::to_string(f) + " has an out-of-range index"); return UNS_ERR_MESH; }
+    }
+    for (int i = 0; i < nop; ++i)
+        if (m->v2c_off[i] > m->v2c_off[i + 1]) { set_last_error("uns_cc_create: bad v2c"); return UNS_ERR_MESH; }
+    for (int k = 0; k < m->v2c_off[nop]; ++k)
+        if (m->v2c[k] < 0 || m->v2c[k] >= ntot) { set_last_error("uns_cc_create: v2c index out of range"); return UNS_ERR_MESH; }
+    for (int i = 0; i < noc; ++i)
+        for (int k = m->c2f_off[i]; k < m->c2f_off[i + 1]; ++k)
+            if (m->c2f[k] < 0 || m->c2f[k] >= nof) { set_last_error("uns_cc_create: c2f index out of range"); return UNS_ERR_MESH; }
+
+    uns_cc_handle* h = new uns_cc_handle();
+    h->P = *p;
+    int rc = UNS_OK;
+    auto fail = [&](int code) { uns_cc_destroy(h); return code; };
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_last_error("uns_cc_create: cudaStreamCreate failed (no usable GPU?)");
+        delete h;
+        return UNS_ERR_CUDA;
+    }
+    // Gas constants: math + initialize (CCFVM/read_input.F90:217-262).
+    Gas& g = h->g;
+    g.gamma = 1.4;
+    g.gamma1 = g.gamma - 1.0;
+    double pi = 4.0 * std::atan(1.0);
+    double aoa = p->aoa_deg * pi / 180.0;
+    double q1 = 1.0, q2 = std::cos(aoa) * 1.0, q3 = std::sin(aoa) * 1.0;
+    g.p_inf = 1.0 / (g.gamma * p->m_inf * p->m_inf);
+    double q0 = g.p_inf / (g.gamma - 1.0) + 0.5;
+    g.r_inf = q1;
+    g.a_inf = std::sqrt(g.gamma * g.p_inf / g.r_inf);
+    g.u_inf = q2 / q1;
+    g.v_inf = q3 / q1;
+    g.m_inf = p->m_inf;
+    g.znd = 1.0 / (g.gamma * p->m_inf * p->m_inf);
+    g.T_infd = 300.0;
+    g.SCONST = 110.4;
+    g.t_wall = p->t_wall / g.T_infd;
+    g.rey = p->rey;
+    g.prandtl = 0.72;
+    g.vll = (p->flow_type != UNS_FLOW_INVISCID) ? 2.0 * g.gamma / (g.prandtl * p->rey * 0.25) : 0.0;
+    g.mref = std::max((double)0.32f, 0.5 * p->m_inf);
+    g.flux = p->flux_type;
+    g.flow = p->flow_type;
+    g.iwall = p->iwall;
+    h->qinf = make_double4(q0, q1, q2, q3);
+
+    // Host-side derived connectivity.
+    std::vector<double2> pxy(nop), cen(ntot), fn(nof), fcen(nof);
+    std::vector<int2> fnb(nof), fpt(nof);
+    for (int i = 0; i < nop; ++i) pxy[i] = make_double2(m->px[i], m->py[i]);
+    for (int i = 0; i < ntot; ++i) cen[i] = make_double2(m->cx[i], m->cy[i]);
+    for (int f = 0; f < nof; ++f) {
+        fnb[f] = make_int2(m->fin[f], m->fout[f]);
+        fpt[f] = make_int2(m->fp1[f], m->fp2[f]);
+        fn[f] = make_double2(m->fnx[f], m->fny[f]);
+        fcen[f] = make_double2(m->fcx[f], m->fcy[f]);
+    }
+    std::vector<int> cnt(noc + 1, 0);
+    for (int f = 0; f < nof; ++f) { cnt[m->fin[f] + 1]++; if (m->fout[f] < noc) cnt[m->fout[f] + 1]++; }
+    for (int i = 0; i < noc; ++i) cnt[i + 1] += cnt[i];
+    std::vector<int> cf(cnt[noc]), pos(cnt.begin(), cnt.end() - 1);
+    for (int f = 0; f < nof; ++f) {  // ascending face index per cell
+        cf[pos[m->fin[f]]++] = f;
+        if (m->fout[f] < noc) cf[pos[m->fout[f]]++] = f | SIDE_BIT;
+    }
+    // LSQ weights (gradient.F90:308-369), host-side in the reference's
+    // expression order (-ffp-contract=off translation unit).
+    std::vector<double4> lsw(nof);
+    for (int f = 0; f < nof; ++f) {
+        int in = m->fin[f], o = m->fout[f];
+        double xc = m->cx[in], yc = m->cy[in], xn = m->cx[o], yn = m->cy[o];
+        double dx = xn - xc, dy = yn - yc;
+        double r11 = m->r11[in], r12 = m->r12[in], r22 = m->r22[in];
+        double alfa1 = dx / r11 / r11;
+        double alfa2 = f < nfi ? (dy - dx * r12 / r11) / (r22 * r22) : (dy - dx * r12 / r11) / r22 / r22;
+        double wx0 = alfa1 - alfa2 * r12 / r11, wy0 = alfa2, wx1 = 0.0, wy1 = 0.0;
+        if (f < nfi) {
+            dx = xc - xn; dy = yc - yn;
+            r11 = m->r11[o]; r12 = m->r12[o]; r22 = m->r22[o];
+            alfa1 = dx / r11 / r11;
+            alfa2 = (dy - dx * r12 / r11) / (r22 * r22);
+            wx1 = alfa1 - alfa2 * r12 / r11; wy1 = alfa2;
+        }
+        lsw[f] = make_double4(wx0, wy0, wx1, wy1);
+    }
+    std::vector<int> rc2f_off(m->c2f_off, m->c2f_off + noc + 1);
+    std::vector<int> rc2f(m->c2f, m->c2f + rc2f_off[noc]);
+
+    CCView& v = h->v;
+    std::memset(&v, 0, sizeof(v));
+    v.nop = nop; v.noc = noc; v.nfi = nfi; v.nbf = nbf; v.nof = nof; v.ntot = ntot;
+    v.g = g;
+    v.grad_type = p->grad_type; v.ilimit = p->ilimit; v.irs = p->irs;
+    v.laminar = p->flow_type == UNS_FLOW_LAMINAR;
+    v.cfl_max = p->cfl_max; v.min_res = p->min_res;
+#define UP(field, vec) if ((rc = h->upload(*(std::remove_const<std::remove_pointer<decltype(v.field)>::type>::type**)&v.field, vec.data(), vec.size()))) return fail(rc)
+#define AL(field, n) if ((rc = h->alloc(v.field, (n)))) return fail(rc)
+    UP(pxy, pxy); UP(cen, cen);
+    { std::vector<double> t(m->cv, m->cv + noc); UP(cv, t); }
+    { std::vector<double> t(m->cov, m->cov + noc); UP(cov, t); }
+    UP(fnb, fnb); UP(fpt, fpt); UP(fn, fn); UP(fcen, fcen);
+    { std::vector<double> t(m->farea, m->farea + nof); UP(farea, t); }
+    { std::vector<int> t(m->fbc, m->fbc + nof); UP(fbc, t); }
+    UP(lsw, lsw);
+    { std::vector<int> t(m->nc2c, m->nc2c + noc); UP(nc2c, t); }
+    UP(cf_off, cnt); UP(cf, cf);
+    UP(rc2f_off, rc2f_off); UP(rc2f, rc2f);
+    { std::vector<int> t(m->v2c_off, m->v2c_off + nop + 1); UP(v2c_off, t); }
+    { std::vector<int> t(m->v2c, m->v2c + m->v2c_off[nop]); UP(v2c, t); }
+    { std::vector<double> t(m->v2c_wt, m->v2c_wt + m->v2c_off[nop]); UP(v2c_wt, t); }
+    AL(qc, ntot); AL(qp, ntot); AL(qT, ntot); AL(qold, noc); AL(res, noc); AL(res0, noc); AL(restmp, noc);
+    AL(gx, noc); AL(gy, noc); AL(phi, noc); AL(dt, noc); AL(la, noc); AL(mul, ntot);
+    AL(pp, nop); AL(ppT, nop); AL(fq, nof); AL(fqT, nof); AL(fla, nof); AL(fmu, nof);
+    AL(fF, nof); AL(fV, nof); AL(fgx, nof); AL(fgy, nof); AL(fgT, nof); AL(fasum, nof);
+    AL(fwall, nbf); AL(fwallv, nbf); AL(lower, noc); AL(upper, noc);
+    AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
+    h->nparts = nblocks(noc);
+    AL(partial, h->nparts);
+    if ((rc = h->alloc(h->d_scalar, 4))) return fail(rc);
+    if ((rc = h->alloc(h->d_iter, 1))) return fail(rc);
+    if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
+    if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
+    if ((rc = h->alloc(h->gs, 1))) return fail(rc);
+    // LU-SGS level schedule on the reference cell order.
+    {
+        std::vector<int> off, cells;
+        std::vector<int> c2fo(m->c2f_off, m->c2f_off + noc + 1), c2fv(m->c2f, m->c2f + m->c2f_off[noc]);
+        build_levels(noc, c2fo, c2fv, m->fin, m->fout, true, off, cells);
+        h->nlf = (int)off.size() - 1;
+        if ((rc = h->upload(h->lf_off, off.data(), off.size()))) return fail(rc);
+        if ((rc = h->upload(h->lf, cells.data(), cells.size()))) return fail(rc);
+        build_levels(noc, c2fo, c2fv, m->fin, m->fout, false, off, cells);
+        h->nlb = (int)off.size() - 1;
+        if ((rc = h->upload(h->lb_off, off.data(), off.size()))) return fail(rc);
+        if ((rc = h->upload(h->lb, cells.data(), cells.size()))) return fail(rc);
+        int dev = 0, nsm = 0, per = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lusgs, kBlock, 0) != cudaSuccess || per < 1) {
+            set_last_error("uns_cc_create: cannot size the cooperative LU-SGS launch");
+            return fail(UNS_ERR_CUDA);
+        }
+        h->coop_blocks = nsm * std::min(per, 2);
+    }
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { set_last_error("uns_cc_create: upload failed"); return fail(UNS_ERR_CUDA); }
+    rc = uns_cc_initialize(h);
+    if (rc) return fail(rc);
+    *out = h;
+    return UNS_OK;
+#undef UP
+#undef AL
+}
+
+int uns_cc_destroy(uns_cc_handle* h) {
+    if (!h) return UNS_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->d_cfl) cudaFree(h->d_cfl);
+    if (h->d_hist) cudaFree(h->d_hist);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return UNS_OK;
+}
+
+int uns_cc_initialize(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    k_initialize<<<nblocks(v.ntot), kBlock, 0, h->stream>>>(v, h->qinf);
+    UNS_CUDA(cudaGetLastError());
+    UNS_CUDA(cudaMemsetAsync(v.mul, 0, sizeof(double) * v.ntot, h->stream));
+    UNS_CUDA(cudaMemsetAsync(v.fmu, 0, sizeof(double) * v.nof, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return UNS_OK;
+}
+
+int uns_cc_set_state(uns_cc_handle* h, const double* qc) {
+    if (!h || !qc) return UNS_ERR_ARG;
+    UNS_CUDA(cudaMemcpyAsync(h->v.qc, qc, sizeof(double4) * h->v.ntot, cudaMemcpyHostToDevice, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return UNS_OK;
+}
+
+int uns_cc_get_state(uns_cc_handle* h, double* qc) {
+    if (!h || !qc) return UNS_ERR_ARG;
+    UNS_CUDA(cudaMemcpyAsync(qc, h->v.qc, sizeof(double4) * h->v.ntot, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return UNS_OK;
+}
+
+int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
+    if (!h || !out) return UNS_ERR_ARG;
+    const CCView& v = h->v;
+    auto d2h = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
+    };
+    auto interleave = [&](const double4* a, const double* b, int n, int stride5) -> int {
+        std::vector<double4> A(n);
+        std::vector<double> B(n);
+        UNS_CUDA(d2h(A.data(), a, sizeof(double4) * n));
+        UNS_CUDA(d2h(B.data(), b, sizeof(double) * n));
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+        for (int i = 0; i < n; ++i) {
+            double* o = out + (size_t)i * stride5;
+            o[0] = A[i].x; o[1] = A[i].y; o[2] = A[i].z; o[3] = A[i].w; o[4] = B[i];
+        }
+        return UNS_OK;
+    };
+    switch (field) {
+        case UNS_CC_QC: UNS_CUDA(d2h(out, v.qc, sizeof(double4) * v.ntot)); break;
+        case UNS_CC_QP: return interleave(v.qp, v.qT, v.ntot, 5);
+        case UNS_CC_QOLD: UNS_CUDA(d2h(out, v.qold, sizeof(double4) * v.noc)); break;
+        case UNS_CC_RES: UNS_CUDA(d2h(out, v.res, sizeof(double4) * v.noc)); break;
+        case UNS_CC_PHI: UNS_CUDA(d2h(out, v.phi, sizeof(double4) * v.noc)); break;
+        case UNS_CC_DT: UNS_CUDA(d2h(out, v.dt, sizeof(double) * v.noc)); break;
+        case UNS_CC_LA: UNS_CUDA(d2h(out, v.la, sizeof(double) * v.noc)); break;
+        case UNS_CC_FLA: UNS_CUDA(d2h(out, v.fla, sizeof(double) * v.nof)); break;
+        case UNS_CC_FMU: UNS_CUDA(d2h(out, v.fmu, sizeof(double) * v.nof)); break;
+        case UNS_CC_MUL: UNS_CUDA(d2h(out, v.mul, sizeof(double) * v.noc)); break;
+        case UNS_CC_PTPRIM: return interleave(v.pp, v.ppT, v.nop, 5);
+        case UNS_CC_FQP: return interleave(v.fq, v.fqT, v.nof, 5);
+        case UNS_CC_GRAD: {
+            std::vector<double4> X(v.noc), Y(v.noc);
+            UNS_CUDA(d2h(X.data(), v.gx, sizeof(double4) * v.noc));
+            UNS_CUDA(d2h(Y.data(), v.gy, sizeof(double4) * v.noc));
+            UNS_CUDA(cudaStreamSynchronize(h->stream));
+            for (int i = 0; i < v.noc; ++i) {
+                double a[4] = {X[i].x, X[i].y, X[i].z, X[i].w}, b[4] = {Y[i].x, Y[i].y, Y[i].z, Y[i].w};
+                for (int j = 0; j < 4; ++j) { out[(size_t)i * 8 + 2 * j] = a[j]; out[(size_t)i * 8 + 2 * j + 1] = b[j]; }
+            }
+            return UNS_OK;
+        }
+        case UNS_CC_FGRAD: {
+            std::vector<double4> X(v.nof), Y(v.nof);
+            std::vector<double2> T(v.nof);
+            UNS_CUDA(d2h(X.data(), v.fgx, sizeof(double4) * v.nof));
+            UNS_CUDA(d2h(Y.data(), v.fgy, sizeof(double4) * v.nof));
+            UNS_CUDA(d2h(T.data(), v.fgT, sizeof(double2) * v.nof));
+            UNS_CUDA(cudaStreamSynchronize(h->stream));
+            for (int f = 0; f < v.nof; ++f) {
+                double a[5] = {X[f].x, X[f].y, X[f].z, X[f].w, T[f].x}, b[5] = {Y[f].x, Y[f].y, Y[f].z, Y[f].w, T[f].y};
+                for (int j = 0; j < 5; ++j) { out[(size_t)f * 10 + 2 * j] = a[j]; out[(size_t)f * 10 + 2 * j + 1] = b[j]; }
+            }
+            return UNS_OK;
+        }
+        default: set_last_error("uns_cc_get_field: unknown field"); return UNS_ERR_ARG;
+    }
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return UNS_OK;
+}
+
+int uns_cc_con2prim(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    LAUNCH(k_begin, v.noc, v, (int)BEGIN_PRIM);
+    return UNS_OK;
+}
+
+int uns_cc_avg_c2v(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH(k_face_prim_spec, v.nof, v);
+    return UNS_OK;
+}
+
+int uns_cc_time_step(uns_cc_handle* h, double cfl, double* dtglobal) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    h->cfl_cur = cfl;  // cirs of this iteration uses the same CFL
+    k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
+    UNS_CUDA(cudaGetLastError());
+    LAUNCH(k_cell_grad, v.noc, v, (int)CG_DT, cfl);
+    if (dtglobal) {
+        unsigned long long e = 0;
+        UNS_CUDA(cudaMemcpyAsync(&e, v.dtmin, 8, cudaMemcpyDeviceToHost, h->stream));
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+        *dtglobal = std::min(1.0e20, dec_ord(e));
+    }
+    return UNS_OK;
+}
+
+int uns_cc_save_old(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    LAUNCH(k_begin, v.noc, v, (int)BEGIN_OLD);
+    return UNS_OK;
+}
+
+int uns_cc_gradient(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    return enqueue_gradient(h, v, 0, 0.0, true);
+}
+
+int uns_cc_limit(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    int rc = enqueue_minmax(h, v);
+    if (rc) return rc;
+    LAUNCH(k_cell_grad, v.noc, v, (int)CG_LIM, 0.0);
+    return UNS_OK;
+}
+
+int uns_cc_fvresidual(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    bool fused = false;
+    return enqueue_fvresidual(h, v, h->cfl_cur, 0, 0, &fused);
+}
+
+int uns_cc_rk_stage(uns_cc_handle* h, int irk) {
+    if (!h || irk < 1 || irk > 3) return UNS_ERR_ARG;
+    CCView v = h->v;
+    LAUNCH(k_rk_stage, v.noc, v, irk);
+    return UNS_OK;
+}
+
+int uns_cc_lusgs(uns_cc_handle* h) {
+    if (!h) return UNS_ERR_ARG;
+    int rc = uns_cc_fvresidual(h);
+    if (rc) return rc;
+    CCView v = h->v;
+    return enqueue_lusgs(h, v);
+}
+
+int uns_cc_check_positivity(uns_cc_handle* h, int* bad) {
+    if (!h) return UNS_ERR_ARG;
+    CCView v = h->v;
+    int rc = check_dev_err(h);
+    if (rc) { if (bad) *bad = -1; return rc; }
+    LAUNCH(k_check_pos, v.noc, v);
+    DevErr e;
+    UNS_CUDA(cudaMemcpyAsync(&e, v.err, sizeof(DevErr), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) *bad = e.code == UNS_ERR_NONPOSITIVE ? e.index : -1;
+    return check_dev_err(h);
+}
+
+int uns_cc_residue(uns_cc_handle* h, double* fres) {
+    if (!h || !fres) return UNS_ERR_ARG;
+    CCView v = h->v;
+    LAUNCH(k_res_partial, v.noc, v);
+    k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);
+    UNS_CUDA(cudaGetLastError());
+    UNS_CUDA(cudaMemcpyAsync(fres, h->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return check_dev_err(h);
+}
+
+int uns_cc_forces(uns_cc_handle* h, double* fx, double* fy) {
+    if (!h || !fx || !fy) return UNS_ERR_ARG;
+    k_forces<<<1, 1, 0, h->stream>>>(h->v, h->d_scalar);
+    UNS_CUDA(cudaGetLastError());
+    double r[2];
+    UNS_CUDA(cudaMemcpyAsync(r, h->d_scalar, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    *fx = r[0];
+    *fy = r[1];
+    return UNS_OK;
+}
+
+int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
+    if (!h || niter < 0 || (niter > 0 && (!cfl || !fres_raw))) return UNS_ERR_ARG;
+    if (done_iters) *done_iters = 0;
+    if (niter == 0) return UNS_OK;
+    if (niter > h->cfl_cap) {
+        if (h->d_cfl) cudaFree(h->d_cfl);
+        if (h->d_hist) cudaFree(h->d_hist);
+        h->d_cfl = nullptr; h->d_hist = nullptr;
+        UNS_CUDA(cudaMalloc(&h->d_cfl, sizeof(double) * niter));
+        UNS_CUDA(cudaMalloc(&h->d_hist, sizeof(double) * niter));
+        h->cfl_cap = niter;
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    }
+    // The smoothing sweeps are launched only while their coefficient is
+    // non-zero; the schedule must agree on that for the whole chunk.
+    bool any_smooth = false, all_smooth = true;
+    for (int k = 0; k < niter; ++k) {
+        bool s = h->P.irs && epsirs_of(h, cfl[k]) > 0.0;
+        any_smooth = any_smooth || s;
+        all_smooth = all_smooth && s;
+    }
+    if (any_smooth) {
+        // Residual smoothing with a CFL above CFLmax changes the sweep
+        // weights per iteration: run the chunk through the per-call path.
+        double f1 = 0.0;
+        int done = 0;
+        for (int k = 0; k < niter; ++k) {
+            int rc;
+            if ((rc = uns_cc_con2prim(h)) || (rc = uns_cc_avg_c2v(h)) || (rc = uns_cc_time_step(h, cfl[k], nullptr)) ||
+                (rc = uns_cc_save_old(h)) || (rc = uns_cc_gradient(h)))
+                return rc;
+            if (h->P.time_mode == UNS_TIME_RK3) {
+                for (int irk = 1; irk <= 3; ++irk)
+                    if ((rc = uns_cc_fvresidual(h)) || (rc = uns_cc_rk_stage(h, irk))) return rc;
+            } else if ((rc = uns_cc_lusgs(h))) return rc;
+            int bad;
+            if ((rc = uns_cc_check_positivity(h, &bad))) return rc;
+            if ((rc = uns_cc_residue(h, &fres_raw[k]))) return rc;
+            ++done;
+            if (first_iter && k == 0) f1 = fres_raw[0];
+            double nf = (f1 >= 2.220446049250313e-16) ? fres_raw[k] / f1 : fres_raw[k];
+            if (!(nf > h->P.min_res)) break;
+        }
+        if (done_iters) *done_iters = done;
+        return UNS_OK;
+    }
+    (void)all_smooth;
+    UNS_CUDA(cudaMemcpyAsync(h->d_cfl, cfl, sizeof(double) * niter, cudaMemcpyHostToDevice, h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_iter, 0, sizeof(int), h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_done, 0, sizeof(int), h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_hist, 0, sizeof(double) * niter, h->stream));
+    if (!h->graph || h->graph_first != (first_iter ? 1 : 0)) {
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+        CCView v = h->v;
+        v.cfl_sched = h->d_cfl;
+        v.iter = h->d_iter;
+        v.done = h->d_done;
+        v.fres_hist = h->d_hist;
+        v.fres1 = h->d_fres1;
+        v.first_iter = first_iter ? 1 : 0;
+        cudaGraph_t graph;
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+        UNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = enqueue_iteration(h, v, 0.0);
+        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        if (rc) return rc;
+        if (ce != cudaSuccess) { set_last_error(std::string("graph capture: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
+        ce = cudaGraphInstantiate(&h->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) { set_last_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
+        h->graph_first = first_iter ? 1 : 0;
+    }
+    for (int k = 0; k < niter; ++k) UNS_CUDA(cudaGraphLaunch(h->graph, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(fres_raw, h->d_hist, sizeof(double) * niter, cudaMemcpyDeviceToHost, h->stream));
+    int it = 0;
+    UNS_CUDA(cudaMemcpyAsync(&it, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    if (done_iters) *done_iters = it;
+    return check_dev_err(h);
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+"""Caller-side meshes: analytic airfoil O-meshes and geometry.inp files, after the
+reference's geometric preprocessing (libunsflow_host.so)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+class _HostMesh:
+    kind = ""
+
+    def __init__(self, handle: int):
+        self._lib = abi.host_lib()
+        self._h = C.c_void_p(handle)
+        view_t = abi.CCMeshView if self.kind == "cc" else abi.NCMeshView
+        v = view_t()
+        fn = getattr(self._lib, f"uns_host_{self.kind}_view")
+        abi.check(fn(self._h, C.byref(v)), self._lib, "view")
+        self.arrays = abi.cc_view_arrays(v) if self.kind == "cc" else abi.nc_view_arrays(v)
+
+    @classmethod
+    def airfoil(cls, ni: int, nj: int, thickness: float = 0.12, rfar: float = 20.0, dwall: float = 1e-3):
+        lib = abi.host_lib()
+        h = C.c_void_p()
+        fn = getattr(lib, f"uns_host_{cls.kind}_airfoil")
+        abi.check(fn(ni, nj, thickness, rfar, dwall, C.byref(h)), lib, f"{cls.kind} airfoil")
+        return cls(h.value)
+
+    @classmethod
+    def read(cls, path: str):
+        lib = abi.host_lib()
+        h = C.c_void_p()
+        fn = getattr(lib, f"uns_host_{cls.kind}_read")
+        abi.check(fn(str(path).encode(), C.byref(h)), lib, f"read {path}")
+        return cls(h.value)
+
+    def write(self, path: str) -> None:
+        fn = getattr(self._lib, f"uns_host_{self.kind}_write")
+        abi.check(fn(self._h, str(path).encode()), self._lib, f"write {path}")
+
+    def newnum(self) -> np.ndarray:
+        n = self.arrays["noc"] if self.kind == "cc" else self.arrays["nop"]
+        out = np.zeros(n, dtype=np.int32)
+        fn = getattr(self._lib, f"uns_host_{self.kind}_newnum")
+        abi.check(fn(self._h, out.ctypes.data_as(C.POINTER(C.c_int32))), self._lib, "newnum")
+        return out
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+    def close(self) -> None:
+        if self._h:
+            getattr(self._lib, f"uns_host_{self.kind}_free")(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CCMesh(_HostMesh):
+    """Cell-centred mesh (CCFVM geometry.inp + CCFVM/geometric.F90)."""
+    kind = "cc"
+
+    @property
+    def ncells(self) -> int:
+        return self.arrays["noc"]
+
+
+class NCMesh(_HostMesh):
+    """Vertex-centred median-dual mesh (NCFVM geometry.inp + NCFVM/geometric.f90)."""
+    kind = "nc"
+
+    @property
+    def nnodes(self) -> int:
+        return self.arrays["nop"]
+
+
+def read_flo_inp(path: str, kind: str = "cc") -> tuple[abi.Params, str]:
+    lib = abi.host_lib()
+    p = abi.Params()
+    grid = C.create_string_buffer(256)
+    fn = lib.uns_host_read_flo_cc if kind == "cc" else lib.uns_host_read_flo_nc
+    abi.check(fn(str(path).encode(), C.byref(p), grid, 256), lib, f"flo.inp {path}")
+    return p, grid.value.decode()
+
+
+def cfl_schedule(p: abi.Params, first: int, n: int, kind: str = "cc", prev: float = 0.0) -> np.ndarray:
+    """CFL of iterations first..first+n-1 (CCFVM/main.F90:148-168, NCFVM/main.f90:316)."""
+    lib = abi.host_lib()
+    out = np.zeros(n)
+    c = prev
+    for k in range(n):
+        if kind == "cc":
+            c = lib.uns_host_cfl_cc(C.byref(p), first + k, c)
+        else:
+            c = lib.uns_host_cfl_nc(C.byref(p), first + k)
+        out[k] = c
+    return out
+
+
+def run_main(flo_inp: str, outdir: str, kind: str = "cc", mode: int = 1) -> tuple[int, float]:
+    """Reference main program on the GPU library; writes outdir/FLO.RES."""
+    lib = abi.host_lib()
+    it = C.c_int()
+    fr = C.c_double()
+    fn = lib.uns_host_cc_main if kind == "cc" else lib.uns_host_nc_main
+    abi.check(fn(str(flo_inp).encode(), str(outdir).encode(), mode, C.byref(it), C.byref(fr)), lib, "main")
+    return it.value, fr.value

@@ -1,0 +1,196 @@
+"""Python face of the GB300 drop-in: one class per solver, one method per
+reference subroutine, each a thin call into libunsflow_gpu.so.
+
+The method names follow the Fortran routines they replace (fvresidual,
+gradient, limit, time_step, lusgs, residue ...), so a test reads like the
+reference main loop.  Nothing here computes: a missing library or a CUDA error
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class _Solver:
+    kind = ""
+    fields: dict = {}
+
+    def _call(self, name: str, *args):
+        rc = getattr(self._lib, f"uns_{self.kind}_{name}")(self._h, *args)
+        abi.check(rc, self._lib, f"uns_{self.kind}_{name}")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            getattr(self._lib, f"uns_{self.kind}_destroy")(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def initialize(self):
+        self._call("initialize")
+
+    def set_state(self, qc: np.ndarray):
+        a = np.ascontiguousarray(qc, dtype=np.float64)
+        assert a.size == self.nstate * 4
+        self._call("set_state", _dp(a))
+
+    def get_state(self) -> np.ndarray:
+        out = np.zeros((self.nstate, 4))
+        self._call("get_state", _dp(out))
+        return out
+
+    def get(self, field: str) -> np.ndarray:
+        shape = self._field_shape(field)
+        out = np.zeros(shape)
+        self._call("get_field", self.fields[field], _dp(out))
+        return out
+
+
+class CCSolver(_Solver):
+    """Cell-centred solver (CCFVM hot path) on the GPU."""
+    kind = "cc"
+    fields = abi.CC_FIELDS
+
+    def __init__(self, mesh, params: abi.Params):
+        self._lib = abi.gpu_lib()
+        arr = mesh.arrays if hasattr(mesh, "arrays") else mesh
+        self.m = arr
+        view, self._keep = abi.cc_view_from_arrays(arr)
+        h = C.c_void_p()
+        abi.check(self._lib.uns_cc_create(C.byref(view), C.byref(params), C.byref(h)), self._lib, "uns_cc_create")
+        self._h = h
+        self.params = params
+        self.noc, self.nbf = arr["noc"], arr["nbf"]
+        self.nstate = self.noc + self.nbf
+
+    def _field_shape(self, f):
+        m = self.m
+        nof = m["nfi"] + m["nbf"]
+        return {"qc": (self.nstate, 4), "qp": (self.nstate, 5), "qold": (self.noc, 4), "res": (self.noc, 4),
+                "grad": (self.noc, 4, 2), "phi": (self.noc, 4), "dt": (self.noc,), "la": (self.noc,),
+                "ptprim": (m["nop"], 5), "fqp": (nof, 5), "fla": (nof,), "fmu": (nof,),
+                "fgrad": (nof, 5, 2), "mul": (self.noc,)}[f]
+
+    # one method per reference subroutine
+    def con2prim(self): self._call("con2prim")
+    def avg_c2v(self): self._call("avg_c2v")
+    def save_old(self): self._call("save_old")
+    def gradient(self): self._call("gradient")
+    def limit(self): self._call("limit")
+    def fvresidual(self): self._call("fvresidual")
+    def rk_stage(self, irk: int): self._call("rk_stage", irk)
+    def lusgs(self): self._call("lusgs")
+
+    def time_step(self, cfl: float) -> float:
+        d = C.c_double()
+        self._call("time_step", C.c_double(cfl), C.byref(d))
+        return d.value
+
+    def check_positivity(self) -> int:
+        bad = C.c_int(-1)
+        self._call("check_positivity", C.byref(bad))
+        return bad.value
+
+    def residue(self) -> float:
+        d = C.c_double()
+        self._call("residue", C.byref(d))
+        return d.value
+
+    def forces(self) -> tuple[float, float]:
+        fx, fy = C.c_double(), C.c_double()
+        self._call("forces", C.byref(fx), C.byref(fy))
+        return fx.value, fy.value
+
+    def iteration(self, cfl: float) -> float:
+        """One main-loop iteration (CCFVM/main.F90:60-115) through the per-routine entry points."""
+        self.con2prim()
+        self.avg_c2v()
+        self.time_step(cfl)
+        self.save_old()
+        self.gradient()
+        if self.params.time_mode == abi.TIME["rk3"]:
+            for irk in (1, 2, 3):
+                self.fvresidual()
+                self.rk_stage(irk)
+        else:
+            self.lusgs()
+        self.check_positivity()
+        return self.residue()
+
+    def iterate(self, cfl: np.ndarray, first_iter: bool) -> np.ndarray:
+        """Graph-replayed iterations; returns the raw residual norms of the iterations run."""
+        cfl = np.ascontiguousarray(cfl, dtype=np.float64)
+        out = np.zeros(len(cfl))
+        done = C.c_int()
+        self._call("iterate", len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), C.byref(done))
+        return out[:done.value]
+
+
+class NCSolver(_Solver):
+    """Vertex-centred median-dual solver (NCFVM hot path) on the GPU."""
+    kind = "nc"
+    fields = abi.NC_FIELDS
+
+    def __init__(self, mesh, params: abi.Params):
+        self._lib = abi.gpu_lib()
+        arr = mesh.arrays if hasattr(mesh, "arrays") else mesh
+        self.m = arr
+        view, self._keep = abi.nc_view_from_arrays(arr)
+        h = C.c_void_p()
+        abi.check(self._lib.uns_nc_create(C.byref(view), C.byref(params), C.byref(h)), self._lib, "uns_nc_create")
+        self._h = h
+        self.params = params
+        self.nop = arr["nop"]
+        self.nstate = self.nop
+
+    def _field_shape(self, f):
+        return {"qc": (self.nop, 4), "qp": (self.nop, 4), "qold": (self.nop, 4), "res": (self.nop, 4),
+                "grad": (self.nop, 4, 2), "phi": (self.nop, 4), "dt": (self.nop,), "la": (self.nop,),
+                "fla": (self.m["nof"],)}[f]
+
+    def save_old(self): self._call("save_old")
+    def fvresidual(self, cfl: float): self._call("fvresidual", C.c_double(cfl))
+    def rk_stage(self, irk: int): self._call("rk_stage", irk)
+    def lusgs(self, cfl: float): self._call("lusgs", C.c_double(cfl))
+
+    def residue(self) -> tuple[float, float, int]:
+        f, fi, ii = C.c_double(), C.c_double(), C.c_int()
+        self._call("residue", C.byref(f), C.byref(fi), C.byref(ii))
+        return f.value, fi.value, ii.value
+
+    def iteration(self, cfl: float) -> tuple[float, float, int]:
+        """One main-loop iteration (NCFVM/main.f90:315-347)."""
+        self.save_old()
+        if self.params.time_mode == abi.TIME["rk3"]:
+            for irk in (1, 2, 3):
+                self.fvresidual(cfl)
+                self.rk_stage(irk)
+        else:
+            self.lusgs(cfl)
+        return self.residue()
+
+    def iterate(self, cfl: np.ndarray, first_iter: bool) -> tuple[np.ndarray, np.ndarray]:
+        cfl = np.ascontiguousarray(cfl, dtype=np.float64)
+        out = np.zeros(len(cfl))
+        outi = np.zeros(len(cfl))
+        done = C.c_int()
+        self._call("iterate", len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), _dp(outi), C.byref(done))
+        return out[:done.value], outi[:done.value]
