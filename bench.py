@@ -1,0 +1,390 @@
+#!/usr/bin/env python3
+"""UNSFlow2D hot-path benchmark on GB300.
+
+Workload (one "step" = one iteration of the solver main loop over the whole
+mesh): NCFVM vertex-centred median-dual Euler on the analytic 12%-thick
+4-digit airfoil, 1024x512 O-mesh split to 1,048,576 triangles (525,312 nodes),
+Mach 0.8, alpha 1.25 deg, AUSM+-up flux, LSQ gradient + Barth limiter, LU-SGS
+with CFL 50, FP64.  Metric: Mcell-iter/s (NCFVM counts nodes) -- whole-job
+throughput, inputs resident in HBM.  `e2e` is the same metric through the
+reference-facing per-routine C-ABI calls with the state copied host->device
+and back every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--workload nc|cc|cc_mixed|nc_mixed]
+
+Multi-GPU: N independent replicas (the LU-SGS sweep order is global, so the
+path does not shard without changing results); value = all ranks' node
+iterations / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+from unsflow2d_gb300 import abi, mesh, replicas  # noqa: E402
+
+METRIC = "Mcell-iter/s & time to 1e-8 residual drop: FP64 plain vs batched/mixed, 1 GB300"
+UNIT = "Mcell-iter/s"
+
+WORKLOADS = {
+    "nc": dict(kind="nc", ni=1024, nj=512, dwall=1e-3,
+               params=dict(m_inf=0.8, aoa_deg=1.25, flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0,
+                           min_res=0.0),
+               desc="NCFVM median-dual Euler, 1024x512 O-mesh split to 1,048,576 triangles (525,312 nodes), "
+                    "M0.8 a1.25, AUSM+-up, LSQ + Barth, LU-SGS CFL 50, FP64"),
+    "nc_mixed": dict(kind="nc", ni=1024, nj=512, dwall=1e-3,
+                     params=dict(m_inf=0.8, aoa_deg=1.25, flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0,
+                                 min_res=0.0, precision="mixed"),
+                     desc="as nc with FP32 face reconstruction + flux, FP64 accumulation"),
+    "cc": dict(kind="cc", ni=2048, nj=1024, dwall=1e-3,
+               params=dict(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0),
+               desc="CCFVM Euler, 2048x1024 O-mesh split to 4,194,304 triangles, M0.75 a2, Roe, GG + VKN, RK3, FP64"),
+    "cc_mixed": dict(kind="cc", ni=2048, nj=1024, dwall=1e-3,
+                     params=dict(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9,
+                                 min_res=0.0, precision="mixed"),
+                     desc="as cc with FP32 face reconstruction + flux, FP64 accumulation"),
+}
+
+# Kernels launched per iteration (our own; memsets excluded).
+LAUNCHES = {("nc", "lusgs"): 7, ("nc", "rk3"): 11, ("cc", "rk3"): 12, ("cc", "lusgs"): 10}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- bytes model
+def algorithmic_bytes(kind: str, m: dict) -> dict:
+    """Unique bytes each kernel must move per launch: every array it touches
+    counted once at its full size, no credit for reuse (the design doc table)."""
+    if kind == "nc":
+        N, E = m["nop"], m["nof"]
+        B = int((m["fbc"] != 0).sum())
+        return {
+            "save_old": 96 * N,
+            "grad_lim": 192 * N + 56 * E,
+            "edge": 144 * N + 80 * E + 80 * B,
+            "node_res": 60 * N + 56 * E + 80 * B,
+            "fold": 32 * N + 96 * E,
+            "lusgs_sweeps": 228 * N + 112 * E,
+            "residue": 16 * ((N + 255) // 256),
+        }
+    N, F, P = m["noc"], m["nfi"] + m["nbf"], m["nop"]
+    G = m["nbf"]
+    return {
+        "begin": 32 * N + 32 * N + 8 * N + 32 * N + 40 * G,
+        "vertex_avg": 40 * (N + G) + 4 * P + 12 * len(m["v2c"]) + 40 * P,
+        "face_prim_spec": 8 * F + 40 * P + 40 * F + 24 * F + 8 * F + 8 * F,
+        "face_ggfc": 8 * F * 2 + 16 * P + 16 * (N + G) + 40 * P + 40 * (N + G) + 88 * F,
+        "cell_grad": 4 * N + 12 * N + 8 * F + 40 * F + 24 * F + 16 * N + 64 * N + 32 * N + 40 * P + 16 * F + 32 * N * 2,
+        "face_conv": 8 * F + 24 * F + 16 * F + 4 * G + 16 * (N + G) + 32 * (N + G) + 64 * N + 32 * N + 32 * F + 72 * G,
+        "cell_res": 16 * N + 32 * F + 32 * N * 4 + 16 * N,
+        "residue": 8 * ((N + 255) // 256),
+    }
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self) -> dict:
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.count(",") >= 8]
+        try:
+            os.unlink(self.f.name)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if "Active" in r[5 + k] and "Not" not in r[5 + k]:
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- runs
+def build_mesh(w):
+    cls = mesh.NCMesh if w["kind"] == "nc" else mesh.CCMesh
+    return cls.airfoil(w["ni"], w["nj"], 0.12, 20.0, w["dwall"])
+
+
+def units_of(w, m) -> int:
+    return m["nop"] if w["kind"] == "nc" else m["noc"]
+
+
+def cfl_list(p, kind, first, n):
+    return mesh.cfl_schedule(p, first, n, kind)
+
+
+def run_ours(args, w, dist, rank, local_rank) -> dict | None:
+    import torch
+    from unsflow2d_gb300.solver import CCSolver, NCSolver
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    t0 = time.time()
+    m = build_mesh(w)
+    p = abi.make_params(**w["params"])
+    S = NCSolver if w["kind"] == "nc" else CCSolver
+    solver = S(m, p)
+    setup_s = time.time() - t0
+    units = units_of(w, m)
+    kind = w["kind"]
+    it = 0
+
+    def iterate(n):
+        nonlocal it
+        c = cfl_list(p, kind, it + 1, n)
+        r = solver.iterate(c, first_iter=(it == 0))
+        it += n
+        f = r if kind == "cc" else r[0]
+        if len(f) != n or not np.isfinite(f).all():
+            raise RuntimeError(f"solver stopped or diverged: {len(f)} of {n} iterations, last norm {f[-1:]}")
+        return r
+
+    iterate(args.warmup)
+    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    replicas.barrier(dist, local_rank)
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        iterate(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    replicas.barrier(dist, local_rank)
+    ms = e0.elapsed_time(e1)
+    tot_units, secs = replicas.reduce_timing(dist, units * args.steps, ms / 1e3, device=str(dev))
+    value = tot_units / secs / 1e6
+
+    # End to end through the per-routine C-ABI (the calls a Fortran driver
+    # makes), with the state in pinned host memory copied in and out each step.
+    lib = abi.gpu_lib()
+    n_e2e = 0 if args.no_e2e else max(3, min(args.steps, 20))
+    host_in = torch.empty((solver.nstate, 4), dtype=torch.float64, pin_memory=True)
+    host_out = torch.empty((solver.nstate, 4), dtype=torch.float64, pin_memory=True)
+    host_in.copy_(torch.from_numpy(solver.get_state()))
+    h = solver._h
+    dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
+    fres = C.c_double()
+    fresi, iresi = C.c_double(), C.c_int()
+    cfls = cfl_list(p, kind, it + 1, n_e2e)
+    replicas.barrier(dist, local_rank)
+    torch.cuda.synchronize()
+    t_e0 = time.perf_counter()
+    lusgs = p.time_mode == abi.TIME["lusgs"]
+    for k in range(n_e2e):
+        c = float(cfls[k])
+        if kind == "nc":
+            calls = [lambda: lib.uns_nc_set_state(h, dp(host_in)), lambda: lib.uns_nc_save_old(h)]
+            if lusgs:
+                calls.append(lambda: lib.uns_nc_lusgs(h, c))
+            else:
+                for irk in (1, 2, 3):
+                    calls += [lambda: lib.uns_nc_fvresidual(h, c), lambda irk=irk: lib.uns_nc_rk_stage(h, irk)]
+            calls += [lambda: lib.uns_nc_residue(h, C.byref(fres), C.byref(fresi), C.byref(iresi)),
+                      lambda: lib.uns_nc_get_state(h, dp(host_out))]
+        else:
+            calls = [lambda: lib.uns_cc_set_state(h, dp(host_in)), lambda: lib.uns_cc_con2prim(h),
+                     lambda: lib.uns_cc_avg_c2v(h), lambda: lib.uns_cc_time_step(h, c, None),
+                     lambda: lib.uns_cc_save_old(h), lambda: lib.uns_cc_gradient(h)]
+            if lusgs:
+                calls.append(lambda: lib.uns_cc_lusgs(h))
+            else:
+                for irk in (1, 2, 3):
+                    calls += [lambda: lib.uns_cc_fvresidual(h), lambda irk=irk: lib.uns_cc_rk_stage(h, irk)]
+            calls += [lambda: lib.uns_cc_residue(h, C.byref(fres)), lambda: lib.uns_cc_get_state(h, dp(host_out))]
+        for call in calls:
+            rc = call()
+            if rc:
+                raise abi.UnsError(rc, lib.uns_last_error().decode())
+        host_in.copy_(host_out)
+    e2e_s = max(time.perf_counter() - t_e0, 1e-9)
+    tot_e2e, e2e_s = replicas.reduce_timing(dist, units * n_e2e, e2e_s, device=str(dev))
+    state_bytes = solver.nstate * 32
+    e2e = {"value": tot_e2e / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+           "d2h_bytes_per_step": state_bytes + (24 if kind == "nc" else 8), "steps": n_e2e,
+           "path": "per-routine C-ABI calls (reference main-loop order), pinned host state in/out each step"}
+
+    # Per-kernel device times (CUDA events on the library stream) -> roofline.
+    prof = solver.profile(float(cfl_list(p, kind, it + 1, 1)[0]), reps=3)
+    nbytes = algorithmic_bytes(kind, m.arrays)
+    peak, peak_src = peaks()
+    dom = max(prof, key=prof.get)
+    rl_kernel = max((k for k in nbytes if k in prof and prof[k] > 0), key=lambda k: prof[k])
+    achieved = nbytes[rl_kernel] / (prof[rl_kernel] * 1e-3) / 1e9
+    kernels = {k: {"ms": round(v, 5), "alg_MB": round(nbytes.get(k, 0) / 1e6, 2),
+                   "GBps": round(nbytes[k] / (v * 1e-3) / 1e9, 1) if k in nbytes and v > 0 else None}
+               for k, v in prof.items()}
+
+    clocks = clk.summary()
+    if rank != 0:
+        return None
+    ws_mb = nbytes_total = sum(nbytes.values()) / 1e6
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if p.precision == abi.PREC["fp64"] else "f32-face/f64-accumulate",
+        "data": "synthetic: seeded analytic-airfoil O-mesh, uniform freestream start",
+        "config": {"workload": w["desc"], "units": units, "edges_or_faces": int(m["nof"] if kind == "nc" else m["nfi"] + m["nbf"]),
+                   "global_batch": units, "seq_len": 1, "parallelism": f"replicas x{args.gpus}",
+                   "l2": f"inputs larger than L2: ~{ws_mb:.0f} MB of per-iteration arrays vs 129 MB L2, no flush",
+                   "setup_s": round(setup_s, 2)},
+        "e2e": e2e,
+        "gpu_launches": LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")] * args.steps,
+        "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else "fallback",
+                     "dominant_phase": dom},
+        "kernels": kernels,
+    }
+    if not args.no_cpu_baseline and args.gpus == 1:
+        out["cpu_baseline"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
+    return out
+
+
+def cpu_baseline(w, m, p, budget_s=15.0) -> dict:
+    """The oracle (serial C++ restatement of the reference) on this host, one core."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import OracleCC, OracleNC
+    O = OracleNC if w["kind"] == "nc" else OracleCC
+    o = O(m, p)
+    kind = w["kind"]
+    c = cfl_list(p, kind, 1, 64)
+    t0 = time.perf_counter()
+    o.iteration(c[0])
+    t1 = time.perf_counter() - t0
+    n = max(1, min(63, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    for k in range(n):
+        o.iteration(c[1 + k])
+    dt = time.perf_counter() - t0
+    units = units_of(w, m)
+    return {"value": round(units * n / dt / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "host_cores": os.cpu_count(),
+            "sample": f"{n} iterations of the full {units}-unit mesh after 1 untimed ({dt:.1f} s, serial oracle)"}
+
+
+def run_reference(args, w) -> dict:
+    """The reference's CPU path: the Fortran reference cannot be built here (no
+    Fortran compiler), so its serial C++ restatement (the oracle port) runs on
+    the host cores; it is serial like the reference, so one thread."""
+    m = build_mesh(w)
+    p = abi.make_params(**w["params"])
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from oracle import OracleCC, OracleNC
+    O = OracleNC if w["kind"] == "nc" else OracleCC
+    o = O(m, p)
+    kind = w["kind"]
+    units = units_of(w, m)
+    nw = min(args.warmup, 1)
+    c = cfl_list(p, kind, 1, nw + 200)
+    for k in range(nw):
+        o.iteration(c[k])
+    t0 = time.perf_counter()
+    o.iteration(c[nw])
+    t_one = time.perf_counter() - t0
+    n = max(1, min(args.steps, int(args.cpu_budget * 4 / max(t_one, 1e-6)))) - 1
+    t0 = time.perf_counter()
+    for k in range(n):
+        o.iteration(c[nw + 1 + k])
+    dt = time.perf_counter() - t0 + t_one
+    n += 1
+    v = units * n / dt / 1e6
+    sample = f"{n} full-mesh iterations ({dt:.1f} s) of the serial oracle port"
+    return {"metric": METRIC, "value": round(v, 4), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": n, "warmup": nw, "ms_per_step": round(dt * 1e3 / n, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["desc"], "units": units},
+            "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": 1, "kind": "port", "sample": sample,
+                             "host_cores": os.cpu_count()},
+            "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="nc", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--mesh", default=None, help="override the O-mesh size, e.g. 512x256 (profiling runs)")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    rank, world, local_rank = replicas.dist_env()
+    w = dict(WORKLOADS[args.workload])
+    if args.mesh:
+        w["ni"], w["nj"] = (int(x) for x in args.mesh.lower().split("x"))
+        w["desc"] += f" [mesh overridden to {args.mesh}]"
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args, w)))
+        return 0
+    dist = replicas.init("nccl")
+    out = run_ours(args, w, dist, rank, local_rank)
+    if out is not None:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

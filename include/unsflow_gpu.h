@@ -114,6 +114,19 @@ int uns_nc_residue(uns_nc_handle* h, double* fres_raw, double* fresi, int* iresi
 int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
                    double* fresi, int* done_iters);
 
+/* ============================================================ timing ====*/
+/* The cudaStream_t a handle queues its work on, so a caller can bracket
+ * calls with its own CUDA events (no reference counterpart: measurement). */
+void* uns_cc_stream(uns_cc_handle* h);
+void* uns_nc_stream(uns_nc_handle* h);
+/* Device time of each phase of one main-loop iteration, averaged over `reps`
+ * iterations run with a CUDA event between phases (no reference
+ * counterpart: measurement).  ms[k] for phase k < nphase; names[k] (may be
+ * NULL) receives a static phase name.  The state advances by reps
+ * iterations, exactly as uns_*_iterate would advance it. */
+int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
+int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,8 +41,11 @@ enum { UNS_GRAD_GG = 0, UNS_GRAD_GGFC = 1, UNS_GRAD_LSQR = 2 };
 enum { UNS_TIME_RK3 = 0, UNS_TIME_LUSGS = 1 };
 enum { UNS_CFL_TANH = 0, UNS_CFL_RAMP = 1 };
 /* NCFVM limiter: limiter_VKN (NCFVM/limiter.f90:15-98) or limiter_min_max
- * (Barth-Jespersen, NCFVM/limiter.f90:192-260). */
-enum { UNS_LIM_VKN = 0, UNS_LIM_BARTH = 1 };
+ * (Barth-Jespersen, NCFVM/limiter.f90:192-260).  limiter_min_max projects
+ * the fp2 gradient with +1/2 (limiter.f90:241), i.e. toward the wrong face
+ * side, and the solve then diverges; UNS_LIM_BARTH_CORRECTED uses -1/2 there,
+ * as limiter_VKN does (limiter.f90:71). */
+enum { UNS_LIM_VKN = 0, UNS_LIM_BARTH = 1, UNS_LIM_BARTH_CORRECTED = 2 };
 /* Arithmetic of the face reconstruction + convective flux.  FP64 everywhere,
  * or FP32 face arithmetic with FP64 accumulation / norm / dt / LU-SGS. */
 enum { UNS_PREC_FP64 = 0, UNS_PREC_MIXED = 1 };

@@ -119,10 +119,12 @@ void limiter_barth(NC& s) {
             for (int side = 0; side < 2; ++side) {
                 int p = side == 0 ? p1 : p2;
                 double D_L = 0.5 * (s.grad[(size_t)p * 8 + j * 2] * d0 + s.grad[(size_t)p * 8 + j * 2 + 1] * d1);
+                if (side == 1 && s.P.limiter_type == UNS_LIM_BARTH_CORRECTED) D_L = -D_L;
                 double ph;
                 if (D_L > 0.0) ph = std::min(1.0, s.dumax[p * 4 + j] / D_L);
                 else if (D_L < 0.0) ph = std::min(1.0, s.dumin[p * 4 + j] / D_L);
                 else ph = 1.0;
+                if (s.P.limiter_type == UNS_LIM_BARTH_CORRECTED) ph = std::max(0.0, ph);
                 s.phi[p * 4 + j] = std::min(s.phi[p * 4 + j], ph);
             }
     }
@@ -276,7 +278,7 @@ void fvresidual(NC& s, double cfl) {
     std::fill(s.res.begin(), s.res.end(), 0.0);
     std::fill(s.la.begin(), s.la.end(), 0.0);
     std::fill(s.fla.begin(), s.fla.end(), 0.0);
-    if (s.P.limiter_type == UNS_LIM_BARTH) limiter_barth(s); else limiter_vkn(s);
+    if (s.P.limiter_type == UNS_LIM_VKN) limiter_vkn(s); else limiter_barth(s);
     for (int ie = 0; ie < s.nof; ++ie) {
         int p1 = s.fp1[ie], p2 = s.fp2[ie];
         double d0 = s.px[p2] - s.px[p1], d1 = s.py[p2] - s.py[p1];

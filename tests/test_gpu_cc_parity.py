@@ -1,18 +1,23 @@
 """CCFVM hot path on the GPU vs the CPU oracle, routine by routine.
 
-Tolerance: 1e-12 of each field's max magnitude (FP64; the GPU fuses
-multiply-adds and sums faces in the same order as the reference, so the
-difference is a few ulps per operation).
+Criteria (see conftest.py): fields 1e-12 of their max magnitude; residuals
+1e-12 of the cell's flux scale; gradients 1e-12 with the rounding-noise floor;
+the limiter value phi 1e-10 (the Venkatakrishnan ratio is evaluated on
+D_L = grad.dx, a cancellation).  The GPU performs the reference's IEEE
+operations in the reference's order (no multiply-add contraction), so the
+remaining differences come from the math library's pow.
 """
 import numpy as np
 import pytest
 
+from conftest import grad_err, inv_h_cc, res_err
 from unsflow2d_gb300 import abi, mesh
 from unsflow2d_gb300.solver import CCSolver
 from oracle import OracleCC
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
+RTOL_PHI = 1e-10
 
 CASES = [
     dict(flux="roe", grad="gg"),
@@ -52,13 +57,13 @@ def test_cc_routine_parity(cc_mesh, case, assert_close):
         for s in (g, o):
             s.save_old()
             s.gradient()
-        assert_close("grad", g.get("grad"), o.get("grad"), RTOL)
-        assert_close("phi", g.get("phi"), o.get("phi"), RTOL)
+        assert grad_err(g.get("grad"), o.get("grad"), o.get("qp")[:o.noc], inv_h_cc(cc_mesh.arrays)) <= RTOL
+        assert_close("phi", g.get("phi"), o.get("phi"), RTOL_PHI)
         if p.time_mode == abi.TIME["rk3"]:
             for irk in (1, 2, 3):
                 for s in (g, o):
                     s.fvresidual()
-                assert_close(f"res it{it} st{irk}", g.get("res"), o.get("res"), RTOL)
+                assert res_err(g.get("res"), o.get("res"), o.get("la"), o.get("qc")[:o.noc]) <= RTOL
                 assert_close("ghost qc", g.get("qc")[g.noc:], o.get("qc")[o.noc:], RTOL)
                 for s in (g, o):
                     s.rk_stage(irk)
@@ -66,7 +71,7 @@ def test_cc_routine_parity(cc_mesh, case, assert_close):
         else:
             for s in (g, o):
                 s.lusgs()
-            assert_close("res", g.get("res"), o.get("res"), RTOL)
+            assert res_err(g.get("res"), o.get("res"), o.get("la"), o.get("qc")[:o.noc]) <= RTOL
             assert_close("qc", g.get("qc"), o.get("qc"), RTOL)
         assert g.check_positivity() == o.check_positivity() == -1
         fg, fo = g.residue(), o.residue()

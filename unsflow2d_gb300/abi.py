@@ -26,7 +26,7 @@ FLUX = {"roe": 0, "ausm": 1, "vanleer": 2, "rusanov": 3}
 GRAD = {"gg": 0, "ggfc": 1, "lsqr": 2}
 TIME = {"rk3": 0, "lusgs": 1}
 CFLT = {"tanh": 0, "ramp": 1}
-LIMITER = {"vkn": 0, "barth": 1}
+LIMITER = {"vkn": 0, "barth": 1, "barth_corrected": 2}
 PREC = {"fp64": 0, "mixed": 1}
 
 CC_FIELDS = {"qc": 0, "qp": 1, "qold": 2, "res": 3, "grad": 4, "phi": 5, "dt": 6, "la": 7,
@@ -204,6 +204,9 @@ def gpu_lib() -> C.CDLL:
             "uns_nc_lusgs": ([vp, C.c_double], i32),
             "uns_nc_residue": ([vp, dp, dp, C.POINTER(C.c_int)], i32),
             "uns_nc_iterate": ([vp, i32, dp, i32, dp, dp, C.POINTER(C.c_int)], i32),
+            "uns_cc_stream": ([vp], vp), "uns_nc_stream": ([vp], vp),
+            "uns_cc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
+            "uns_nc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)

@@ -26,7 +26,11 @@ OBJ = PKG / "_build"
 INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+# --fmad=false: no multiply-add contraction in device code, so the FP64 path
+# performs the same IEEE operations, in the same order, as the reference
+# expressions (and the CPU oracle, built with -ffp-contract=off).  Divisions
+# and square roots are correctly rounded either way.
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
              "-I", str(INCLUDE), "-I", str(CSRC / "host")]

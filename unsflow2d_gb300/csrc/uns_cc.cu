@@ -91,6 +91,11 @@ struct CCView {
     double2* fwallv;  // per boundary face: wall viscous (-flux3*A, -flux4*A)
     double4* lower;
     double4* upper;
+    double* diag;     // lusgs2 diagonal cv/dt + 0.5*omega*la (lusgs.F90:236)
+    double4* fold1;   // normal flux of qold[out] along +n (consumer: cell in)
+    double4* fold2;   // normal flux of qold[in] along -n (consumer: cell out)
+    double4* pw;      // sweep-published primitives of qold+dq: (rho, u, v, p)
+    double* pe;       // and e*rho, as normal_flux forms them (lusgs.F90:338-346)
     unsigned long long* minmax;  // encoded qmax[4], qmin[4]
     unsigned long long* dtmin;   // encoded dtglobal
     double* partial;
@@ -288,6 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         double cfl = cur_cfl(v, cfl_in);
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
+        v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
         atomicMin(v.dtmin, enc_ord(dt));
     }
     double gx[4], gy[4];
@@ -609,8 +615,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
         }
         v.res[i] = d4(r);
         if (irk > 0) {
-            const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
-            double a = A[irk - 1], b = B[irk - 1];
+            double a = rk3_a(irk), b = rk3_b(irk);
             double dtbyarea = v.dt[i] / v.cv[i];
             double o[4], c[4], q[4];
             d4get(v.qold[i], o);
@@ -658,8 +663,7 @@ __global__ void __launch_bounds__(kBlock) k_cirs(CCView v, const double4* src, d
 __global__ void __launch_bounds__(kBlock) k_rk_stage(CCView v, int irk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
-    const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
-    double a = A[irk - 1], b = B[irk - 1];
+    double a = rk3_a(irk), b = rk3_b(irk);
     double dtbyarea = v.dt[i] / v.cv[i];
     double o[4], c[4], r[4], q[4];
     d4get(v.qold[i], o);
@@ -776,59 +780,115 @@ __device__ __forceinline__ void normal_flux_d(const Gas& g, const double4& qo, c
     for (int k = 0; k < 4; ++k) out[k] = area * (f2[k] - f1[k]);
 }
 
-__global__ void __launch_bounds__(kBlock) k_lusgs(CCView v, const int* __restrict__ lf_off, const int* __restrict__ lf,
-                                                  int nlf, const int* __restrict__ lb_off, const int* __restrict__ lb,
-                                                  int nlb, GridSync* gs) {
-    const double omega = 1.5;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+// normal_flux pieces (lusgs.F90:328-359): the flux of a state along (nx, ny).
+__device__ __forceinline__ void nflux_prims(const double4& w, double et, double nx, double ny, double o[4]) {
+    double un = w.y * nx + w.z * ny;
+    o[0] = (et + w.w) * un;
+    o[1] = w.x * un;
+    o[2] = o[1] * w.y + w.w * nx;
+    o[3] = o[1] * w.z + w.w * ny;
+}
+
+// Flux of qold on both sides of every interior face (constant during the
+// sweeps, so evaluated once per face instead of once per sweep visit).
+__global__ void __launch_bounds__(kBlock) k_cc_fold(CCView v) {
     if (stopped(v)) return;
-    for (int pass = 0; pass < 2; ++pass) {
-        const int* off = pass == 0 ? lf_off : lb_off;
-        const int* cells = pass == 0 ? lf : lb;
-        int nl = pass == 0 ? nlf : nlb;
-        for (int L = 0; L < nl; ++L) {
-            for (int t = off[L] + tid; t < off[L + 1]; t += nth) {
-                int it = cells[t];
-                double cres[4] = {0.0, 0.0, 0.0, 0.0};
-                for (int k = v.rc2f_off[it]; k < v.rc2f_off[it + 1]; ++k) {
-                    int c = v.rc2f[k];
-                    double2 n = v.fn[c];
-                    double nx = n.x, ny = n.y;
-                    int2 nb = v.fnb[c];
-                    int out = nb.y;
-                    if (out == it) { out = nb.x; nx = -n.x; ny = -n.y; }
-                    bool take = (pass == 0) ? (out < it && out >= 0 && out < v.noc) : (out > it && out >= 0 && out < v.noc);
-                    if (!take) continue;
-                    double4 dq = pass == 0 ? v.lower[out] : v.upper[out];
-                    double df[4];
-                    normal_flux_d(v.g, v.qold[out], dq, nx, ny, v.farea[c], df);
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nfi) return;
+    int2 nb = v.fnb[f];
+    double2 n = v.fn[f];
+    double4 a = v.qold[nb.y], b = v.qold[nb.x];
+    Prim P = con2prim(v.g, a.x, a.y, a.z, a.w);
+    double o[4];
+    nflux_prims(make_double4(P.rho, P.u, P.v, P.p), P.e * P.rho, n.x, n.y, o);
+    v.fold1[f] = d4(o);
+    Prim Q = con2prim(v.g, b.x, b.y, b.z, b.w);
+    nflux_prims(make_double4(Q.rho, Q.u, Q.v, Q.p), Q.e * Q.rho, -n.x, -n.y, o);
+    v.fold2[f] = d4(o);
+}
+
+// lusgs2 sweeps (lusgs.F90:245-318) as a dataflow kernel: items are the
+// forward sweep's cells in dependency-level order, then the backward sweep's;
+// item s goes to warp s mod (warps in the grid).  Lanes take the cell's faces
+// in the reference c2f order and wait for the neighbour's completion flag
+// (bounded) when it precedes the cell in the sweep, then form
+// area*(F(qold+dq) - F(qold)) from the primitives the neighbour published;
+// lane 0 adds the terms in c2f order, updates the cell, publishes the
+// primitives of qold + its own dq and releases its flag.  Every wait targets
+// an earlier item and the cooperative launch keeps all warps resident.
+__global__ void __launch_bounds__(kBlock) k_lusgs(CCView v, const int* __restrict__ order, int nfwd, int nitems,
+                                                  int* flag) {
+    __shared__ double sterm[kBlock / 32][32][4];
+    const double omega = 1.5;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (kBlock / 32) + wib, nw = gridDim.x * (kBlock / 32);
+    if (stopped(v)) return;
+    for (int s = gw; s < nitems; s += nw) {
+        const int pass = s < nfwd ? 0 : 1;
+        const int it = order[s];
+        const int k0 = v.rc2f_off[it], deg = v.rc2f_off[it + 1] - k0;
+        bool take = false, ok = true;
+        double t4[4] = {0.0, 0.0, 0.0, 0.0};
+        if (lane < deg) {
+            int c = v.rc2f[k0 + lane];
+            double2 n = v.fn[c];
+            double nx = n.x, ny = n.y;
+            int2 nb = v.fnb[c];
+            int out = nb.y;
+            bool flip = false;
+            if (out == it) { out = nb.x; nx = -n.x; ny = -n.y; flip = true; }
+            take = pass == 0 ? (out < it && out >= 0 && out < v.noc) : (out > it && out >= 0 && out < v.noc);
+            if (take) {
+                ok = wait_flag(flag + out, pass + 1, v.err);
+                if (ok) {
+                    double4 dq = ldcg4(pass == 0 ? &v.lower[out] : &v.upper[out]);
+                    double f1[4], f2[4];
+                    d4get(flip ? v.fold2[c] : v.fold1[c], f1);
+                    nflux_prims(ldcg4(&v.pw[out]), __ldcg(&v.pe[out]), nx, ny, f2);
+                    double area = v.farea[c];
                     double lam = v.fla[c];
                     double d[4] = {dq.x, dq.y, dq.z, dq.w};
 #pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + (df[iv] - omega * lam * d[iv]);
-                }
-                double diag = v.cv[it] / v.dt[it] + 0.5 * omega * v.la[it];
-                double r[4];
-                if (pass == 0) {
-                    d4get(v.res[it], r);
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) r[iv] = (-r[iv] - 0.5 * cres[iv]) / diag;
-                    v.lower[it] = d4(r);
-                } else {
-                    double lo[4], o[4], q[4];
-                    d4get(v.lower[it], lo);
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) r[iv] = lo[iv] - 0.5 * cres[iv] / diag;
-                    v.upper[it] = d4(r);
-                    d4get(v.qold[it], o);
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) q[iv] = o[iv] + r[iv];
-                    v.qc[it] = d4(q);
+                    for (int iv = 0; iv < 4; ++iv) t4[iv] = area * (f2[iv] - f1[iv]) - omega * lam * d[iv];
                 }
             }
-            __threadfence();
-            if (!grid_barrier(gs, v.err)) return;
         }
+        if (pass == 1 && lane == 0) ok = ok && wait_flag(flag + it, 1, v.err);  // own lower
+        if (__ballot_sync(0xffffffffu, !ok)) return;
+        unsigned taken = __ballot_sync(0xffffffffu, take);
+#pragma unroll
+        for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
+        __syncwarp();
+        if (lane == 0) {
+            double cres[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int j = 0; j < deg; ++j)
+                if (taken & (1u << j))
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + sterm[wib][j][iv];
+            const double diag = v.diag[it];
+            double r[4], o[4], w[4];
+            d4get(v.qold[it], o);
+            if (pass == 0) {
+                d4get(v.res[it], r);
+#pragma unroll
+                for (int iv = 0; iv < 4; ++iv) r[iv] = (-r[iv] - 0.5 * cres[iv]) / diag;
+                stcg4(&v.lower[it], d4(r));
+            } else {
+                double lo[4];
+                d4get(ldcg4(&v.lower[it]), lo);
+#pragma unroll
+                for (int iv = 0; iv < 4; ++iv) r[iv] = lo[iv] - 0.5 * cres[iv] / diag;
+                stcg4(&v.upper[it], d4(r));
+            }
+#pragma unroll
+            for (int iv = 0; iv < 4; ++iv) w[iv] = o[iv] + r[iv];  // qold + dq (and the new qc)
+            if (pass == 1) v.qc[it] = d4(w);
+            Prim P = con2prim(v.g, w[0], w[1], w[2], w[3]);
+            stcg4(&v.pw[it], make_double4(P.rho, P.u, P.v, P.p));
+            __stcg(&v.pe[it], P.e * P.rho);
+            st_release(flag + it, pass + 1);
+        }
+        __syncwarp();
     }
 }
 
@@ -843,9 +903,8 @@ struct uns_cc_handle {
     std::vector<void*> allocs;
     int nparts = 0;
     // LU-SGS levels
-    int* lf_off = nullptr; int* lf = nullptr; int nlf = 0;
-    int* lb_off = nullptr; int* lb = nullptr; int nlb = 0;
-    GridSync* gs = nullptr;
+    int* order = nullptr;  // forward items (level order) then backward items
+    int* flag = nullptr;   // per-cell sweep progress: 0, 1 forward done, 2 backward done
     int coop_blocks = 0;
     double4 qinf;
     // graph fast path
@@ -988,9 +1047,10 @@ int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int par
 }
 
 int enqueue_lusgs(uns_cc_handle* h, CCView& v) {
+    if (v.nfi > 0) LAUNCH(k_cc_fold, v.nfi, v);
     UNS_CUDA(cudaMemsetAsync(v.lower, 0, sizeof(double4) * v.noc, h->stream));
     UNS_CUDA(cudaMemsetAsync(v.upper, 0, sizeof(double4) * v.noc, h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GridSync), h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int) * v.noc, h->stream));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h->coop_blocks);
     cfg.blockDim = dim3(kBlock);
@@ -1000,8 +1060,7 @@ int enqueue_lusgs(uns_cc_handle* h, CCView& v) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_lusgs, v, (const int*)h->lf_off, (const int*)h->lf, h->nlf,
-                                (const int*)h->lb_off, (const int*)h->lb, h->nlb, h->gs));
+    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_lusgs, v, (const int*)h->order, v.noc, 2 * v.noc, h->flag));
     return UNS_OK;
 }
 
@@ -1166,6 +1225,7 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     AL(pp, nop); AL(ppT, nop); AL(fq, nof); AL(fqT, nof); AL(fla, nof); AL(fmu, nof);
     AL(fF, nof); AL(fV, nof); AL(fgx, nof); AL(fgy, nof); AL(fgT, nof); AL(fasum, nof);
     AL(fwall, nbf); AL(fwallv, nbf); AL(lower, noc); AL(upper, noc);
+    AL(diag, noc); AL(fold1, nfi); AL(fold2, nfi); AL(pw, noc); AL(pe, noc);
     AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
     h->nparts = nblocks(noc);
     AL(partial, h->nparts);
@@ -1173,26 +1233,25 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     if ((rc = h->alloc(h->d_iter, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
-    if ((rc = h->alloc(h->gs, 1))) return fail(rc);
-    // LU-SGS level schedule on the reference cell order.
+    // LU-SGS dataflow order on the reference cell order.
     {
-        std::vector<int> off, cells;
+        int maxdeg = 0;
+        for (int i = 0; i < noc; ++i) maxdeg = std::max(maxdeg, m->c2f_off[i + 1] - m->c2f_off[i]);
+        if (maxdeg > 32) { set_last_error("uns_cc_create: a cell has more than 32 faces"); return fail(UNS_ERR_MESH); }
+        std::vector<int> off, fwd, bwd;
         std::vector<int> c2fo(m->c2f_off, m->c2f_off + noc + 1), c2fv(m->c2f, m->c2f + m->c2f_off[noc]);
-        build_levels(noc, c2fo, c2fv, m->fin, m->fout, true, off, cells);
-        h->nlf = (int)off.size() - 1;
-        if ((rc = h->upload(h->lf_off, off.data(), off.size()))) return fail(rc);
-        if ((rc = h->upload(h->lf, cells.data(), cells.size()))) return fail(rc);
-        build_levels(noc, c2fo, c2fv, m->fin, m->fout, false, off, cells);
-        h->nlb = (int)off.size() - 1;
-        if ((rc = h->upload(h->lb_off, off.data(), off.size()))) return fail(rc);
-        if ((rc = h->upload(h->lb, cells.data(), cells.size()))) return fail(rc);
+        build_levels(noc, c2fo, c2fv, m->fin, m->fout, true, off, fwd);
+        build_levels(noc, c2fo, c2fv, m->fin, m->fout, false, off, bwd);
+        fwd.insert(fwd.end(), bwd.begin(), bwd.end());
+        if ((rc = h->upload(h->order, fwd.data(), fwd.size()))) return fail(rc);
+        if ((rc = h->alloc(h->flag, noc))) return fail(rc);
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lusgs, kBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_cc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
-        h->coop_blocks = nsm * std::min(per, 2);
+        h->coop_blocks = nsm * std::min(per, 4);
     }
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) { set_last_error("uns_cc_create: upload failed"); return fail(UNS_ERR_CUDA); }
     rc = uns_cc_initialize(h);
@@ -1490,6 +1549,89 @@ int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_ite
     UNS_CUDA(cudaMemcpyAsync(&it, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     if (done_iters) *done_iters = it;
+    return check_dev_err(h);
+}
+
+void* uns_cc_stream(uns_cc_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
+    static const char* kNames[] = {"begin", "vertex_avg", "face_prim_spec", "face_ggfc", "cell_grad", "face_conv",
+                                   "viscous", "cell_res", "cirs", "lusgs_sweeps", "residue"};
+    const int NP = 11;
+    if (!h || reps < 1 || !ms) return UNS_ERR_ARG;
+    std::vector<double> acc(NP, 0.0);
+    cudaEvent_t e0, e1;
+    UNS_CUDA(cudaEventCreate(&e0));
+    UNS_CUDA(cudaEventCreate(&e1));
+    CCView v = h->v;
+    int rc = UNS_OK;
+    auto timed = [&](int phase, auto&& launch) -> int {
+        UNS_CUDA(cudaEventRecord(e0, h->stream));
+        int r = launch();
+        if (r) return r;
+        UNS_CUDA(cudaEventRecord(e1, h->stream));
+        UNS_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UNS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        acc[phase] += t;
+        return UNS_OK;
+    };
+    const bool rk3 = h->P.time_mode == UNS_TIME_RK3;
+    const double eps = v.irs ? epsirs_of(h, cfl) : 0.0;
+    const bool smooth = v.irs && eps > 0.0;
+    for (int r = 0; r < reps && !rc; ++r) {
+        rc = timed(0, [&]() -> int {
+            k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
+            UNS_CUDA(cudaGetLastError());
+            LAUNCH(k_begin, v.ntot, v, BEGIN_PRIM | BEGIN_OLD | BEGIN_POS | (v.ilimit ? BEGIN_MINMAX : 0));
+            return UNS_OK;
+        });
+        if (!rc) rc = timed(1, [&]() -> int { LAUNCH(k_vertex_avg, v.nop, v); return UNS_OK; });
+        if (!rc) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
+        if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
+        if (!rc) rc = timed(4, [&]() -> int { LAUNCH(k_cell_grad, v.noc, v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), cfl); return UNS_OK; });
+        for (int irk = 1; irk <= (rk3 ? 3 : 1) && !rc; ++irk) {
+            rc = timed(5, [&]() -> int {
+                if (h->P.precision == UNS_PREC_MIXED) LAUNCH(k_face_conv<float>, v.nof, v);
+                else LAUNCH(k_face_conv<double>, v.nof, v);
+                return UNS_OK;
+            });
+            if (!rc && v.laminar) rc = timed(6, [&]() -> int {
+                LAUNCH(k_cell_mul, v.noc, v);
+                if (v.grad_type != UNS_GRAD_GGFC) {
+                    CCView w = v;
+                    w.grad_type = UNS_GRAD_GGFC;
+                    int r2 = enqueue_gradient(h, w, 0, cfl, true);
+                    if (r2) return r2;
+                }
+                LAUNCH(k_face_visc, v.nof, v);
+                return UNS_OK;
+            });
+            int fuse = (rk3 && !smooth) ? irk : 0;
+            if (!rc) rc = timed(7, [&]() -> int { LAUNCH(k_cell_res, v.noc, v, fuse, smooth ? 0 : 1); return UNS_OK; });
+            if (!rc && smooth) rc = timed(8, [&]() -> int {
+                UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
+                LAUNCH(k_cirs, v.noc, v, (const double4*)v.res0, v.restmp, eps);
+                LAUNCH(k_cirs, v.noc, v, (const double4*)v.restmp, v.res, eps);
+                LAUNCH(k_res_partial, v.noc, v);
+                if (rk3) LAUNCH(k_rk_stage, v.noc, v, irk);
+                return UNS_OK;
+            });
+        }
+        if (!rc && !rk3) rc = timed(9, [&]() -> int { return enqueue_lusgs(h, v); });
+        if (!rc) rc = timed(10, [&]() -> int {
+            k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);
+            UNS_CUDA(cudaGetLastError());
+            return UNS_OK;
+        });
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    for (int k = 0; k < nphase; ++k) {
+        ms[k] = k < NP ? acc[k] / reps : 0.0;
+        if (names) names[k] = k < NP ? kNames[k] : "";
+    }
     return check_dev_err(h);
 }
 

@@ -65,6 +65,9 @@ struct NCView {
     double4* fold1;  // normalflux(qold(fp1)) on the edge (LU-SGS)
     double4* fold2;
     double4* dqc;
+    double* diag;    // LU-SGS diagonal cv/dt + 0.5*omega*la (lusgs.f90:36)
+    double4* pw;     // sweep-published primitives of qc: (rho, u, v, p)
+    double* pe;      // and e*rho, as normalflux forms them (lusgs.f90:144-147)
     double* partial;   // [2*nblk]: sum, max
     int* partial_i;    // argmax
     DevErr* err;
@@ -154,11 +157,14 @@ __global__ void __launch_bounds__(kBlock) k_nc_grad_lim(NCView v) {
                 double nr = alfa * alfa + 2.0 * D_L * alfa + TOL;
                 double dr = alfa * alfa + 2.0 * D_L * D_L + D_L * alfa + TOL;
                 phj = rmin(1.0, nr / dr);
-            } else {  // Barth-Jespersen incl. the +1/2 on the fp2 side
+            } else {  // Barth-Jespersen: reference form projects fp2 with +1/2
+                const bool corrected = v.limiter == UNS_LIM_BARTH_CORRECTED;
                 double D_L = 0.5 * s;
+                if (corrected && (e & P2_BIT)) D_L = -D_L;
                 if (D_L > 0.0) phj = rmin(1.0, dmx[j] / D_L);
                 else if (D_L < 0.0) phj = rmin(1.0, dmn[j] / D_L);
                 else phj = 1.0;
+                if (corrected) phj = rmax(0.0, phj);
             }
             ph[j] = rmin(ph[j], phj);
         }
@@ -282,9 +288,9 @@ __global__ void __launch_bounds__(kBlock) k_nc_node_res(NCView v, double cfl_in,
         double cfl = v.cfl_sched ? v.cfl_sched[*v.iter] : cfl_in;
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
+        v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
         if (irk > 0) {
-            const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
-            double a = A[irk - 1], b = B[irk - 1];
+            double a = rk3_a(irk), b = rk3_b(irk);
             double dtbyarea = dt / v.cv[i];
             double o[4], c[4], q[4];
             g4(v.qold[i], o);
@@ -329,8 +335,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_node_res(NCView v, double cfl_in,
 __global__ void __launch_bounds__(kBlock) k_nc_rk(NCView v, int irk) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nop) return;
-    const double A[3] = {0.0, 3.0 / 4.0, 1.0 / 3.0}, B[3] = {1.0, 1.0 / 4.0, 2.0 / 3.0};
-    double a = A[irk - 1], b = B[irk - 1];
+    double a = rk3_a(irk), b = rk3_b(irk);
     double dtbyarea = v.dt[i] / v.cv[i];
     double o[4], c[4], r[4], q[4];
     g4(v.qold[i], o); g4(v.qc[i], c); g4(v.res[i], r);
@@ -448,58 +453,98 @@ __global__ void __launch_bounds__(kBlock) k_nc_fold(NCView v) {
     v.fold2[f] = m4(o);
 }
 
-__global__ void __launch_bounds__(kBlock) k_nc_lusgs(NCView v, const int* __restrict__ lf_off, const int* __restrict__ lf,
-                                                     int nlf, const int* __restrict__ lb_off, const int* __restrict__ lb,
-                                                     int nlb, GridSync* gs) {
+// normalflux (lusgs.f90:137-155) from primitives a sweep has published.
+__device__ __forceinline__ void normalflux_prims(const double4& w, double et, double nx, double ny, double ds,
+                                                 double o[4]) {
+    double un = w.y * nx + w.z * ny;
+    o[0] = (et + w.w) * un;
+    o[1] = w.x * un;
+    o[2] = o[1] * w.y + w.w * nx;
+    o[3] = o[1] * w.z + w.w * ny;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = o[k] * ds;
+}
+
+// lusgs sweeps (lusgs.f90:48-124) as a dataflow kernel.  Items are the
+// forward sweep's nodes sorted by dependency level, then the backward sweep's;
+// item s goes to warp s mod (warps in the grid).  A warp's lanes take the
+// node's edges (reference v2f order), wait for the neighbour's completion flag
+// when that neighbour precedes the node in the sweep, and form the edge term
+// from the primitives the neighbour published; lane 0 adds the terms in edge
+// order -- the reference's summation order -- updates the node, publishes its
+// primitives (the con2prim a later normalflux of this node would do) and
+// releases its flag.  Every wait targets an earlier item, and the cooperative
+// launch keeps all warps resident, so the sweep always completes; each wait is
+// also bounded (wait_flag).
+__global__ void __launch_bounds__(kBlock) k_nc_lusgs(NCView v, const int* __restrict__ order, int nfwd, int nitems,
+                                                     int* flag) {
+    __shared__ double sterm[kBlock / 32][32][4];
     const double omega = 1.5;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (kBlock / 32) + wib, nw = gridDim.x * (kBlock / 32);
     if (stopped(v)) return;
-    for (int pass = 0; pass < 2; ++pass) {
-        const int* off = pass == 0 ? lf_off : lb_off;
-        const int* nodes = pass == 0 ? lf : lb;
-        int nl = pass == 0 ? nlf : nlb;
-        for (int L = 0; L < nl; ++L) {
-            for (int t = off[L] + tid; t < off[L + 1]; t += nth) {
-                int it = nodes[t];
-                double cres[4] = {0.0, 0.0, 0.0, 0.0};
-                for (int k = v.rv2f_off[it]; k < v.rv2f_off[it + 1]; ++k) {
-                    int c = v.rv2f[k];
-                    int2 p = v.fpt[c];
-                    double sign = 1.0;
-                    int p2 = p.y;
-                    bool nb_is_p1 = false;
-                    if (p2 == it) { p2 = p.x; sign = -1.0; nb_is_p1 = true; }
-                    bool take = pass == 0 ? (p2 < it && p2 >= 0) : (p2 > it && p2 >= 0);
-                    if (!take) continue;
+    for (int s = gw; s < nitems; s += nw) {
+        const int pass = s < nfwd ? 0 : 1;
+        const int it = order[s];
+        const int k0 = v.rv2f_off[it], deg = v.rv2f_off[it + 1] - k0;
+        bool take = false, ok = true;
+        double t4[4] = {0.0, 0.0, 0.0, 0.0};
+        if (lane < deg) {
+            int c = v.rv2f[k0 + lane];
+            int2 p = v.fpt[c];
+            int nb = p.y;
+            double sign = 1.0;
+            bool nb_is_p1 = false;
+            if (nb == it) { nb = p.x; sign = -1.0; nb_is_p1 = true; }
+            take = pass == 0 ? (nb < it && nb >= 0) : (nb > it && nb >= 0);
+            if (take) {
+                ok = wait_flag(flag + nb, pass + 1, v.err);
+                if (ok) {
                     double2 n = v.fn[c];
                     double f1[4], f2[4], dq[4];
                     g4(nb_is_p1 ? v.fold1[c] : v.fold2[c], f1);
-                    normalflux_nc(v.g, v.qc[p2], n.x, n.y, v.farea[c], f2);
-                    g4(v.dqc[p2], dq);
+                    normalflux_prims(ldcg4(&v.pw[nb]), __ldcg(&v.pe[nb]), n.x, n.y, v.farea[c], f2);
+                    g4(ldcg4(&v.dqc[nb]), dq);
                     double ol = omega * v.fla[c];
 #pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + 0.5 * (sign * (f2[iv] - f1[iv]) - ol * dq[iv]);
+                    for (int iv = 0; iv < 4; ++iv) t4[iv] = 0.5 * (sign * (f2[iv] - f1[iv]) - ol * dq[iv]);
                 }
-                double D = v.cv[it] / v.dt[it] + 0.5 * omega * v.la[it];
-                double d[4], o[4], r[4], q[4];
-                g4(v.qold[it], o);
-                if (pass == 0) {
-                    g4(v.res[it], r);
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) d[iv] = (-r[iv] - cres[iv]) / D;
-                } else {
-                    g4(v.dqc[it], d);
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) d[iv] = d[iv] - cres[iv] / D;
-                }
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) q[iv] = o[iv] + d[iv];
-                v.dqc[it] = m4(d);
-                v.qc[it] = m4(q);
             }
-            __threadfence();
-            if (!grid_barrier(gs, v.err)) return;
         }
+        if (pass == 1 && lane == 0) ok = ok && wait_flag(flag + it, 1, v.err);  // own forward value
+        if (__ballot_sync(0xffffffffu, !ok)) return;
+        unsigned taken = __ballot_sync(0xffffffffu, take);
+#pragma unroll
+        for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
+        __syncwarp();
+        if (lane == 0) {
+            double cres[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int j = 0; j < deg; ++j)
+                if (taken & (1u << j))
+#pragma unroll
+                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + sterm[wib][j][iv];
+            const double D = v.diag[it];
+            double d[4], o[4], r[4], q[4];
+            g4(v.qold[it], o);
+            if (pass == 0) {
+                g4(v.res[it], r);
+#pragma unroll
+                for (int iv = 0; iv < 4; ++iv) d[iv] = (-r[iv] - cres[iv]) / D;
+            } else {
+                g4(ldcg4(&v.dqc[it]), d);
+#pragma unroll
+                for (int iv = 0; iv < 4; ++iv) d[iv] = d[iv] - cres[iv] / D;
+            }
+#pragma unroll
+            for (int iv = 0; iv < 4; ++iv) q[iv] = o[iv] + d[iv];
+            Prim P = con2prim(v.g, q[0], q[1], q[2], q[3]);
+            stcg4(&v.dqc[it], m4(d));
+            stcg4(&v.pw[it], make_double4(P.rho, P.u, P.v, P.p));
+            __stcg(&v.pe[it], P.e * P.rho);
+            v.qc[it] = m4(q);
+            st_release(flag + it, pass + 1);
+        }
+        __syncwarp();
     }
 }
 
@@ -542,9 +587,8 @@ struct uns_nc_handle {
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     int nparts = 0;
-    int* lf_off = nullptr; int* lf = nullptr; int nlf = 0;
-    int* lb_off = nullptr; int* lb = nullptr; int nlb = 0;
-    GridSync* gs = nullptr;
+    int* order = nullptr;   // forward items (level order) then backward items
+    int* flag = nullptr;    // per-node sweep progress: 0, 1 forward done, 2 backward done
     int coop_blocks = 0;
     double4 qinf;
     cudaGraphExec_t graph = nullptr;
@@ -609,10 +653,9 @@ int enqueue_fvres_nc(uns_nc_handle* h, NCView& v, double cfl, int irk, int parti
     return UNS_OK;
 }
 
-int enqueue_lusgs_nc(uns_nc_handle* h, NCView& v) {
-    NLAUNCH(k_nc_fold, v.nof, v);
+int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
     UNS_CUDA(cudaMemsetAsync(v.dqc, 0, sizeof(double4) * v.nop, h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->gs, 0, sizeof(GridSync), h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int) * v.nop, h->stream));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h->coop_blocks);
     cfg.blockDim = dim3(kBlock);
@@ -622,9 +665,13 @@ int enqueue_lusgs_nc(uns_nc_handle* h, NCView& v) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->lf_off, (const int*)h->lf, h->nlf,
-                                (const int*)h->lb_off, (const int*)h->lb, h->nlb, h->gs));
+    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->order, v.nop, 2 * v.nop, h->flag));
     return UNS_OK;
+}
+
+int enqueue_lusgs_nc(uns_nc_handle* h, NCView& v) {
+    NLAUNCH(k_nc_fold, v.nof, v);
+    return launch_sweeps_nc(h, v);
 }
 
 int enqueue_iteration_nc(uns_nc_handle* h, NCView& v) {
@@ -651,7 +698,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     *out = nullptr;
     if (m->nop <= 0 || m->nof <= 0 || !(p->m_inf > 0.0) || p->time_mode < 0 || p->time_mode > 1 ||
         (p->flux_type != UNS_FLUX_VANLEER && p->flux_type != UNS_FLUX_AUSM) ||
-        (p->limiter_type != UNS_LIM_VKN && p->limiter_type != UNS_LIM_BARTH)) {
+        (p->limiter_type < UNS_LIM_VKN || p->limiter_type > UNS_LIM_BARTH_CORRECTED)) {
         set_last_error("uns_nc_create: bad sizes or parameters");
         return UNS_ERR_ARG;
     }
@@ -735,7 +782,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
     ALN(qc, nop); ALN(qp, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
-    ALN(fold1, nof); ALN(fold2, nof); ALN(dqc, nop); ALN(err, 1);
+    ALN(fold1, nof); ALN(fold2, nof); ALN(dqc, nop); ALN(diag, nop); ALN(pw, nop); ALN(pe, nop); ALN(err, 1);
     h->nparts = nblocks(nop);
     ALN(partial, 2 * h->nparts);
     ALN(partial_i, h->nparts);
@@ -743,24 +790,24 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     if ((rc = h->alloc(h->d_iter, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
-    if ((rc = h->alloc(h->gs, 1))) return fail(rc);
     {
-        std::vector<int> off, nodes;
-        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, true, off, nodes);
-        h->nlf = (int)off.size() - 1;
-        if ((rc = h->upload(h->lf_off, off.data(), off.size()))) return fail(rc);
-        if ((rc = h->upload(h->lf, nodes.data(), nodes.size()))) return fail(rc);
-        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, false, off, nodes);
-        h->nlb = (int)off.size() - 1;
-        if ((rc = h->upload(h->lb_off, off.data(), off.size()))) return fail(rc);
-        if ((rc = h->upload(h->lb, nodes.data(), nodes.size()))) return fail(rc);
+        // Dataflow order of the two sweeps; a warp per node handles up to 32 edges.
+        int maxdeg = 0;
+        for (int i = 0; i < nop; ++i) maxdeg = std::max(maxdeg, m->v2f_off[i + 1] - m->v2f_off[i]);
+        if (maxdeg > 32) { set_last_error("uns_nc_create: a node has more than 32 edges"); return fail(UNS_ERR_MESH); }
+        std::vector<int> off, fwd, bwd;
+        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, true, off, fwd);
+        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, false, off, bwd);
+        fwd.insert(fwd.end(), bwd.begin(), bwd.end());
+        if ((rc = h->upload(h->order, fwd.data(), fwd.size()))) return fail(rc);
+        if ((rc = h->alloc(h->flag, nop))) return fail(rc);
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs, kBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_nc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
-        h->coop_blocks = nsm * std::min(per, 2);
+        h->coop_blocks = nsm * std::min(per, 4);
     }
 #undef UPN
 #undef ALN
@@ -927,6 +974,61 @@ int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_ite
     UNS_CUDA(cudaMemcpyAsync(&it, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     if (done_iters) *done_iters = it;
+    return check_err_nc(h);
+}
+
+void* uns_nc_stream(uns_nc_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
+    static const char* kNames[] = {"save_old", "grad_lim", "edge", "node_res", "fold", "lusgs_sweeps", "residue"};
+    const int NP = 7;
+    if (!h || reps < 1 || !ms) return UNS_ERR_ARG;
+    std::vector<double> acc(NP, 0.0);
+    cudaEvent_t e0, e1;
+    UNS_CUDA(cudaEventCreate(&e0));
+    UNS_CUDA(cudaEventCreate(&e1));
+    NCView v = h->v;
+    int rc = UNS_OK;
+    auto timed = [&](int phase, auto&& launch) -> int {
+        UNS_CUDA(cudaEventRecord(e0, h->stream));
+        int r = launch();
+        if (r) return r;
+        UNS_CUDA(cudaEventRecord(e1, h->stream));
+        UNS_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        UNS_CUDA(cudaEventElapsedTime(&t, e0, e1));
+        acc[phase] += t;
+        return UNS_OK;
+    };
+    const bool rk3 = h->P.time_mode == UNS_TIME_RK3;
+    for (int r = 0; r < reps && !rc; ++r) {
+        rc = timed(0, [&]() -> int { NLAUNCH(k_nc_save_old, v.nop, v); return UNS_OK; });
+        for (int irk = 1; irk <= (rk3 ? 3 : 1) && !rc; ++irk) {
+            if (!rc) rc = timed(1, [&]() -> int { NLAUNCH(k_nc_grad_lim, v.nop, v); return UNS_OK; });
+            if (!rc) rc = timed(2, [&]() -> int {
+                if (h->P.precision == UNS_PREC_MIXED) NLAUNCH(k_nc_edge<float>, v.nof, v);
+                else NLAUNCH(k_nc_edge<double>, v.nof, v);
+                return UNS_OK;
+            });
+            if (!rc) rc = timed(3, [&]() -> int { NLAUNCH(k_nc_node_res, v.nop, v, cfl, rk3 ? irk : 0, rk3 ? (irk == 3) : 1); return UNS_OK; });
+        }
+        if (!rk3) {
+            if (!rc) rc = timed(4, [&]() -> int { NLAUNCH(k_nc_fold, v.nof, v); return UNS_OK; });
+            if (!rc) rc = timed(5, [&]() -> int { return launch_sweeps_nc(h, v); });
+        }
+        if (!rc) rc = timed(6, [&]() -> int {
+            k_nc_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);
+            UNS_CUDA(cudaGetLastError());
+            return UNS_OK;
+        });
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    for (int k = 0; k < nphase; ++k) {
+        ms[k] = k < NP ? acc[k] / reps : 0.0;
+        if (names) names[k] = k < NP ? kNames[k] : "";
+    }
     return check_err_nc(h);
 }
 

@@ -57,6 +57,18 @@ class _Solver:
         self._call("get_state", _dp(out))
         return out
 
+    def stream(self) -> int:
+        """cudaStream_t of this handle (for CUDA events recorded by the caller)."""
+        return int(getattr(self._lib, f"uns_{self.kind}_stream")(self._h) or 0)
+
+    def profile(self, cfl: float, reps: int = 3) -> dict:
+        """Average device time [ms] of each phase of one iteration."""
+        n = 16
+        ms = np.zeros(n)
+        names = (C.c_char_p * n)()
+        self._call("profile", C.c_double(cfl), reps, _dp(ms), names, n)
+        return {names[k].decode(): float(ms[k]) for k in range(n) if names[k] and names[k].decode()}
+
     def get(self, field: str) -> np.ndarray:
         shape = self._field_shape(field)
         out = np.zeros(shape)
