@@ -127,6 +127,25 @@ void* uns_nc_stream(uns_nc_handle* h);
 int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
 
+/* ===================================================== no-allocation ====*/
+/* Largest ncells uns_residue_rms_noalloc accepts: its scratch is a static
+ * device array of UNS_RMS_NOALLOC_MAX_CELLS / 256 partial sums (128 KiB). */
+#define UNS_RMS_NOALLOC_MAX_CELLS 4194304
+
+/* The residual norm of uns_cc_residue, sqrt(sum res^2 / ncells / 4), over a
+ * residual array the caller owns on the current device (ncells rows of 4
+ * doubles, 32-byte aligned), queued on `stream` (NULL: the default stream)
+ * and returned in *fres_raw after the stream synchronises.  No reference
+ * counterpart: it exists for callers that must not allocate.  The call
+ * allocates and frees nothing; its scratch is a fixed static device array,
+ * whose every slot a call writes before reading it, so nothing needs to start
+ * at zero.  ncells > UNS_RMS_NOALLOC_MAX_CELLS, NULL pointers or a misaligned
+ * array give UNS_ERR_ARG before any device work.  The first call on each
+ * device looks up the scratch address; make it before any stream capture.
+ * Calls that overlap on one device (other threads or streams) share the
+ * scratch and race: serialise them. */
+int uns_residue_rms_noalloc(const double* res, int ncells, double* fres_raw, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -207,6 +207,7 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_stream": ([vp], vp), "uns_nc_stream": ([vp], vp),
             "uns_cc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
             "uns_nc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
+            "uns_residue_rms_noalloc": ([vp, i32, dp, vp], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)
