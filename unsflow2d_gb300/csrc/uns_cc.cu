@@ -30,6 +30,7 @@
 
 #include "uns_common.cuh"
 #include "uns_phys.cuh"
+#include "uns_sched.hpp"
 #include "unsflow_gpu.h"
 
 using namespace uns;
@@ -89,13 +90,19 @@ struct CCView {
     double* fasum; // a1 + a2
     double2* fwall;   // per boundary face: wall convective (flux3, flux4)
     double2* fwallv;  // per boundary face: wall viscous (-flux3*A, -flux4*A)
-    double4* lower;
-    double4* upper;
     double* diag;     // lusgs2 diagonal cv/dt + 0.5*omega*la (lusgs.F90:236)
-    double4* fold1;   // normal flux of qold[out] along +n (consumer: cell in)
-    double4* fold2;   // normal flux of qold[in] along -n (consumer: cell out)
-    double4* pw;      // sweep-published primitives of qold+dq: (rho, u, v, p)
-    double* pe;       // and e*rho, as normal_flux forms them (lusgs.F90:338-346)
+    // LU-SGS sweep schedule (host-built): per position of the warp lists
+    // (it, pass, first record, records); per record, in the reference c2f
+    // order of the taken faces: face, neighbour, 1 if the face normal points
+    // into the cell (the sweep then uses -n).
+    const int4* sched;
+    const int* rec_face;
+    const int* rec_nb;
+    const int* rec_flip;
+    int nrec;
+    double4* rec;     // per record, per LU-SGS call: 3 x double4, see k_cc_sweep_prep
+    double4* rec_a;   // sweep records [pass * noc + cell]: (u, v, p, e*rho) of qold + dq
+    double4* rec_b;   //   and dq (lower / upper); rho is rebuilt as qold.rho + dq.rho
     unsigned long long* minmax;  // encoded qmax[4], qmin[4]
     unsigned long long* dtmin;   // encoded dtglobal
     double* partial;
@@ -789,106 +796,155 @@ __device__ __forceinline__ void nflux_prims(const double4& w, double et, double 
     o[3] = o[1] * w.z + w.w * ny;
 }
 
-// Flux of qold on both sides of every interior face (constant during the
-// sweeps, so evaluated once per face instead of once per sweep visit).
-__global__ void __launch_bounds__(kBlock) k_cc_fold(CCView v) {
+constexpr int kSweepBlock = 128;
+constexpr double kOmega = 1.5;  // lusgs.F90:229
+
+// Per LU-SGS call: everything a sweep item needs from a face that does not
+// change during the sweeps, contiguous in schedule order:
+//   rec[3r]   normal_flux of qold(nb) along the cell's outward normal
+//             (lusgs.F90:328-346, the flux1 part)
+//   rec[3r+1] (nx, ny, area, omega * la) with the cell's outward normal
+//   rec[3r+2] (qold(nb).rho, 0, nb as integer bits, 0)
+__global__ void __launch_bounds__(kBlock) k_cc_sweep_prep(CCView v) {
     if (stopped(v)) return;
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= v.nfi) return;
-    int2 nb = v.fnb[f];
-    double2 n = v.fn[f];
-    double4 a = v.qold[nb.y], b = v.qold[nb.x];
-    Prim P = con2prim(v.g, a.x, a.y, a.z, a.w);
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= v.nrec) return;
+    const int c = v.rec_face[r], nb = v.rec_nb[r];
+    const double2 n = v.fn[c];
+    const double nx = v.rec_flip[r] ? -n.x : n.x, ny = v.rec_flip[r] ? -n.y : n.y;
+    const double4 q = v.qold[nb];
+    Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
     double o[4];
-    nflux_prims(make_double4(P.rho, P.u, P.v, P.p), P.e * P.rho, n.x, n.y, o);
-    v.fold1[f] = d4(o);
-    Prim Q = con2prim(v.g, b.x, b.y, b.z, b.w);
-    nflux_prims(make_double4(Q.rho, Q.u, Q.v, Q.p), Q.e * Q.rho, -n.x, -n.y, o);
-    v.fold2[f] = d4(o);
+    nflux_prims(make_double4(P.rho, P.u, P.v, P.p), P.e * P.rho, nx, ny, o);
+    v.rec[3 * (size_t)r] = d4(o);
+    v.rec[3 * (size_t)r + 1] = make_double4(nx, ny, v.farea[c], kOmega * v.fla[c]);
+    v.rec[3 * (size_t)r + 2] = make_double4(q.y, 0.0, __longlong_as_double((long long)nb), 0.0);
 }
 
-// lusgs2 sweeps (lusgs.F90:245-318) as a dataflow kernel: items are the
-// forward sweep's cells in dependency-level order, then the backward sweep's;
-// item s goes to warp s mod (warps in the grid).  Lanes take the cell's faces
-// in the reference c2f order and wait for the neighbour's completion flag
-// (bounded) when it precedes the cell in the sweep, then form
-// area*(F(qold+dq) - F(qold)) from the primitives the neighbour published;
-// lane 0 adds the terms in c2f order, updates the cell, publishes the
-// primitives of qold + its own dq and releases its flag.  Every wait targets
-// an earlier item and the cooperative launch keeps all warps resident.
-__global__ void __launch_bounds__(kBlock) k_lusgs(CCView v, const int* __restrict__ order, int nfwd, int nitems,
-                                                  int* flag) {
-    __shared__ double sterm[kBlock / 32][32][4];
-    const double omega = 1.5;
+__device__ __forceinline__ double pick4(int k, double a, double b, double c, double d) {
+    return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d));
+}
+
+// What a lane loads ahead for one sweep item: its record (lanes < records)
+// and, in lanes 0..3, variable `lane` of the cell's own data.
+struct SweepIn {
+    double f1[4], nx, ny, area, ol, rho_old;
+    int nb;
+    double D, o, r;
+};
+
+__device__ __forceinline__ void sweep_load(const CCView& v, const int4& S, int lane, SweepIn& x) {
+    if (lane < S.w) {
+        const double4* p = v.rec + 3 * (size_t)(S.z + lane);
+        double4 a = p[0], b = p[1], c = p[2];
+        x.f1[0] = a.x; x.f1[1] = a.y; x.f1[2] = a.z; x.f1[3] = a.w;
+        x.nx = b.x; x.ny = b.y; x.area = b.z; x.ol = b.w;
+        x.rho_old = c.x; x.nb = (int)__double_as_longlong(c.z);
+    }
+    if (lane < 4) {
+        x.D = v.diag[S.x];
+        x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
+        if (S.y == 0) x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
+    }
+}
+
+// lusgs2 sweeps (lusgs.F90:245-318) as one cooperative launch.  Each warp runs
+// its own list of items (cell, pass) from the host-side list schedule, in
+// order, loading the next item's inputs while it works on the current one.
+// Per item: lane j takes the j-th face (reference c2f order) whose neighbour
+// precedes the cell in this pass; it takes the neighbour's values from
+// registers when the warp itself computed that neighbour last, else polls its
+// record, and forms area*(F(qold+dq) - F(qold)) - omega*lam*dq; lanes 0..3 add
+// the terms of one variable each in c2f order and apply the diagonal; the new
+// values are shuffled to all lanes, which form the primitives of qold + dq
+// (kept for the next item) while lanes 0 and 1 publish the record.
+__global__ void __launch_bounds__(kSweepBlock) k_lusgs(CCView v, const int* __restrict__ woff) {
+    __shared__ double sterm[kSweepBlock / 32][32][4];
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * (kBlock / 32) + wib, nw = gridDim.x * (kBlock / 32);
+    const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
     if (stopped(v)) return;
-    for (int s = gw; s < nitems; s += nw) {
-        const int pass = s < nfwd ? 0 : 1;
-        const int it = order[s];
-        const int k0 = v.rc2f_off[it], deg = v.rc2f_off[it + 1] - k0;
-        bool take = false, ok = true;
+    const int n = v.noc;
+    const int kbeg = woff[gw], kend = woff[gw + 1];
+    if (kbeg >= kend) return;
+    const int4 none = make_int4(0, 0, 0, 0);
+    int4 S = v.sched[kbeg];
+    int4 Sn = kbeg + 1 < kend ? v.sched[kbeg + 1] : none;
+    SweepIn X = {}, Xn = {};
+    sweep_load(v, S, lane, X);
+    int last = -1;  // code of the warp's previous item; its values below, in every lane
+    double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    for (int k = kbeg; k < kend; ++k) {
+        // ---- next item's inputs (independent of the sweep), in flight meanwhile
+        const int4 Snn = k + 2 < kend ? v.sched[k + 2] : none;
+        if (k + 1 < kend) sweep_load(v, Sn, lane, Xn);
+        const int it = S.x, pass = S.y, ntake = S.w;
+        // ---- values of earlier items
+        bool ok = true;
         double t4[4] = {0.0, 0.0, 0.0, 0.0};
-        if (lane < deg) {
-            int c = v.rc2f[k0 + lane];
-            double2 n = v.fn[c];
-            double nx = n.x, ny = n.y;
-            int2 nb = v.fnb[c];
-            int out = nb.y;
-            bool flip = false;
-            if (out == it) { out = nb.x; nx = -n.x; ny = -n.y; flip = true; }
-            take = pass == 0 ? (out < it && out >= 0 && out < v.noc) : (out > it && out >= 0 && out < v.noc);
-            if (take) {
-                ok = wait_flag(flag + out, pass + 1, v.err);
-                if (ok) {
-                    double4 dq = ldcg4(pass == 0 ? &v.lower[out] : &v.upper[out]);
-                    double f1[4], f2[4];
-                    d4get(flip ? v.fold2[c] : v.fold1[c], f1);
-                    nflux_prims(ldcg4(&v.pw[out]), __ldcg(&v.pe[out]), nx, ny, f2);
-                    double area = v.farea[c];
-                    double lam = v.fla[c];
-                    double d[4] = {dq.x, dq.y, dq.z, dq.w};
+        if (lane < ntake) {
+            double w[8], rho;
+            if (((X.nb << 1) | pass) == last) {
+                w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
+                rho = Lrho;
+            } else {
+                const size_t slot = (size_t)pass * n + X.nb;
+                ok = poll_record<2>(v.rec_a + slot, w, v.err) && poll_record<2>(v.rec_b + slot, w + 4, v.err);
+                rho = X.rho_old + w[5];
+            }
+            if (ok) {
+                double f2[4];
+                nflux_prims(make_double4(rho, w[0], w[1], w[2]), w[3], X.nx, X.ny, f2);
 #pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) t4[iv] = area * (f2[iv] - f1[iv]) - omega * lam * d[iv];
-                }
+                for (int iv = 0; iv < 4; ++iv) t4[iv] = X.area * (f2[iv] - X.f1[iv]) - X.ol * w[4 + iv];
             }
         }
-        if (pass == 1 && lane == 0) ok = ok && wait_flag(flag + it, 1, v.err);  // own lower
-        if (__ballot_sync(0xffffffffu, !ok)) return;
-        unsigned taken = __ballot_sync(0xffffffffu, take);
+        double r = X.r;
+        if (pass == 1 && lane < 4) {  // own lower
+            if ((it << 1) == last) {
+                r = pick4(lane, L0, L1, L2, L3);
+            } else {
+                double dq[4];
+                ok = ok && poll_record<2>(v.rec_b + it, dq, v.err);
+                r = pick4(lane, dq[0], dq[1], dq[2], dq[3]);
+            }
+        }
+        if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
 #pragma unroll
         for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
         __syncwarp();
-        if (lane == 0) {
-            double cres[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int j = 0; j < deg; ++j)
-                if (taken & (1u << j))
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + sterm[wib][j][iv];
-            const double diag = v.diag[it];
-            double r[4], o[4], w[4];
-            d4get(v.qold[it], o);
-            if (pass == 0) {
-                d4get(v.res[it], r);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) r[iv] = (-r[iv] - 0.5 * cres[iv]) / diag;
-                stcg4(&v.lower[it], d4(r));
-            } else {
-                double lo[4];
-                d4get(ldcg4(&v.lower[it]), lo);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) r[iv] = lo[iv] - 0.5 * cres[iv] / diag;
-                stcg4(&v.upper[it], d4(r));
-            }
-#pragma unroll
-            for (int iv = 0; iv < 4; ++iv) w[iv] = o[iv] + r[iv];  // qold + dq (and the new qc)
-            if (pass == 1) v.qc[it] = d4(w);
-            Prim P = con2prim(v.g, w[0], w[1], w[2], w[3]);
-            stcg4(&v.pw[it], make_double4(P.rho, P.u, P.v, P.p));
-            __stcg(&v.pe[it], P.e * P.rho);
-            st_release(flag + it, pass + 1);
+        double d = 0.0, q = 0.0;
+        if (lane < 4) {
+            double cres = 0.0;
+            for (int j = 0; j < ntake; ++j) cres = cres + sterm[wib][j][lane];
+            d = pass == 0 ? (-r - 0.5 * cres) / X.D : r - 0.5 * cres / X.D;
+            q = X.o + d;  // qold + dq (and, after the backward sweep, the new qc)
         }
         __syncwarp();
+        const double q0 = __shfl_sync(full, q, 0), q1 = __shfl_sync(full, q, 1), q2 = __shfl_sync(full, q, 2),
+                     q3 = __shfl_sync(full, q, 3);
+        L0 = __shfl_sync(full, d, 0);
+        L1 = __shfl_sync(full, d, 1);
+        L2 = __shfl_sync(full, d, 2);
+        L3 = __shfl_sync(full, d, 3);
+        Prim P = con2prim(v.g, q0, q1, q2, q3);
+        Lrho = P.rho; Lu = P.u; Lv = P.v; Lp = P.p; Le = P.e * P.rho;
+        last = (it << 1) | pass;
+        const size_t slot = (size_t)pass * n + it;
+        if (lane == 0) {
+            double2* a = reinterpret_cast<double2*>(v.rec_a + slot);
+            st_relaxed2(a, Lu, Lv);
+            st_relaxed2(a + 1, Lp, Le);
+        } else if (lane == 1) {
+            double2* b = reinterpret_cast<double2*>(v.rec_b + slot);
+            st_relaxed2(b, L0, L1);
+            st_relaxed2(b + 1, L2, L3);
+        } else if (lane == 2 && pass == 1) {
+            v.qc[it] = make_double4(q0, q1, q2, q3);
+        }
+        S = Sn;
+        Sn = Snn;
+        X = Xn;
     }
 }
 
@@ -903,8 +959,7 @@ struct uns_cc_handle {
     std::vector<void*> allocs;
     int nparts = 0;
     // LU-SGS levels
-    int* order = nullptr;  // forward items (level order) then backward items
-    int* flag = nullptr;   // per-cell sweep progress: 0, 1 forward done, 2 backward done
+    int* woff = nullptr;   // LU-SGS warp schedule: per-warp ranges of v.sched
     int coop_blocks = 0;
     double4 qinf;
     // graph fast path
@@ -962,29 +1017,6 @@ int check_dev_err(uns_cc_handle* h) {
 
 // Build the forward/backward level schedules of the lusgs2 sweeps: a cell
 // waits for every interior neighbour that precedes it in sweep order.
-void build_levels(int noc, const std::vector<int>& c2f_off, const std::vector<int>& c2f, const int* fin,
-                  const int* fout, bool forward, std::vector<int>& off, std::vector<int>& cells) {
-    std::vector<int> lev(noc, 0);
-    int maxl = 0;
-    for (int s = 0; s < noc; ++s) {
-        int it = forward ? s : noc - 1 - s;
-        int l = 0;
-        for (int k = c2f_off[it]; k < c2f_off[it + 1]; ++k) {
-            int c = c2f[k];
-            int nb = fin[c] == it ? fout[c] : fin[c];
-            if (nb < 0 || nb >= noc || nb == it) continue;
-            if (forward ? nb < it : nb > it) l = std::max(l, lev[nb] + 1);
-        }
-        lev[it] = l;
-        maxl = std::max(maxl, l);
-    }
-    off.assign(maxl + 2, 0);
-    for (int i = 0; i < noc; ++i) off[lev[i] + 1]++;
-    for (int l = 0; l <= maxl; ++l) off[l + 1] += off[l];
-    cells.assign(noc, 0);
-    std::vector<int> pos(off.begin(), off.end() - 1);
-    for (int i = 0; i < noc; ++i) cells[pos[lev[i]]++] = i;
-}
 
 void launch_cfg(int n, dim3& g, dim3& b) { b = dim3(kBlock); g = dim3(std::max(1, nblocks(n))); }
 
@@ -1047,20 +1079,21 @@ int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int par
 }
 
 int enqueue_lusgs(uns_cc_handle* h, CCView& v) {
-    if (v.nfi > 0) LAUNCH(k_cc_fold, v.nfi, v);
-    UNS_CUDA(cudaMemsetAsync(v.lower, 0, sizeof(double4) * v.noc, h->stream));
-    UNS_CUDA(cudaMemsetAsync(v.upper, 0, sizeof(double4) * v.noc, h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int) * v.noc, h->stream));
+    if (v.nrec > 0) LAUNCH(k_cc_sweep_prep, v.nrec, v);
+    const long long n2 = 2LL * v.noc * 2;  // double2 per record array
+    k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_a, n2);
+    k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_b, n2);
+    UNS_CUDA(cudaGetLastError());
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h->coop_blocks);
-    cfg.blockDim = dim3(kBlock);
+    cfg.blockDim = dim3(kSweepBlock);
     cfg.stream = h->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_lusgs, v, (const int*)h->order, v.noc, 2 * v.noc, h->flag));
+    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_lusgs, v, (const int*)h->woff));
     return UNS_OK;
 }
 
@@ -1224,8 +1257,8 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     AL(gx, noc); AL(gy, noc); AL(phi, noc); AL(dt, noc); AL(la, noc); AL(mul, ntot);
     AL(pp, nop); AL(ppT, nop); AL(fq, nof); AL(fqT, nof); AL(fla, nof); AL(fmu, nof);
     AL(fF, nof); AL(fV, nof); AL(fgx, nof); AL(fgy, nof); AL(fgT, nof); AL(fasum, nof);
-    AL(fwall, nbf); AL(fwallv, nbf); AL(lower, noc); AL(upper, noc);
-    AL(diag, noc); AL(fold1, nfi); AL(fold2, nfi); AL(pw, noc); AL(pe, noc);
+    AL(fwall, nbf); AL(fwallv, nbf);
+    AL(diag, noc); AL(rec_a, 2 * (size_t)noc); AL(rec_b, 2 * (size_t)noc);
     AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
     h->nparts = nblocks(noc);
     AL(partial, h->nparts);
@@ -1233,25 +1266,49 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     if ((rc = h->alloc(h->d_iter, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
-    // LU-SGS dataflow order on the reference cell order.
+    // LU-SGS warp schedule on the reference c2f lists.
     {
         int maxdeg = 0;
         for (int i = 0; i < noc; ++i) maxdeg = std::max(maxdeg, m->c2f_off[i + 1] - m->c2f_off[i]);
         if (maxdeg > 32) { set_last_error("uns_cc_create: a cell has more than 32 faces"); return fail(UNS_ERR_MESH); }
-        std::vector<int> off, fwd, bwd;
-        std::vector<int> c2fo(m->c2f_off, m->c2f_off + noc + 1), c2fv(m->c2f, m->c2f + m->c2f_off[noc]);
-        build_levels(noc, c2fo, c2fv, m->fin, m->fout, true, off, fwd);
-        build_levels(noc, c2fo, c2fv, m->fin, m->fout, false, off, bwd);
-        fwd.insert(fwd.end(), bwd.begin(), bwd.end());
-        if ((rc = h->upload(h->order, fwd.data(), fwd.size()))) return fail(rc);
-        if ((rc = h->alloc(h->flag, noc))) return fail(rc);
+        if (noc >= (1 << 30)) { set_last_error("uns_cc_create: too many cells"); return fail(UNS_ERR_MESH); }
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lusgs, kBlock, 0) != cudaSuccess || per < 1) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_lusgs, kSweepBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_cc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
         h->coop_blocks = nsm * std::min(per, 4);
+        // the cell across each c2f face (ghosts >= noc), and whether the face
+        // normal points into the cell
+        auto other = [&](int i, int f, int* flip) {
+            if (m->fout[f] == i) { *flip = 1; return m->fin[f]; }
+            *flip = 0;
+            return m->fout[f];
+        };
+        std::vector<int> nbr(m->c2f_off[noc]);
+        for (int i = 0; i < noc; ++i)
+            for (int k = m->c2f_off[i]; k < m->c2f_off[i + 1]; ++k) {
+                int fl;
+                nbr[k] = other(i, m->c2f[k], &fl);
+            }
+        WarpSchedule ws = list_schedule(noc, m->c2f_off, nbr.data(), h->coop_blocks * (kSweepBlock / 32));
+        std::vector<int4> sched(ws.items.size());
+        std::vector<int> rf, rn, rl;
+        for (size_t pos = 0; pos < ws.items.size(); ++pos) {
+            const int it = ws.items[pos] >> 1, pass = ws.items[pos] & 1;
+            const int first = (int)rf.size();
+            for (int k = m->c2f_off[it]; k < m->c2f_off[it + 1]; ++k) {
+                int fl, nb = other(it, m->c2f[k], &fl);
+                bool take = nb >= 0 && nb < noc && (pass == 0 ? nb < it : nb > it);
+                if (take) { rf.push_back(m->c2f[k]); rn.push_back(nb); rl.push_back(fl); }
+            }
+            sched[pos] = make_int4(it, pass, first, (int)rf.size() - first);
+        }
+        v.nrec = (int)rf.size();
+        if ((rc = h->upload(h->woff, ws.off.data(), ws.off.size()))) return fail(rc);
+        UP(sched, sched); UP(rec_face, rf); UP(rec_nb, rn); UP(rec_flip, rl);
+        AL(rec, 3 * rf.size());
     }
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) { set_last_error("uns_cc_create: upload failed"); return fail(UNS_ERR_CUDA); }
     rc = uns_cc_initialize(h);

@@ -1,6 +1,6 @@
 // uns_common.cuh -- shared plumbing of the UNSFlow2D GB300 library: status
-// handling, the device error word, warp reductions and the bounded
-// acquire/release flag waits of the dataflow LU-SGS sweeps.
+// handling, the device error word, warp reductions and the bounded record
+// polls of the LU-SGS sweeps.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -48,27 +48,61 @@ __device__ __forceinline__ T warp_sum(T v) {
 // Bound on every spin-wait in the library's kernels (~2 s at 2 GHz).
 constexpr long long kWaitCycles = 4000000000LL;
 
-// L2-coherent (L1-bypassing) 32-byte load / store for data that other SMs
-// publish within the same kernel.
-__device__ __forceinline__ double4 ldcg4(const double4* p) {
-    const double2* q = reinterpret_cast<const double2*>(p);
-    double2 a = __ldcg(q), b = __ldcg(q + 1);
-    return make_double4(a.x, a.y, b.x, b.y);
-}
-__device__ __forceinline__ void stcg4(double4* p, const double4& v) {
-    double2* q = reinterpret_cast<double2*>(p);
-    __stcg(q, make_double2(v.x, v.y));
-    __stcg(q + 1, make_double2(v.z, v.w));
-}
+// ---------------------------------------------------------------------------
+// Sweep records.  Each LU-SGS sweep item publishes its values once, into
+// slots pre-filled with kUnset: a signalling-NaN bit pattern, which no
+// floating-point operation produces (IEEE 754 results are never signalling
+// NaNs).  A consumer polls the slots themselves until none holds kUnset, so
+// a value and its "ready" state travel together: the producer needs no
+// release fence and the consumer no separate flag load.  Every slot is an
+// aligned 64-bit word written exactly once per sweep, so a value that is not
+// kUnset is final.
+constexpr unsigned long long kUnset = 0x7FF40000DEAD0001ULL;
 
-// Acquire / release accesses to per-node completion flags (dataflow sweeps).
-__device__ __forceinline__ int ld_acquire(const int* p) {
-    int v;
-    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+__device__ __forceinline__ bool is_unset(double x) {
+    return (unsigned long long)__double_as_longlong(x) == kUnset;
+}
+__device__ __forceinline__ double2 ld_relaxed2(const double2* p) {
+    double2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void st_release(int* p, int v) {
-    asm volatile("st.release.gpu.global.s32 [%0], %1;" : : "l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed2(double2* p, double a, double b) {
+    asm volatile("st.relaxed.gpu.global.v2.f64 [%0], {%1, %2};" : : "l"(p), "d"(a), "d"(b) : "memory");
+}
+
+// Reads n2 consecutive double2 of a record into out[0 .. 2*n2), waiting
+// until none is kUnset.  Bounded: gives up after kWaitCycles (or as soon as
+// another thread has recorded UNS_ERR_TIMEOUT) and records UNS_ERR_TIMEOUT,
+// so no sweep wait can hang the device.
+template <int n2>
+__device__ __forceinline__ bool poll_record(const double4* rec, double* out, DevErr* err) {
+    const double2* p = reinterpret_cast<const double2*>(rec);
+    long long t0 = 0;
+    for (int spins = 0;; ++spins) {
+        bool ready = true;
+#pragma unroll
+        for (int k = 0; k < n2; ++k) {
+            double2 x = ld_relaxed2(p + k);
+            out[2 * k] = x.x;
+            out[2 * k + 1] = x.y;
+            ready = ready && !is_unset(x.x) && !is_unset(x.y);
+        }
+        if (ready) return true;
+        if (spins == 0) t0 = clock64();
+        if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > kWaitCycles) {
+            set_err(err, UNS_ERR_TIMEOUT, -1);
+            return false;
+        }
+        if (spins > 64) __nanosleep(32);
+    }
+}
+
+// Fills n doubles with kUnset (re-arms the records before a sweep).
+static __global__ void __launch_bounds__(kBlock) k_fill_unset(double2* p, long long n2) {
+    const double u = __longlong_as_double((long long)kUnset);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n2; i += (long long)gridDim.x * blockDim.x)
+        p[i] = make_double2(u, u);
 }
 
 // Three-stage RK weights q = a*qold + b*(qc - dt/area*res), stage irk = 1..3
@@ -76,24 +110,5 @@ __device__ __forceinline__ void st_release(int* p, int v) {
 // Selected by branch, not by indexing a local table (which lands on the stack).
 __device__ __forceinline__ double rk3_a(int irk) { return irk == 2 ? 3.0 / 4.0 : (irk == 3 ? 1.0 / 3.0 : 0.0); }
 __device__ __forceinline__ double rk3_b(int irk) { return irk == 2 ? 1.0 / 4.0 : (irk == 3 ? 2.0 / 3.0 : 1.0); }
-
-// Waits until *flag >= want.  Bounded: gives up after kWaitCycles (or as
-// soon as another thread has recorded UNS_ERR_TIMEOUT) and records
-// UNS_ERR_TIMEOUT, so no dataflow wait can hang the device.
-__device__ __forceinline__ bool wait_flag(const int* flag, int want, DevErr* err) {
-    if (ld_acquire(flag) >= want) return true;
-    long long t0 = clock64();
-    int spins = 0;
-    while (ld_acquire(flag) < want) {
-        if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > kWaitCycles) {
-            set_err(err, UNS_ERR_TIMEOUT, -1);
-            return false;
-        }
-        // Dependencies usually land within a microsecond: poll tightly first,
-        // then back off so long waits leave issue slots to the producers.
-        if (++spins > 64) __nanosleep(32);
-    }
-    return true;
-}
 
 }  // namespace uns

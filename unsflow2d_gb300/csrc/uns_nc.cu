@@ -23,6 +23,7 @@
 
 #include "uns_common.cuh"
 #include "uns_phys.cuh"
+#include "uns_sched.hpp"
 #include "unsflow_gpu.h"
 
 using namespace uns;
@@ -62,12 +63,18 @@ struct NCView {
     double4* bres1;  // boundary closure residual into fp1 / fp2
     double4* bres2;
     double2* bla;    // boundary closure spectral radius into fp1 / fp2
-    double4* fold1;  // normalflux(qold(fp1)) on the edge (LU-SGS)
-    double4* fold2;
-    double4* dqc;
+    // LU-SGS sweep schedule (host-built): per position of the warp lists
+    // (it, pass, first record, records); per record, in the reference v2f
+    // order of the taken edges: edge, neighbour, orientation sign.
+    const int4* sched;
+    const int* rec_edge;
+    const int* rec_nb;
+    const int* rec_sign;
+    int nrec;
+    double4* rec;    // per record, per LU-SGS call: 3 x double4, see k_nc_sweep_prep
     double* diag;    // LU-SGS diagonal cv/dt + 0.5*omega*la (lusgs.f90:36)
-    double4* pw;     // sweep-published primitives of qc: (rho, u, v, p)
-    double* pe;      // and e*rho, as normalflux forms them (lusgs.f90:144-147)
+    double4* rec_a;  // sweep records [pass * nop + node]: (u, v, p, e*rho) of qc
+    double4* rec_b;  //   and dqc; rho is rebuilt as qold.rho + dqc.rho
     double* partial;   // [2*nblk]: sum, max
     int* partial_i;    // argmax
     DevErr* err;
@@ -440,111 +447,166 @@ __device__ __forceinline__ void normalflux_nc(const Gas& g, const double4& q, do
     for (int k = 0; k < 4; ++k) o[k] = o[k] * ds;
 }
 
-__global__ void __launch_bounds__(kBlock) k_nc_fold(NCView v) {
+constexpr int kSweepBlock = 128;
+constexpr double kOmega = 1.5;  // lusgs.f90:28
+
+// Per LU-SGS call: everything a sweep item needs from an edge that does not
+// change during the sweeps, laid out contiguously in schedule order so a
+// lane fetches it with three 32-byte loads and no index chasing:
+//   rec[3r]   normalflux(qold(nb)) on the edge (lusgs.f90:137-155)
+//   rec[3r+1] (nx, ny, ds, omega * la)
+//   rec[3r+2] (qold(nb).rho, sign, nb as integer bits, 0)
+__global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     if (stopped(v)) return;
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= v.nof) return;
-    int2 p = v.fpt[f];
-    double2 n = v.fn[f];
-    double ds = v.farea[f], o[4];
-    normalflux_nc(v.g, v.qold[p.x], n.x, n.y, ds, o);
-    v.fold1[f] = m4(o);
-    normalflux_nc(v.g, v.qold[p.y], n.x, n.y, ds, o);
-    v.fold2[f] = m4(o);
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= v.nrec) return;
+    const int c = v.rec_edge[r], nb = v.rec_nb[r];
+    const double2 n = v.fn[c];
+    const double ds = v.farea[c];
+    const double4 q = v.qold[nb];
+    double o[4];
+    normalflux_nc(v.g, q, n.x, n.y, ds, o);
+    v.rec[3 * (size_t)r] = m4(o);
+    v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
+    v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
 }
 
 // normalflux (lusgs.f90:137-155) from primitives a sweep has published.
-__device__ __forceinline__ void normalflux_prims(const double4& w, double et, double nx, double ny, double ds,
-                                                 double o[4]) {
-    double un = w.y * nx + w.z * ny;
-    o[0] = (et + w.w) * un;
-    o[1] = w.x * un;
-    o[2] = o[1] * w.y + w.w * nx;
-    o[3] = o[1] * w.z + w.w * ny;
+__device__ __forceinline__ void normalflux_prims(double rho, double u, double vv, double p, double et, double nx,
+                                                 double ny, double ds, double o[4]) {
+    double un = u * nx + vv * ny;
+    o[0] = (et + p) * un;
+    o[1] = rho * un;
+    o[2] = o[1] * u + p * nx;
+    o[3] = o[1] * vv + p * ny;
 #pragma unroll
     for (int k = 0; k < 4; ++k) o[k] = o[k] * ds;
 }
 
-// lusgs sweeps (lusgs.f90:48-124) as a dataflow kernel.  Items are the
-// forward sweep's nodes sorted by dependency level, then the backward sweep's;
-// item s goes to warp s mod (warps in the grid).  A warp's lanes take the
-// node's edges (reference v2f order), wait for the neighbour's completion flag
-// when that neighbour precedes the node in the sweep, and form the edge term
-// from the primitives the neighbour published; lane 0 adds the terms in edge
-// order -- the reference's summation order -- updates the node, publishes its
-// primitives (the con2prim a later normalflux of this node would do) and
-// releases its flag.  Every wait targets an earlier item, and the cooperative
-// launch keeps all warps resident, so the sweep always completes; each wait is
-// also bounded (wait_flag).
-__global__ void __launch_bounds__(kBlock) k_nc_lusgs(NCView v, const int* __restrict__ order, int nfwd, int nitems,
-                                                     int* flag) {
-    __shared__ double sterm[kBlock / 32][32][4];
-    const double omega = 1.5;
+__device__ __forceinline__ double pick4(int k, double a, double b, double c, double d) {
+    return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d));
+}
+
+// What a lane loads ahead for one sweep item: its record (lanes < records)
+// and, in lanes 0..3, variable `lane` of the node's own data.
+struct SweepIn {
+    double f1[4], nx, ny, ds, ol, rho_old, sign;
+    int nb;
+    double D, o, r;
+};
+
+__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
+    if (lane < S.w) {
+        const double4* p = v.rec + 3 * (size_t)(S.z + lane);
+        double4 a = p[0], b = p[1], c = p[2];
+        x.f1[0] = a.x; x.f1[1] = a.y; x.f1[2] = a.z; x.f1[3] = a.w;
+        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+        x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
+    }
+    if (lane < 4) {
+        x.D = v.diag[S.x];
+        x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
+        if (S.y == 0) x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
+    }
+}
+
+// lusgs sweeps (lusgs.f90:48-124) as one cooperative launch.  Each warp runs
+// its own list of items (node, pass) from the host-side list schedule, in
+// order, loading the next item's inputs while it works on the current one.
+// Per item: lane j takes the j-th edge (reference v2f order) whose neighbour
+// precedes the node in this pass; it takes the neighbour's values from
+// registers when the warp itself computed that neighbour last, else polls
+// its record, and forms the edge term; lanes 0..3 add the terms of one
+// variable each in edge order (the reference's summation order) and divide
+// by the diagonal; the new state is shuffled to all lanes, which form its
+// primitives (kept for the next item) while lanes 0 and 1 publish the record.
+__global__ void __launch_bounds__(kSweepBlock) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
+    __shared__ double sterm[kSweepBlock / 32][32][4];
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gw = blockIdx.x * (kBlock / 32) + wib, nw = gridDim.x * (kBlock / 32);
+    const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
     if (stopped(v)) return;
-    for (int s = gw; s < nitems; s += nw) {
-        const int pass = s < nfwd ? 0 : 1;
-        const int it = order[s];
-        const int k0 = v.rv2f_off[it], deg = v.rv2f_off[it + 1] - k0;
-        bool take = false, ok = true;
+    const int n = v.nop;
+    const int kbeg = woff[gw], kend = woff[gw + 1];
+    if (kbeg >= kend) return;
+    const int4 none = make_int4(0, 0, 0, 0);
+    int4 S = v.sched[kbeg];
+    int4 Sn = kbeg + 1 < kend ? v.sched[kbeg + 1] : none;
+    SweepIn X = {}, Xn = {};
+    sweep_load(v, S, lane, X);
+    int last = -1;  // code of the warp's previous item; its values below, in every lane
+    double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    for (int k = kbeg; k < kend; ++k) {
+        // ---- next item's inputs (independent of the sweep), in flight meanwhile
+        const int4 Snn = k + 2 < kend ? v.sched[k + 2] : none;
+        if (k + 1 < kend) sweep_load(v, Sn, lane, Xn);
+        const int it = S.x, pass = S.y, ntake = S.w;
+        // ---- values of earlier items
+        bool ok = true;
         double t4[4] = {0.0, 0.0, 0.0, 0.0};
-        if (lane < deg) {
-            int c = v.rv2f[k0 + lane];
-            int2 p = v.fpt[c];
-            int nb = p.y;
-            double sign = 1.0;
-            bool nb_is_p1 = false;
-            if (nb == it) { nb = p.x; sign = -1.0; nb_is_p1 = true; }
-            take = pass == 0 ? (nb < it && nb >= 0) : (nb > it && nb >= 0);
-            if (take) {
-                ok = wait_flag(flag + nb, pass + 1, v.err);
-                if (ok) {
-                    double2 n = v.fn[c];
-                    double f1[4], f2[4], dq[4];
-                    g4(nb_is_p1 ? v.fold1[c] : v.fold2[c], f1);
-                    normalflux_prims(ldcg4(&v.pw[nb]), __ldcg(&v.pe[nb]), n.x, n.y, v.farea[c], f2);
-                    g4(ldcg4(&v.dqc[nb]), dq);
-                    double ol = omega * v.fla[c];
+        if (lane < ntake) {
+            double w[8], rho;
+            if (((X.nb << 1) | pass) == last) {
+                w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
+                rho = Lrho;
+            } else {
+                const size_t slot = (size_t)pass * n + X.nb;
+                ok = poll_record<2>(v.rec_a + slot, w, v.err) && poll_record<2>(v.rec_b + slot, w + 4, v.err);
+                rho = X.rho_old + w[5];
+            }
+            if (ok) {
+                double f2[4];
+                normalflux_prims(rho, w[0], w[1], w[2], w[3], X.nx, X.ny, X.ds, f2);
 #pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) t4[iv] = 0.5 * (sign * (f2[iv] - f1[iv]) - ol * dq[iv]);
-                }
+                for (int iv = 0; iv < 4; ++iv) t4[iv] = 0.5 * (X.sign * (f2[iv] - X.f1[iv]) - X.ol * w[4 + iv]);
             }
         }
-        if (pass == 1 && lane == 0) ok = ok && wait_flag(flag + it, 1, v.err);  // own forward value
-        if (__ballot_sync(0xffffffffu, !ok)) return;
-        unsigned taken = __ballot_sync(0xffffffffu, take);
+        double r = X.r;
+        if (pass == 1 && lane < 4) {  // own forward dqc
+            if ((it << 1) == last) {
+                r = pick4(lane, L0, L1, L2, L3);
+            } else {
+                double dq[4];
+                ok = ok && poll_record<2>(v.rec_b + it, dq, v.err);
+                r = pick4(lane, dq[0], dq[1], dq[2], dq[3]);
+            }
+        }
+        if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
 #pragma unroll
         for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
         __syncwarp();
-        if (lane == 0) {
-            double cres[4] = {0.0, 0.0, 0.0, 0.0};
-            for (int j = 0; j < deg; ++j)
-                if (taken & (1u << j))
-#pragma unroll
-                    for (int iv = 0; iv < 4; ++iv) cres[iv] = cres[iv] + sterm[wib][j][iv];
-            const double D = v.diag[it];
-            double d[4], o[4], r[4], q[4];
-            g4(v.qold[it], o);
-            if (pass == 0) {
-                g4(v.res[it], r);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) d[iv] = (-r[iv] - cres[iv]) / D;
-            } else {
-                g4(ldcg4(&v.dqc[it]), d);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) d[iv] = d[iv] - cres[iv] / D;
-            }
-#pragma unroll
-            for (int iv = 0; iv < 4; ++iv) q[iv] = o[iv] + d[iv];
-            Prim P = con2prim(v.g, q[0], q[1], q[2], q[3]);
-            stcg4(&v.dqc[it], m4(d));
-            stcg4(&v.pw[it], make_double4(P.rho, P.u, P.v, P.p));
-            __stcg(&v.pe[it], P.e * P.rho);
-            v.qc[it] = m4(q);
-            st_release(flag + it, pass + 1);
+        double d = 0.0, q = 0.0;
+        if (lane < 4) {
+            double cres = 0.0;
+            for (int j = 0; j < ntake; ++j) cres = cres + sterm[wib][j][lane];
+            d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
+            q = X.o + d;
         }
         __syncwarp();
+        const double q0 = __shfl_sync(full, q, 0), q1 = __shfl_sync(full, q, 1), q2 = __shfl_sync(full, q, 2),
+                     q3 = __shfl_sync(full, q, 3);
+        L0 = __shfl_sync(full, d, 0);
+        L1 = __shfl_sync(full, d, 1);
+        L2 = __shfl_sync(full, d, 2);
+        L3 = __shfl_sync(full, d, 3);
+        Prim P = con2prim(v.g, q0, q1, q2, q3);
+        Lrho = P.rho; Lu = P.u; Lv = P.v; Lp = P.p; Le = P.e * P.rho;
+        last = (it << 1) | pass;
+        const size_t slot = (size_t)pass * n + it;
+        if (lane == 0) {
+            double2* a = reinterpret_cast<double2*>(v.rec_a + slot);
+            st_relaxed2(a, Lu, Lv);
+            st_relaxed2(a + 1, Lp, Le);
+        } else if (lane == 1) {
+            double2* b = reinterpret_cast<double2*>(v.rec_b + slot);
+            st_relaxed2(b, L0, L1);
+            st_relaxed2(b + 1, L2, L3);
+        } else if (lane == 2 && pass == 1) {
+            v.qc[it] = make_double4(q0, q1, q2, q3);
+        }
+        S = Sn;
+        Sn = Snn;
+        X = Xn;
     }
 }
 
@@ -555,29 +617,6 @@ __global__ void k_nc_initialize(NCView v, double4 qinf, double phi0) {
     v.phi[i] = make_double4(phi0, phi0, phi0, phi0);
 }
 
-void build_levels_nc(int nop, const int* v2f_off, const int* v2f, const int* fp1, const int* fp2, bool forward,
-                     std::vector<int>& off, std::vector<int>& nodes) {
-    std::vector<int> lev(nop, 0);
-    int maxl = 0;
-    for (int s = 0; s < nop; ++s) {
-        int it = forward ? s : nop - 1 - s;
-        int l = 0;
-        for (int k = v2f_off[it]; k < v2f_off[it + 1]; ++k) {
-            int c = v2f[k];
-            int nb = fp2[c] == it ? fp1[c] : fp2[c];
-            if (nb < 0 || nb == it) continue;
-            if (forward ? nb < it : nb > it) l = std::max(l, lev[nb] + 1);
-        }
-        lev[it] = l;
-        maxl = std::max(maxl, l);
-    }
-    off.assign(maxl + 2, 0);
-    for (int i = 0; i < nop; ++i) off[lev[i] + 1]++;
-    for (int l = 0; l <= maxl; ++l) off[l + 1] += off[l];
-    nodes.assign(nop, 0);
-    std::vector<int> pos(off.begin(), off.end() - 1);
-    for (int i = 0; i < nop; ++i) nodes[pos[lev[i]]++] = i;
-}
 
 }  // namespace
 
@@ -587,8 +626,7 @@ struct uns_nc_handle {
     cudaStream_t stream = nullptr;
     std::vector<void*> allocs;
     int nparts = 0;
-    int* order = nullptr;   // forward items (level order) then backward items
-    int* flag = nullptr;    // per-node sweep progress: 0, 1 forward done, 2 backward done
+    int* woff = nullptr;    // LU-SGS warp schedule: per-warp ranges of v.sched
     int coop_blocks = 0;
     double4 qinf;
     cudaGraphExec_t graph = nullptr;
@@ -654,23 +692,25 @@ int enqueue_fvres_nc(uns_nc_handle* h, NCView& v, double cfl, int irk, int parti
 }
 
 int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
-    UNS_CUDA(cudaMemsetAsync(v.dqc, 0, sizeof(double4) * v.nop, h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->flag, 0, sizeof(int) * v.nop, h->stream));
+    const long long n2 = 2LL * v.nop * 2;  // double2 per record array
+    k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_a, n2);
+    k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_b, n2);
+    UNS_CUDA(cudaGetLastError());
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(h->coop_blocks);
-    cfg.blockDim = dim3(kBlock);
+    cfg.blockDim = dim3(kSweepBlock);
     cfg.stream = h->stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->order, v.nop, 2 * v.nop, h->flag));
+    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->woff));
     return UNS_OK;
 }
 
 int enqueue_lusgs_nc(uns_nc_handle* h, NCView& v) {
-    NLAUNCH(k_nc_fold, v.nof, v);
+    if (v.nrec > 0) NLAUNCH(k_nc_sweep_prep, v.nrec, v);
     return launch_sweeps_nc(h, v);
 }
 
@@ -782,7 +822,8 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
     ALN(qc, nop); ALN(qp, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
-    ALN(fold1, nof); ALN(fold2, nof); ALN(dqc, nop); ALN(diag, nop); ALN(pw, nop); ALN(pe, nop); ALN(err, 1);
+    ALN(diag, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
+    ALN(err, 1);
     h->nparts = nblocks(nop);
     ALN(partial, 2 * h->nparts);
     ALN(partial_i, h->nparts);
@@ -791,23 +832,47 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
     {
-        // Dataflow order of the two sweeps; a warp per node handles up to 32 edges.
+        // LU-SGS warp schedule; a warp per item handles up to 32 edges.
         int maxdeg = 0;
         for (int i = 0; i < nop; ++i) maxdeg = std::max(maxdeg, m->v2f_off[i + 1] - m->v2f_off[i]);
         if (maxdeg > 32) { set_last_error("uns_nc_create: a node has more than 32 edges"); return fail(UNS_ERR_MESH); }
-        std::vector<int> off, fwd, bwd;
-        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, true, off, fwd);
-        build_levels_nc(nop, m->v2f_off, m->v2f, m->fp1, m->fp2, false, off, bwd);
-        fwd.insert(fwd.end(), bwd.begin(), bwd.end());
-        if ((rc = h->upload(h->order, fwd.data(), fwd.size()))) return fail(rc);
-        if ((rc = h->alloc(h->flag, nop))) return fail(rc);
+        if (nop >= (1 << 30)) { set_last_error("uns_nc_create: too many nodes"); return fail(UNS_ERR_MESH); }
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs, kBlock, 0) != cudaSuccess || per < 1) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs, kSweepBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_nc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
         h->coop_blocks = nsm * std::min(per, 4);
+        // other end of each v2f edge, and the reference's orientation sign
+        auto other = [&](int i, int e, int* sign) {
+            if (m->fp2[e] == i) { *sign = -1; return m->fp1[e]; }
+            *sign = 1;
+            return m->fp2[e];
+        };
+        std::vector<int> nbr(m->v2f_off[nop]);
+        for (int i = 0; i < nop; ++i)
+            for (int k = m->v2f_off[i]; k < m->v2f_off[i + 1]; ++k) {
+                int sg;
+                nbr[k] = other(i, m->v2f[k], &sg);
+            }
+        WarpSchedule ws = list_schedule(nop, m->v2f_off, nbr.data(), h->coop_blocks * (kSweepBlock / 32));
+        std::vector<int4> sched(ws.items.size());
+        std::vector<int> re, rn, rs;
+        for (size_t pos = 0; pos < ws.items.size(); ++pos) {
+            const int it = ws.items[pos] >> 1, pass = ws.items[pos] & 1;
+            const int first = (int)re.size();
+            for (int k = m->v2f_off[it]; k < m->v2f_off[it + 1]; ++k) {
+                int sg, nb = other(it, m->v2f[k], &sg);
+                bool take = nb >= 0 && nb < nop && (pass == 0 ? nb < it : nb > it);
+                if (take) { re.push_back(m->v2f[k]); rn.push_back(nb); rs.push_back(sg); }
+            }
+            sched[pos] = make_int4(it, pass, first, (int)re.size() - first);
+        }
+        h->v.nrec = (int)re.size();
+        if ((rc = h->upload(h->woff, ws.off.data(), ws.off.size()))) return fail(rc);
+        UPN(sched, sched); UPN(rec_edge, re); UPN(rec_nb, rn); UPN(rec_sign, rs);
+        ALN(rec, 3 * re.size());
     }
 #undef UPN
 #undef ALN
@@ -980,7 +1045,7 @@ int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_ite
 void* uns_nc_stream(uns_nc_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
-    static const char* kNames[] = {"save_old", "grad_lim", "edge", "node_res", "fold", "lusgs_sweeps", "residue"};
+    static const char* kNames[] = {"save_old", "grad_lim", "edge", "node_res", "sweep_prep", "lusgs_sweeps", "residue"};
     const int NP = 7;
     if (!h || reps < 1 || !ms) return UNS_ERR_ARG;
     std::vector<double> acc(NP, 0.0);
@@ -1013,7 +1078,7 @@ int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const cha
             if (!rc) rc = timed(3, [&]() -> int { NLAUNCH(k_nc_node_res, v.nop, v, cfl, rk3 ? irk : 0, rk3 ? (irk == 3) : 1); return UNS_OK; });
         }
         if (!rk3) {
-            if (!rc) rc = timed(4, [&]() -> int { NLAUNCH(k_nc_fold, v.nof, v); return UNS_OK; });
+            if (!rc) rc = timed(4, [&]() -> int { if (v.nrec > 0) NLAUNCH(k_nc_sweep_prep, v.nrec, v); return UNS_OK; });
             if (!rc) rc = timed(5, [&]() -> int { return launch_sweeps_nc(h, v); });
         }
         if (!rc) rc = timed(6, [&]() -> int {
