@@ -797,6 +797,9 @@ __device__ __forceinline__ void nflux_prims(const double4& w, double et, double 
 }
 
 constexpr int kSweepBlock = 128;
+// One sweep block per SM: one warp per SM sub-partition, so concurrently
+// active items never share an FP64 unit.
+constexpr int kSweepBlocksPerSM = 1;
 constexpr double kOmega = 1.5;  // lusgs.F90:229
 
 // Per LU-SGS call: everything a sweep item needs from a face that does not
@@ -825,46 +828,58 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
     return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d));
 }
 
-// What a lane loads ahead for one sweep item: its record (lanes < records)
-// and, in lanes 0..3, variable `lane` of the cell's own data.
+// Lanes of a sweep item: lane = 4 * slot + k, slot = the taken face (up to 8
+// per round), k = the variable.  An FP64 instruction costs its SM
+// sub-partition the same whatever the number of active lanes, so each item's
+// arithmetic is spread over the lanes: the four flux components of up to
+// eight faces in one pass, the per-variable sums and divides in lanes 0..3,
+// and the three divisions of con2prim in lanes 0, 2 and 3 at once.
 struct SweepIn {
-    double f1[4], nx, ny, area, ol, rho_old;
+    double f1, nx, ny, area, ol, rho_old;  // the slot's record; f1 = component k
     int nb;
-    double D, o, r;
+    double D, o, r;  // lanes 0..3: the cell's diagonal, qold and res, variable k
 };
 
+__device__ __forceinline__ void sweep_load_face(const CCView& v, int rec, int k, SweepIn& x) {
+    const double4* p = v.rec + 3 * (size_t)rec;
+    x.f1 = reinterpret_cast<const double*>(p)[k];
+    double4 b = p[1], c = p[2];
+    x.nx = b.x; x.ny = b.y; x.area = b.z; x.ol = b.w;
+    x.rho_old = c.x; x.nb = (int)__double_as_longlong(c.z);
+}
+
 __device__ __forceinline__ void sweep_load(const CCView& v, const int4& S, int lane, SweepIn& x) {
-    if (lane < S.w) {
-        const double4* p = v.rec + 3 * (size_t)(S.z + lane);
-        double4 a = p[0], b = p[1], c = p[2];
-        x.f1[0] = a.x; x.f1[1] = a.y; x.f1[2] = a.z; x.f1[3] = a.w;
-        x.nx = b.x; x.ny = b.y; x.area = b.z; x.ol = b.w;
-        x.rho_old = c.x; x.nb = (int)__double_as_longlong(c.z);
-    }
+    if ((lane >> 2) < S.w) sweep_load_face(v, S.z + (lane >> 2), lane & 3, x);
     if (lane < 4) {
         x.D = v.diag[S.x];
         x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
         if (S.y == 0) x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
+    } else {  // benign operands: the warp-wide divides must not meet 0 or inf
+        x.D = 1.0;
+        x.o = 1.0;
+        x.r = 0.0;
     }
 }
 
 // lusgs2 sweeps (lusgs.F90:245-318) as one cooperative launch.  Each warp runs
 // its own list of items (cell, pass) from the host-side list schedule, in
 // order, loading the next item's inputs while it works on the current one.
-// Per item: lane j takes the j-th face (reference c2f order) whose neighbour
-// precedes the cell in this pass; it takes the neighbour's values from
-// registers when the warp itself computed that neighbour last, else polls its
-// record, and forms area*(F(qold+dq) - F(qold)) - omega*lam*dq; lanes 0..3 add
-// the terms of one variable each in c2f order and apply the diagonal; the new
-// values are shuffled to all lanes, which form the primitives of qold + dq
-// (kept for the next item) while lanes 0 and 1 publish the record.
-__global__ void __launch_bounds__(kSweepBlock) k_lusgs(CCView v, const int* __restrict__ woff) {
-    __shared__ double sterm[kSweepBlock / 32][32][4];
+// Per item, for each face whose neighbour precedes the cell in this pass
+// (reference c2f order): the neighbour's values come from registers when the
+// warp itself computed that neighbour last, else from its polled record; the
+// face term area*(F(qold+dq) - F(qold)) - omega*lam*dq is formed per
+// component; lanes 0..3 add the terms in c2f order and apply the diagonal;
+// the new values are spread to all lanes, which keep the primitives of
+// qold + dq for the next item while lanes 0 and 1 publish the record.  Every
+// operation and operand order is the reference's.
+__global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
+    const int slot = lane >> 2, k = lane & 3;
     if (stopped(v)) return;
     const int n = v.noc;
+    const double gm1 = v.g.gamma - 1.0;
     const int kbeg = woff[gw], kend = woff[gw + 1];
     if (kbeg >= kend) return;
     const int4 none = make_int4(0, 0, 0, 0);
@@ -874,73 +889,81 @@ __global__ void __launch_bounds__(kSweepBlock) k_lusgs(CCView v, const int* __re
     sweep_load(v, S, lane, X);
     int last = -1;  // code of the warp's previous item; its values below, in every lane
     double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
-    for (int k = kbeg; k < kend; ++k) {
-        // ---- next item's inputs (independent of the sweep), in flight meanwhile
-        const int4 Snn = k + 2 < kend ? v.sched[k + 2] : none;
-        if (k + 1 < kend) sweep_load(v, Sn, lane, Xn);
+    for (int kk = kbeg; kk < kend; ++kk) {
+        const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
         const int it = S.x, pass = S.y, ntake = S.w;
-        // ---- values of earlier items
-        bool ok = true;
-        double t4[4] = {0.0, 0.0, 0.0, 0.0};
-        if (lane < ntake) {
-            double w[8], rho;
-            if (((X.nb << 1) | pass) == last) {
-                w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
-                rho = Lrho;
-            } else {
-                const size_t slot = (size_t)pass * n + X.nb;
-                ok = poll_record<2>(v.rec_a + slot, w, v.err) && poll_record<2>(v.rec_b + slot, w + 4, v.err);
-                rho = X.rho_old + w[5];
+        double cres = 0.0;  // lanes 0..3: sum over faces of component k
+        for (int base = 0; base < ntake; base += 8) {
+            SweepIn E = X;
+            if (base > 0 && base + slot < ntake) sweep_load_face(v, S.z + base + slot, k, E);
+            bool ok = true;
+            double t = 0.0;
+            if (base + slot < ntake) {
+                // the neighbour's values: registers when this warp computed it
+                // last, else its record
+                double w[8], rho;
+                if (((E.nb << 1) | pass) == last) {
+                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
+                    rho = Lrho;
+                } else {
+                    const size_t rs = (size_t)pass * n + E.nb;
+                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
+                    rho = E.rho_old + w[5];
+                }
+                // normal_flux (lusgs.F90:348-357) component k, then the face term
+                const double u = w[0], vv = w[1], p = w[2], et = w[3];
+                const double un = u * E.nx + vv * E.ny;
+                const double o1 = rho * un;
+                const double prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
+                const double pn = p * (k == 2 ? E.nx : E.ny);
+                const double o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
+                const double dqk = k == 0 ? w[4] : (k == 1 ? w[5] : (k == 2 ? w[6] : w[7]));
+                t = E.area * (o - E.f1) - E.ol * dqk;
             }
-            if (ok) {
-                double f2[4];
-                nflux_prims(make_double4(rho, w[0], w[1], w[2]), w[3], X.nx, X.ny, f2);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) t4[iv] = X.area * (f2[iv] - X.f1[iv]) - X.ol * w[4 + iv];
-            }
+            if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
+            const int nr = min(8, ntake - base);
+            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
         }
+        // next item's inputs (independent of the sweep), issued once this
+        // item's polls are done so they do not queue ahead of them
+        if (kk + 1 < kend) sweep_load(v, Sn, lane, Xn);
         double r = X.r;
+        bool ok = true;
         if (pass == 1 && lane < 4) {  // own lower
             if ((it << 1) == last) {
                 r = pick4(lane, L0, L1, L2, L3);
             } else {
-                double dq[4];
-                ok = ok && poll_record<2>(v.rec_b + it, dq, v.err);
-                r = pick4(lane, dq[0], dq[1], dq[2], dq[3]);
+                ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
             }
         }
-        if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
-#pragma unroll
-        for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
-        __syncwarp();
-        double d = 0.0, q = 0.0;
-        if (lane < 4) {
-            double cres = 0.0;
-            for (int j = 0; j < ntake; ++j) cres = cres + sterm[wib][j][lane];
-            d = pass == 0 ? (-r - 0.5 * cres) / X.D : r - 0.5 * cres / X.D;
-            q = X.o + d;  // qold + dq (and, after the backward sweep, the new qc)
-        }
-        __syncwarp();
-        const double q0 = __shfl_sync(full, q, 0), q1 = __shfl_sync(full, q, 1), q2 = __shfl_sync(full, q, 2),
-                     q3 = __shfl_sync(full, q, 3);
+        if (__ballot_sync(full, !ok)) return;
+        // lower / upper (lusgs.F90:276-279 / 314-317), component k in lane k
+        const double d = pass == 0 ? (-r - 0.5 * cres) / X.D : r - 0.5 * cres / X.D;
+        const double q = X.o + d;  // qold + dq (and, after the backward sweep, the new qc)
+        // con2prim (pri.F90:13-37): rho = q1, then E/rho, rhou/rho, rhov/rho in lanes 0, 2, 3
+        const double rho = __shfl_sync(full, q, 1);
+        const double quo = q / rho;
+        const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
+        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        const double qq = u * u + vv * vv;
+        const double p = gm1 * (E0 - 0.5 * rho * qq);
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
         L3 = __shfl_sync(full, d, 3);
-        Prim P = con2prim(v.g, q0, q1, q2, q3);
-        Lrho = P.rho; Lu = P.u; Lv = P.v; Lp = P.p; Le = P.e * P.rho;
+        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
         last = (it << 1) | pass;
-        const size_t slot = (size_t)pass * n + it;
+        const size_t slotr = (size_t)pass * n + it;
         if (lane == 0) {
-            double2* a = reinterpret_cast<double2*>(v.rec_a + slot);
+            double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
             st_relaxed2(a, Lu, Lv);
             st_relaxed2(a + 1, Lp, Le);
         } else if (lane == 1) {
-            double2* b = reinterpret_cast<double2*>(v.rec_b + slot);
+            double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
         } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(q0, q1, q2, q3);
+            v.qc[it] = make_double4(E0, rho, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
@@ -1278,7 +1301,7 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
             set_last_error("uns_cc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
-        h->coop_blocks = nsm * std::min(per, 4);
+        h->coop_blocks = nsm * std::min(per, kSweepBlocksPerSM);
         // the cell across each c2f face (ghosts >= noc), and whether the face
         // normal points into the cell
         auto other = [&](int i, int f, int* flip) {

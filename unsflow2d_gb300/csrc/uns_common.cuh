@@ -71,30 +71,43 @@ __device__ __forceinline__ void st_relaxed2(double2* p, double a, double b) {
     asm volatile("st.relaxed.gpu.global.v2.f64 [%0], {%1, %2};" : : "l"(p), "d"(a), "d"(b) : "memory");
 }
 
-// Reads n2 consecutive double2 of a record into out[0 .. 2*n2), waiting
-// until none is kUnset.  Bounded: gives up after kWaitCycles (or as soon as
-// another thread has recorded UNS_ERR_TIMEOUT) and records UNS_ERR_TIMEOUT,
-// so no sweep wait can hang the device.
-template <int n2>
-__device__ __forceinline__ bool poll_record(const double4* rec, double* out, DevErr* err) {
-    const double2* p = reinterpret_cast<const double2*>(rec);
+// Bounded wait shared by the record polls: false (and UNS_ERR_TIMEOUT
+// recorded) once kWaitCycles have passed or another thread has timed out.
+__device__ __forceinline__ bool poll_continue(int spins, long long& t0, DevErr* err) {
+    if (spins == 0) t0 = clock64();
+    if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > kWaitCycles) {
+        set_err(err, UNS_ERR_TIMEOUT, -1);
+        return false;
+    }
+    if (spins > 64) __nanosleep(32);
+    return true;
+}
+
+// Reads the 2 x 32-byte record (a, b) of a sweep item into out[0..8), all
+// four loads in flight together, waiting (bounded) until none is kUnset.
+__device__ __forceinline__ bool poll_record2(const double4* a, const double4* b, double out[8], DevErr* err) {
+    const double2* pa = reinterpret_cast<const double2*>(a);
+    const double2* pb = reinterpret_cast<const double2*>(b);
     long long t0 = 0;
     for (int spins = 0;; ++spins) {
+        double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1), x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
+        out[0] = x0.x; out[1] = x0.y; out[2] = x1.x; out[3] = x1.y;
+        out[4] = x2.x; out[5] = x2.y; out[6] = x3.x; out[7] = x3.y;
         bool ready = true;
 #pragma unroll
-        for (int k = 0; k < n2; ++k) {
-            double2 x = ld_relaxed2(p + k);
-            out[2 * k] = x.x;
-            out[2 * k + 1] = x.y;
-            ready = ready && !is_unset(x.x) && !is_unset(x.y);
-        }
+        for (int j = 0; j < 8; ++j) ready = ready && !is_unset(out[j]);
         if (ready) return true;
-        if (spins == 0) t0 = clock64();
-        if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > kWaitCycles) {
-            set_err(err, UNS_ERR_TIMEOUT, -1);
-            return false;
-        }
-        if (spins > 64) __nanosleep(32);
+        if (!poll_continue(spins, t0, err)) return false;
+    }
+}
+
+// One published value, waiting (bounded) until it is not kUnset.
+__device__ __forceinline__ bool poll_value(const double* p, double& out, DevErr* err) {
+    long long t0 = 0;
+    for (int spins = 0;; ++spins) {
+        asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(out) : "l"(p) : "memory");
+        if (!is_unset(out)) return true;
+        if (!poll_continue(spins, t0, err)) return false;
     }
 }
 

@@ -448,6 +448,9 @@ __device__ __forceinline__ void normalflux_nc(const Gas& g, const double4& q, do
 }
 
 constexpr int kSweepBlock = 128;
+// One sweep block per SM: one warp per SM sub-partition, so concurrently
+// active items never share an FP64 unit.
+constexpr int kSweepBlocksPerSM = 1;
 constexpr double kOmega = 1.5;  // lusgs.f90:28
 
 // Per LU-SGS call: everything a sweep item needs from an edge that does not
@@ -487,46 +490,58 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
     return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d));
 }
 
-// What a lane loads ahead for one sweep item: its record (lanes < records)
-// and, in lanes 0..3, variable `lane` of the node's own data.
+// Lanes of a sweep item: lane = 4 * slot + k, slot = the taken edge (up to 8
+// per round), k = the variable.  An FP64 instruction costs its SM
+// sub-partition the same whatever the number of active lanes, so each item's
+// arithmetic is spread over the lanes: the four flux components of up to
+// eight edges in one pass, the per-variable sums and divides in lanes 0..3,
+// and the three divisions of con2prim in lanes 0, 2 and 3 at once.
 struct SweepIn {
-    double f1[4], nx, ny, ds, ol, rho_old, sign;
+    double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
     int nb;
-    double D, o, r;
+    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
 };
 
+__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
+    const double4* p = v.rec + 3 * (size_t)rec;
+    x.f1 = reinterpret_cast<const double*>(p)[k];
+    double4 b = p[1], c = p[2];
+    x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+    x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
+}
+
 __device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
-    if (lane < S.w) {
-        const double4* p = v.rec + 3 * (size_t)(S.z + lane);
-        double4 a = p[0], b = p[1], c = p[2];
-        x.f1[0] = a.x; x.f1[1] = a.y; x.f1[2] = a.z; x.f1[3] = a.w;
-        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-        x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
-    }
+    if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
     if (lane < 4) {
         x.D = v.diag[S.x];
         x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
         if (S.y == 0) x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
+    } else {  // benign operands: the warp-wide divides must not meet 0 or inf
+        x.D = 1.0;
+        x.o = 1.0;
+        x.r = 0.0;
     }
 }
 
 // lusgs sweeps (lusgs.f90:48-124) as one cooperative launch.  Each warp runs
 // its own list of items (node, pass) from the host-side list schedule, in
 // order, loading the next item's inputs while it works on the current one.
-// Per item: lane j takes the j-th edge (reference v2f order) whose neighbour
-// precedes the node in this pass; it takes the neighbour's values from
-// registers when the warp itself computed that neighbour last, else polls
-// its record, and forms the edge term; lanes 0..3 add the terms of one
-// variable each in edge order (the reference's summation order) and divide
-// by the diagonal; the new state is shuffled to all lanes, which form its
-// primitives (kept for the next item) while lanes 0 and 1 publish the record.
-__global__ void __launch_bounds__(kSweepBlock) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
-    __shared__ double sterm[kSweepBlock / 32][32][4];
+// Per item, for each edge whose neighbour precedes the node in this pass
+// (reference v2f order): the neighbour's values come from registers when the
+// warp itself computed that neighbour last, else from its polled record; the
+// edge term 0.5*(sign*(F(qc) - F(qold)) - omega*la*dqc) is formed per
+// component; lanes 0..3 add the terms in edge order (the reference's
+// summation order) and divide by the diagonal; the new state is spread to all
+// lanes, which keep its primitives for the next item while lanes 0 and 1
+// publish the record.  Every operation and operand order is the reference's.
+__global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
+    const int slot = lane >> 2, k = lane & 3;
     if (stopped(v)) return;
     const int n = v.nop;
+    const double gm1 = v.g.gamma - 1.0;
     const int kbeg = woff[gw], kend = woff[gw + 1];
     if (kbeg >= kend) return;
     const int4 none = make_int4(0, 0, 0, 0);
@@ -536,73 +551,83 @@ __global__ void __launch_bounds__(kSweepBlock) k_nc_lusgs(NCView v, const int* _
     sweep_load(v, S, lane, X);
     int last = -1;  // code of the warp's previous item; its values below, in every lane
     double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
-    for (int k = kbeg; k < kend; ++k) {
-        // ---- next item's inputs (independent of the sweep), in flight meanwhile
-        const int4 Snn = k + 2 < kend ? v.sched[k + 2] : none;
-        if (k + 1 < kend) sweep_load(v, Sn, lane, Xn);
+    for (int kk = kbeg; kk < kend; ++kk) {
+        const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
         const int it = S.x, pass = S.y, ntake = S.w;
-        // ---- values of earlier items
-        bool ok = true;
-        double t4[4] = {0.0, 0.0, 0.0, 0.0};
-        if (lane < ntake) {
-            double w[8], rho;
-            if (((X.nb << 1) | pass) == last) {
-                w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
-                rho = Lrho;
-            } else {
-                const size_t slot = (size_t)pass * n + X.nb;
-                ok = poll_record<2>(v.rec_a + slot, w, v.err) && poll_record<2>(v.rec_b + slot, w + 4, v.err);
-                rho = X.rho_old + w[5];
+        double cres = 0.0;  // lanes 0..3: sum over edges of component k
+        for (int base = 0; base < ntake; base += 8) {
+            SweepIn E = X;
+            if (base > 0 && base + slot < ntake) sweep_load_edge(v, S.z + base + slot, k, E);
+            bool ok = true;
+            double t = 0.0;
+            if (base + slot < ntake) {
+                // the neighbour's values: registers when this warp computed it
+                // last, else its record
+                double w[8], rho;
+                if (((E.nb << 1) | pass) == last) {
+                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
+                    rho = Lrho;
+                } else {
+                    const size_t rs = (size_t)pass * n + E.nb;
+                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
+                    rho = E.rho_old + w[5];
+                }
+                // normalflux (lusgs.f90:144-150) component k, then the edge term
+                const double u = w[0], vv = w[1], p = w[2], et = w[3];
+                const double un = u * E.nx + vv * E.ny;
+                const double o1 = rho * un;
+                const double prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
+                const double pn = p * (k == 2 ? E.nx : E.ny);
+                double o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
+                o = o * E.ds;
+                const double diff = o - E.f1;
+                const double dqk = k == 0 ? w[4] : (k == 1 ? w[5] : (k == 2 ? w[6] : w[7]));
+                t = 0.5 * ((E.sign < 0.0 ? -diff : diff) - E.ol * dqk);
             }
-            if (ok) {
-                double f2[4];
-                normalflux_prims(rho, w[0], w[1], w[2], w[3], X.nx, X.ny, X.ds, f2);
-#pragma unroll
-                for (int iv = 0; iv < 4; ++iv) t4[iv] = 0.5 * (X.sign * (f2[iv] - X.f1[iv]) - X.ol * w[4 + iv]);
-            }
+            if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
+            const int nr = min(8, ntake - base);
+            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
         }
+        // next item's inputs (independent of the sweep), issued once this
+        // item's polls are done so they do not queue ahead of them
+        if (kk + 1 < kend) sweep_load(v, Sn, lane, Xn);
         double r = X.r;
+        bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
             if ((it << 1) == last) {
                 r = pick4(lane, L0, L1, L2, L3);
             } else {
-                double dq[4];
-                ok = ok && poll_record<2>(v.rec_b + it, dq, v.err);
-                r = pick4(lane, dq[0], dq[1], dq[2], dq[3]);
+                ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
             }
         }
-        if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
-#pragma unroll
-        for (int iv = 0; iv < 4; ++iv) sterm[wib][lane][iv] = t4[iv];
-        __syncwarp();
-        double d = 0.0, q = 0.0;
-        if (lane < 4) {
-            double cres = 0.0;
-            for (int j = 0; j < ntake; ++j) cres = cres + sterm[wib][j][lane];
-            d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
-            q = X.o + d;
-        }
-        __syncwarp();
-        const double q0 = __shfl_sync(full, q, 0), q1 = __shfl_sync(full, q, 1), q2 = __shfl_sync(full, q, 2),
-                     q3 = __shfl_sync(full, q, 3);
+        if (__ballot_sync(full, !ok)) return;
+        // dqc and qc = qold + dqc (lusgs.f90:78-81 / 117-120), component k in lane k
+        const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
+        const double q = X.o + d;
+        // con2prim (pri.f90): rho = q1, then E/rho, rhou/rho, rhov/rho in lanes 0, 2, 3
+        const double rho = __shfl_sync(full, q, 1);
+        const double quo = q / rho;
+        const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
+        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        const double qq = u * u + vv * vv;
+        const double p = gm1 * (E0 - 0.5 * rho * qq);
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
         L3 = __shfl_sync(full, d, 3);
-        Prim P = con2prim(v.g, q0, q1, q2, q3);
-        Lrho = P.rho; Lu = P.u; Lv = P.v; Lp = P.p; Le = P.e * P.rho;
+        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
         last = (it << 1) | pass;
-        const size_t slot = (size_t)pass * n + it;
+        const size_t slotr = (size_t)pass * n + it;
         if (lane == 0) {
-            double2* a = reinterpret_cast<double2*>(v.rec_a + slot);
+            double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
             st_relaxed2(a, Lu, Lv);
             st_relaxed2(a + 1, Lp, Le);
         } else if (lane == 1) {
-            double2* b = reinterpret_cast<double2*>(v.rec_b + slot);
+            double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
         } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(q0, q1, q2, q3);
+            v.qc[it] = make_double4(E0, rho, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
@@ -843,7 +868,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
             set_last_error("uns_nc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
-        h->coop_blocks = nsm * std::min(per, 4);
+        h->coop_blocks = nsm * std::min(per, kSweepBlocksPerSM);
         // other end of each v2f edge, and the reference's orientation sign
         auto other = [&](int i, int e, int* sign) {
             if (m->fp2[e] == i) { *sign = -1; return m->fp1[e]; }

@@ -21,6 +21,7 @@
 // always proceed: the sweep cannot deadlock.
 #pragma once
 #include <algorithm>
+#include <cstdlib>
 #include <functional>
 #include <queue>
 #include <utility>
@@ -36,9 +37,10 @@ struct WarpSchedule {
 };
 
 // nbr_off / nbr: CSR neighbour lists of the n entities (any order, entries
-// outside [0, n) ignored).  nwarps: warps of the cooperative launch.
-inline WarpSchedule list_schedule(int n, const int* nbr_off, const int* nbr, int nwarps) {
-    constexpr double kCompute = 1.0, kSync = 1.0;
+// outside [0, n) ignored).  nwarps: warps of the cooperative launch.  kSync:
+// the extra delay of a cross-warp dependency, in units of one item's compute.
+inline WarpSchedule list_schedule(int n, const int* nbr_off, const int* nbr, int nwarps, double kSync = 0.25) {
+    constexpr double kCompute = 1.0;
     // Topological orders: forward by dependency level (then index), backward
     // by backward level (then descending index).
     std::vector<int> lev(n, 0), levb(n, 0);
@@ -90,14 +92,18 @@ inline WarpSchedule list_schedule(int n, const int* nbr_off, const int* nbr, int
             for (int p : preds) s = std::max(s, fin[p] + (wof[p] == w ? 0.0 : kSync));
             return s;
         };
-        int crit = -1;
-        for (int p : preds)
-            if (crit < 0 || fin[p] > fin[crit]) crit = p;
-        int wa = -1;
+        // candidate warps: those whose newest item is a predecessor (the
+        // chain continues there); ties go to the predecessor nearest in
+        // index, so chains follow the mesh numbering where they can
+        const int self = code >> 1;
+        int wa = -1, da = 0;
         double sa = 0.0;
-        if (crit >= 0 && wlast[wof[crit]] == crit) {
-            wa = wof[crit];
-            sa = start_on(wa);
+        for (int p : preds) {
+            int w = wof[p];
+            if (wlast[w] != p) continue;
+            double s = start_on(w);
+            int dist = std::abs((p >> 1) - self);
+            if (wa < 0 || s < sa || (s == sa && dist < da)) { wa = w; sa = s; da = dist; }
         }
         while (heap.top().first != wfree[heap.top().second]) heap.pop();  // drop stale entries
         int wb = heap.top().second;
