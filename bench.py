@@ -61,7 +61,7 @@ WORKLOADS = {
 }
 
 # Kernels launched per iteration (our own; memsets excluded).
-LAUNCHES = {("nc", "lusgs"): 7, ("nc", "rk3"): 11, ("cc", "rk3"): 12, ("cc", "lusgs"): 10}
+LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 12, ("cc", "lusgs"): 12}
 
 
 def peaks():
@@ -84,8 +84,13 @@ def algorithmic_bytes(kind: str, m: dict) -> dict:
             "grad_lim": 192 * N + 56 * E,
             "edge": 144 * N + 80 * E + 80 * B,
             "node_res": 60 * N + 56 * E + 80 * B,
-            "fold": 32 * N + 96 * E,
-            "lusgs_sweeps": 228 * N + 112 * E,
+            # per taken edge record R (2 per interior edge): 12 B of indices,
+            # normal 16, length 8, la 8, qold 32 read; 96 B written
+            "sweep_prep": 172 * 2 * E,
+            # per node: two items (schedule 16, diag 8, qold 32), res 32,
+            # records written 2 x 64, qc 32; per record: 96 B read plus the
+            # neighbour's 64 B record polled
+            "lusgs_sweeps": 304 * N + 160 * 2 * E,
             "residue": 16 * ((N + 255) // 256),
         }
     N, F, P = m["noc"], m["nfi"] + m["nbf"], m["nop"]
@@ -100,6 +105,24 @@ def algorithmic_bytes(kind: str, m: dict) -> dict:
         "cell_res": 16 * N + 32 * F + 32 * N * 4 + 16 * N,
         "residue": 8 * ((N + 255) // 256),
     }
+
+
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
+# the dominant kernels, per unit of the workload, from one ncu capture each of
+# a quarter-size case (reads grow in proportion to the units; see the
+# summaries under profiles/): scaled here to the benchmark's size.
+TRAFFIC_PER_UNIT = {
+    ("nc", "lusgs_sweeps"): (103.81e6 / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
+    ("cc", "face_conv"): (57.09e6 / 393728, "faces", "profiles/cc_face_conv_512x256_full.md"),
+}
+
+
+def launches_per_iter(kind: str, rk3: bool, laminar: bool) -> dict:
+    """How many launches of each profiled phase one iteration makes."""
+    n = 3 if rk3 else 1
+    if kind == "nc":
+        return {"grad_lim": n, "edge": n, "node_res": n}
+    return {"face_conv": n, "cell_res": n, "viscous": n if laminar else 0, "cirs": n}
 
 
 # ---------------------------------------------------------------- clocks
@@ -261,11 +284,19 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     nbytes = algorithmic_bytes(kind, m.arrays)
     peak, peak_src = peaks()
     dom = max(prof, key=prof.get)
+    nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"])
+    per_launch = {k: v / max(nl.get(k, 1), 1) for k, v in prof.items()}  # ms per launch
     rl_kernel = max((k for k in nbytes if k in prof and prof[k] > 0), key=lambda k: prof[k])
-    achieved = nbytes[rl_kernel] / (prof[rl_kernel] * 1e-3) / 1e9
-    kernels = {k: {"ms": round(v, 5), "alg_MB": round(nbytes.get(k, 0) / 1e6, 2),
-                   "GBps": round(nbytes[k] / (v * 1e-3) / 1e9, 1) if k in nbytes and v > 0 else None}
+    achieved = nbytes[rl_kernel] / (per_launch[rl_kernel] * 1e-3) / 1e9
+    kernels = {k: {"ms_per_iter": round(v, 5), "launches_per_iter": nl.get(k, 1),
+                   "alg_MB_per_launch": round(nbytes.get(k, 0) / 1e6, 2),
+                   "GBps": round(nbytes[k] / (per_launch[k] * 1e-3) / 1e9, 1) if k in nbytes and v > 0 else None}
                for k, v in prof.items()}
+    tr = TRAFFIC_PER_UNIT.get((kind, rl_kernel))
+    traffic = None
+    if tr is not None:
+        nunits = m["nop"] if tr[1] == "nodes" else (m["nfi"] + m["nbf"] if tr[1] == "faces" else m["noc"])
+        traffic = round(tr[0] * nunits)
 
     clocks = clk.summary()
     if rank != 0:
@@ -285,7 +316,10 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
         "gpu_launches": LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")] * args.steps,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": None,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": (f"ncu dram bytes per {tr[1][:-1]} x {tr[1]} ({tr[2]})" if tr else None),
+                     "duration_ms": round(per_launch[rl_kernel], 4),
+                     "timing": "CUDA events on the library stream around each phase, 3 iterations after the timed region",
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else "fallback",
                      "dominant_phase": dom},
         "kernels": kernels,

@@ -114,6 +114,14 @@ int uns_nc_residue(uns_nc_handle* h, double* fres_raw, double* fresi, int* iresi
 int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
                    double* fresi, int* done_iters);
 
+/* ========================================================= precision ====*/
+/* Switches the arithmetic form (UNS_PREC_*) between calls; waits for the
+ * handle's stream, and the next uns_*_iterate captures a new graph.  No
+ * reference counterpart: it lets a caller run the FP32-flux form while it
+ * converges and finish in FP64 below the FP32 residual floor. */
+int uns_cc_set_precision(uns_cc_handle* h, int precision);
+int uns_nc_set_precision(uns_nc_handle* h, int precision);
+
 /* ============================================================ timing ====*/
 /* The cudaStream_t a handle queues its work on, so a caller can bracket
  * calls with its own CUDA events (no reference counterpart: measurement). */

@@ -46,9 +46,14 @@ enum { UNS_CFL_TANH = 0, UNS_CFL_RAMP = 1 };
  * side, and the solve then diverges; UNS_LIM_BARTH_CORRECTED uses -1/2 there,
  * as limiter_VKN does (limiter.f90:71). */
 enum { UNS_LIM_VKN = 0, UNS_LIM_BARTH = 1, UNS_LIM_BARTH_CORRECTED = 2 };
-/* Arithmetic of the face reconstruction + convective flux.  FP64 everywhere,
- * or FP32 face arithmetic with FP64 accumulation / norm / dt / LU-SGS. */
-enum { UNS_PREC_FP64 = 0, UNS_PREC_MIXED = 1 };
+/* Arithmetic form.  UNS_PREC_FP64: FP64 everywhere (the reference's).
+ * UNS_PREC_MIXED: FP32 face reconstruction and flux arithmetic, in the
+ * residual and in the LU-SGS sweeps; FP64 residual accumulation, norm, dt and
+ * LU-SGS diagonal inversion.  Its residual floors near a 1e-5 drop (FP32
+ * rounding of the near-cancelling fluxes).  UNS_PREC_MIXED_SWEEP: FP64
+ * residual, FP32 flux arithmetic only inside the LU-SGS sweeps (the implicit
+ * operator), so the solve converges as far as the FP64 one. */
+enum { UNS_PREC_FP64 = 0, UNS_PREC_MIXED = 1, UNS_PREC_MIXED_SWEEP = 2 };
 
 /* Field identifiers for the state accessors (uns_cc_get_field,
  * uns_nc_get_field).  Layouts are row-major with the variable index fastest,

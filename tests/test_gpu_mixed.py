@@ -1,0 +1,100 @@
+"""Mixed-precision form: FP32 face reconstruction and flux arithmetic (residual
+and LU-SGS sweeps), FP64 residual accumulation, residual norm, timestep and
+LU-SGS diagonal inversion.
+
+It is not bit-compatible with the reference by design; it is checked against
+the FP64 path (itself bit-compatible with the oracle): the residual history
+tracks the FP64 one, and converged to a 1e-8 density-residual drop the
+solution and the wall forces agree to the tolerances below.
+"""
+import numpy as np
+import pytest
+
+from unsflow2d_gb300 import abi, mesh
+from unsflow2d_gb300.solver import CCSolver, NCSolver, converge
+
+pytestmark = pytest.mark.gpu
+
+
+def _coefficients(fx, fy, p):
+    """Lift / drag coefficients of the wall force (unit chord, rho=1, |V|=1)."""
+    a = np.deg2rad(p.aoa_deg)
+    q = 0.5
+    return (fy * np.cos(a) - fx * np.sin(a)) / q, (fx * np.cos(a) + fy * np.sin(a)) / q
+
+
+@pytest.mark.parametrize("case", [
+    dict(flux="roe", grad="gg", m_inf=0.5, aoa_deg=2.0),
+    dict(flux="vanleer", grad="lsqr", m_inf=0.5, aoa_deg=2.0),
+    dict(flux="roe", grad="gg", time="lusgs", cfl_type="ramp", cfl_min=0.5, cfl_max=5.0, cfl_ramp_steps=10),
+], ids=["roe_rk3", "vanleer_rk3", "roe_lusgs"])
+def test_cc_mixed_tracks_fp64(case):
+    m = mesh.CCMesh.airfoil(32, 16)
+    p64 = abi.make_params(**case)
+    p32 = abi.make_params(precision="mixed", **case)
+    cfl = mesh.cfl_schedule(p64, 1, 100, "cc")
+    a, b = CCSolver(m, p64), CCSolver(m, p32)
+    fa, fb = a.iterate(cfl, first_iter=True), b.iterate(cfl, first_iter=True)
+    assert len(fa) == len(fb) == 100 and np.isfinite(fb).all()
+    assert np.max(np.abs(np.log10(fb / fb[0]) - np.log10(fa / fa[0]))) < 1e-2
+    qa, qb = a.get_state(), b.get_state()
+    assert np.max(np.abs(qb - qa)) <= 1e-4 * np.max(np.abs(qa))
+
+
+@pytest.mark.parametrize("case", [
+    dict(flux="vanleer", limiter="vkn", time="rk3", cfl_max=0.9, m_inf=0.6, aoa_deg=2.89),
+    dict(flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0, m_inf=0.8, aoa_deg=1.25),
+], ids=["rk3", "lusgs"])
+def test_nc_mixed_tracks_fp64(case):
+    m = mesh.NCMesh.airfoil(32, 16)
+    p64 = abi.make_params(**case)
+    p32 = abi.make_params(precision="mixed", **case)
+    cfl = mesh.cfl_schedule(p64, 1, 60, "nc")
+    a, b = NCSolver(m, p64), NCSolver(m, p32)
+    fa, _ = a.iterate(cfl, first_iter=True)
+    fb, _ = b.iterate(cfl, first_iter=True)
+    assert len(fa) == len(fb) == 60 and np.isfinite(fb).all()
+    assert np.max(np.abs(np.log10(fb / fb[0]) - np.log10(fa / fa[0]))) < 1e-2
+    qa, qb = a.get_state(), b.get_state()
+    # transonic start-up with limiter switching: FP32 flux rounding shifts
+    # the transient by ~1e-4 of the state scale
+    assert np.max(np.abs(qb - qa)) <= 1e-3 * np.max(np.abs(qa))
+
+
+def test_cc_mixed_converged_forces():
+    """FP64 and the mixed form with its precision ramp (FP32 fluxes until the
+    residual has dropped 1e-4 or stalls, FP64 after) both reach a 1e-8
+    density-residual drop; C_L and C_D agree to 1e-6."""
+    m = mesh.CCMesh.airfoil(32, 16)
+    case = dict(flux="roe", grad="gg", time="lusgs", cfl_type="ramp", cfl_min=0.5, cfl_max=5.0,
+                cfl_ramp_steps=10, m_inf=0.5, aoa_deg=2.0, min_res=1e-8)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        p = abi.make_params(precision=prec, **case)
+        s = CCSolver(m, p)
+        r = converge(s, 1e-8, 30000, switch_drop=1e-4 if prec == "mixed" else None)
+        assert r["history"][-1] < 1e-8, (prec, r["iterations"], r["history"][-1])
+        out[prec] = (_coefficients(*s.forces(), p), r)
+    (cl64, cd64), r64 = out["fp64"]
+    (cl32, cd32), r32 = out["mixed"]
+    print(f"C_L fp64 {cl64:.10f} mixed {cl32:.10f} | C_D fp64 {cd64:.10f} mixed {cd32:.10f} | "
+          f"iterations {r64['iterations']} {r32['iterations']} (FP64 from {r32['switched_at']})")
+    assert r32["switched_at"] is not None
+    assert abs(cl32 - cl64) < 1e-6 and abs(cd32 - cd64) < 1e-6
+
+
+def test_nc_mixed_sweep_converges_like_fp64():
+    """FP32 arithmetic only inside the LU-SGS sweeps: the FP64 residual keeps
+    the full convergence; the converged states agree."""
+    m = mesh.NCMesh.airfoil(32, 16)
+    case = dict(flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0, m_inf=0.8, aoa_deg=1.25,
+                min_res=1e-8)
+    res = {}
+    for prec in ("fp64", "mixed_sweep"):
+        s = NCSolver(m, abi.make_params(precision=prec, **case))
+        r = converge(s, 1e-8, 20000)
+        assert r["history"][-1] < 1e-8, (prec, r["iterations"], r["history"][-1])
+        res[prec] = (s.get_state(), r["iterations"])
+    print("iterations", res["fp64"][1], res["mixed_sweep"][1])
+    qa, qb = res["fp64"][0], res["mixed_sweep"][0]
+    assert np.max(np.abs(qb - qa)) <= 1e-6 * np.max(np.abs(qa))

@@ -27,7 +27,7 @@ GRAD = {"gg": 0, "ggfc": 1, "lsqr": 2}
 TIME = {"rk3": 0, "lusgs": 1}
 CFLT = {"tanh": 0, "ramp": 1}
 LIMITER = {"vkn": 0, "barth": 1, "barth_corrected": 2}
-PREC = {"fp64": 0, "mixed": 1}
+PREC = {"fp64": 0, "mixed": 1, "mixed_sweep": 2}
 
 CC_FIELDS = {"qc": 0, "qp": 1, "qold": 2, "res": 3, "grad": 4, "phi": 5, "dt": 6, "la": 7,
              "ptprim": 8, "fqp": 9, "fla": 10, "fmu": 11, "fgrad": 12, "mul": 13}
@@ -208,6 +208,7 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
             "uns_nc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
             "uns_residue_rms_noalloc": ([vp, i32, dp, vp], i32),
+            "uns_cc_set_precision": ([vp, i32], i32), "uns_nc_set_precision": ([vp, i32], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)

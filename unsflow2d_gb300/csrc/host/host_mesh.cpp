@@ -860,6 +860,7 @@ int read_flo_inp_cc(const std::string& path, uns_params& p, std::string& grid, s
         if (p.time_mode == UNS_TIME_RK3 && !(p.cfl_max < 1.0)) { err = "CFL should be less than 1 for rk3"; return UNS_ERR_ARG; }
         p.precision = UNS_PREC_FP64;
         if (L[15].size() >= 3 && L[15][2] == "mixed") p.precision = UNS_PREC_MIXED;
+        if (L[15].size() >= 3 && L[15][2] == "mixed_sweep") p.precision = UNS_PREC_MIXED_SWEEP;
     } catch (...) {
         err = "flo.inp: unparsable value";
         return UNS_ERR_IO;
@@ -913,6 +914,7 @@ int read_flo_inp_nc(const std::string& path, uns_params& p, std::string& grid, s
         p.flux_type = (flux == "ausm") ? UNS_FLUX_AUSM : UNS_FLUX_VANLEER;
         p.limiter_type = (L[15].size() >= 3 && L[15][2] == "barth") ? UNS_LIM_BARTH : UNS_LIM_VKN;
         if (L[15].size() >= 4 && L[15][3] == "mixed") p.precision = UNS_PREC_MIXED;
+        if (L[15].size() >= 4 && L[15][3] == "mixed_sweep") p.precision = UNS_PREC_MIXED_SWEEP;
         if (p.ilimit != 0 && p.ilimit != 1) { err = "Unknown limiter option"; return UNS_ERR_ARG; }
         if (vortex != 0 && vortex != 1) { err = "Unknown vortex option"; return UNS_ERR_ARG; }
         if (p.time_mode == UNS_TIME_RK3 && !(p.cfl_max < 1.0)) { err = "CFL should be less than 1 for rk3"; return UNS_ERR_ARG; }

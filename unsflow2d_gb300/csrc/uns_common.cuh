@@ -111,6 +111,38 @@ __device__ __forceinline__ bool poll_value(const double* p, double& out, DevErr*
     }
 }
 
+// FP32 records (mixed precision) use a signalling-NaN float pattern the same way.
+constexpr unsigned kUnsetF = 0x7FA0DEADu;
+__device__ __forceinline__ bool is_unset(float x) { return (unsigned)__float_as_int(x) == kUnsetF; }
+
+// A mixed-precision record: float4 (u, v, p, e*rho) and double4 dq, all
+// three loads in flight together.
+__device__ __forceinline__ bool poll_record_fd(const float4* a, const double4* b, float w[4], double dq[4],
+                                               DevErr* err) {
+    const double2* pb = reinterpret_cast<const double2*>(b);
+    long long t0 = 0;
+    for (int spins = 0;; ++spins) {
+        asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "l"(a) : "memory");
+        double2 x0 = ld_relaxed2(pb), x1 = ld_relaxed2(pb + 1);
+        dq[0] = x0.x; dq[1] = x0.y; dq[2] = x1.x; dq[3] = x1.y;
+        bool ready = !is_unset(w[0]) && !is_unset(w[1]) && !is_unset(w[2]) && !is_unset(w[3]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) ready = ready && !is_unset(dq[j]);
+        if (ready) return true;
+        if (!poll_continue(spins, t0, err)) return false;
+    }
+}
+__device__ __forceinline__ void st_relaxed4f(float4* p, float a, float b, float c, float d) {
+    asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" : : "l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
+                 : "memory");
+}
+static __global__ void __launch_bounds__(kBlock) k_fill_unset_f(float4* p, long long n4) {
+    const float u = __int_as_float((int)kUnsetF);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x)
+        p[i] = make_float4(u, u, u, u);
+}
+
 // Fills n doubles with kUnset (re-arms the records before a sweep).
 static __global__ void __launch_bounds__(kBlock) k_fill_unset(double2* p, long long n2) {
     const double u = __longlong_as_double((long long)kUnset);

@@ -455,10 +455,13 @@ constexpr double kOmega = 1.5;  // lusgs.f90:28
 
 // Per LU-SGS call: everything a sweep item needs from an edge that does not
 // change during the sweeps, laid out contiguously in schedule order so a
-// lane fetches it with three 32-byte loads and no index chasing:
+// lane fetches it with three vector loads and no index chasing:
 //   rec[3r]   normalflux(qold(nb)) on the edge (lusgs.f90:137-155)
 //   rec[3r+1] (nx, ny, ds, omega * la)
 //   rec[3r+2] (qold(nb).rho, sign, nb as integer bits, 0)
+// R = double: the reference arithmetic.  R = float (mixed precision): the
+// flux arithmetic in FP32, records of float4.
+template <class R>
 __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     if (stopped(v)) return;
     int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -467,11 +470,24 @@ __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     const double2 n = v.fn[c];
     const double ds = v.farea[c];
     const double4 q = v.qold[nb];
-    double o[4];
-    normalflux_nc(v.g, q, n.x, n.y, ds, o);
-    v.rec[3 * (size_t)r] = m4(o);
-    v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
-    v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
+    if constexpr (std::is_same<R, double>::value) {
+        double o[4];
+        normalflux_nc(v.g, q, n.x, n.y, ds, o);
+        v.rec[3 * (size_t)r] = m4(o);
+        v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
+        v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
+    } else {
+        const float rho = (float)q.y, E = (float)q.x;
+        const float u = (float)q.z / rho, vv = (float)q.w / rho;
+        const float p = (float)v.g.gamma1 * (E - 0.5f * rho * (u * u + vv * vv));
+        const float nx = (float)n.x, ny = (float)n.y, dsf = (float)ds;
+        const float un = u * nx + vv * ny;
+        const float o1 = rho * un;
+        float4* rf = reinterpret_cast<float4*>(v.rec);
+        rf[3 * (size_t)r] = make_float4((E + p) * un * dsf, o1 * dsf, (o1 * u + p * nx) * dsf, (o1 * vv + p * ny) * dsf);
+        rf[3 * (size_t)r + 1] = make_float4(nx, ny, dsf, (float)(kOmega * v.fla[c]));
+        rf[3 * (size_t)r + 2] = make_float4(rho, (float)v.rec_sign[r], __int_as_float(nb), 0.f);
+    }
 }
 
 // normalflux (lusgs.f90:137-155) from primitives a sweep has published.
@@ -496,22 +512,33 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
 // arithmetic is spread over the lanes: the four flux components of up to
 // eight edges in one pass, the per-variable sums and divides in lanes 0..3,
 // and the three divisions of con2prim in lanes 0, 2 and 3 at once.
+template <class R>
 struct SweepIn {
-    double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
+    R f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
     int nb;
     double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
 };
 
-__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
-    const double4* p = v.rec + 3 * (size_t)rec;
-    x.f1 = reinterpret_cast<const double*>(p)[k];
-    double4 b = p[1], c = p[2];
-    x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-    x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
+template <class R>
+__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn<R>& x) {
+    if constexpr (std::is_same<R, double>::value) {
+        const double4* p = v.rec + 3 * (size_t)rec;
+        x.f1 = reinterpret_cast<const double*>(p)[k];
+        double4 b = p[1], c = p[2];
+        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+        x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
+    } else {
+        const float4* p = reinterpret_cast<const float4*>(v.rec) + 3 * (size_t)rec;
+        x.f1 = reinterpret_cast<const float*>(p)[k];
+        float4 b = p[1], c = p[2];
+        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+        x.rho_old = c.x; x.sign = c.y; x.nb = __float_as_int(c.z);
+    }
 }
 
-__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
-    if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
+template <class R>
+__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn<R>& x) {
+    if ((lane >> 2) < S.w) sweep_load_edge<R>(v, S.z + (lane >> 2), lane & 3, x);
     if (lane < 4) {
         x.D = v.diag[S.x];
         x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
@@ -521,6 +548,46 @@ __device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int l
         x.o = 1.0;
         x.r = 0.0;
     }
+}
+
+// The (u, v, p, e*rho) half of a record: double4 (FP64) or float4 (mixed).
+template <class R>
+__device__ __forceinline__ bool poll_neighbour(const NCView& v, size_t rs, R w[4], double dq[4]) {
+    if constexpr (std::is_same<R, double>::value) {
+        double x[8];
+        bool ok = poll_record2(v.rec_a + rs, v.rec_b + rs, x, v.err);
+        w[0] = x[0]; w[1] = x[1]; w[2] = x[2]; w[3] = x[3];
+        dq[0] = x[4]; dq[1] = x[5]; dq[2] = x[6]; dq[3] = x[7];
+        return ok;
+    } else {
+        return poll_record_fd(reinterpret_cast<const float4*>(v.rec_a) + rs, v.rec_b + rs, w, dq, v.err);
+    }
+}
+
+// One unconditional read of a neighbour record, issued early; the values
+// are checked (record_set) only when the item that needs them starts.
+template <class R>
+__device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, R w[4], double dq[4]) {
+    const double2* pb = reinterpret_cast<const double2*>(v.rec_b + rs);
+    double2 x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
+    if constexpr (std::is_same<R, double>::value) {
+        const double2* pa = reinterpret_cast<const double2*>(v.rec_a + rs);
+        double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1);
+        w[0] = x0.x; w[1] = x0.y; w[2] = x1.x; w[3] = x1.y;
+    } else {
+        const float4* pa = reinterpret_cast<const float4*>(v.rec_a) + rs;
+        asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "l"(pa) : "memory");
+    }
+    dq[0] = x2.x; dq[1] = x2.y; dq[2] = x3.x; dq[3] = x3.y;
+}
+
+template <class R>
+__device__ __forceinline__ bool record_set(const R w[4], const double dq[4]) {
+    bool ready = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ready = ready && !is_unset(w[j]) && !is_unset(dq[j]);
+    return ready;
 }
 
 // lusgs sweeps (lusgs.f90:48-124) as one cooperative launch.  Each warp runs
@@ -533,7 +600,10 @@ __device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int l
 // component; lanes 0..3 add the terms in edge order (the reference's
 // summation order) and divide by the diagonal; the new state is spread to all
 // lanes, which keep its primitives for the next item while lanes 0 and 1
-// publish the record.  Every operation and operand order is the reference's.
+// publish the record.  R = double: every operation and operand order is the
+// reference's.  R = float (mixed precision): the flux arithmetic and the
+// primitives are FP32; the sums, the diagonal division and dqc stay FP64.
+template <class R>
 __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -541,48 +611,59 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
     const int slot = lane >> 2, k = lane & 3;
     if (stopped(v)) return;
     const int n = v.nop;
-    const double gm1 = v.g.gamma - 1.0;
+    const R gm1 = (R)(v.g.gamma - 1.0);
     const int kbeg = woff[gw], kend = woff[gw + 1];
     if (kbeg >= kend) return;
     const int4 none = make_int4(0, 0, 0, 0);
     int4 S = v.sched[kbeg];
     int4 Sn = kbeg + 1 < kend ? v.sched[kbeg + 1] : none;
-    SweepIn X = {}, Xn = {};
-    sweep_load(v, S, lane, X);
+    SweepIn<R> X = {}, Xn = {};
+    sweep_load<R>(v, S, lane, X);
     int last = -1;  // code of the warp's previous item; its values below, in every lane
-    double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    R Lrho = 0, Lu = 0, Lv = 0, Lp = 0, Le = 0;
+    double L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    // early look at the current item's first-round neighbour record, loaded
+    // during the previous item (usually already published)
+    R Sw[4] = {0, 0, 0, 0};
+    double Sdq[4] = {0.0, 0.0, 0.0, 0.0};
+    bool spec = false;
     for (int kk = kbeg; kk < kend; ++kk) {
         const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
         const int it = S.x, pass = S.y, ntake = S.w;
         double cres = 0.0;  // lanes 0..3: sum over edges of component k
         for (int base = 0; base < ntake; base += 8) {
-            SweepIn E = X;
-            if (base > 0 && base + slot < ntake) sweep_load_edge(v, S.z + base + slot, k, E);
+            SweepIn<R> E = X;
+            if (base > 0 && base + slot < ntake) sweep_load_edge<R>(v, S.z + base + slot, k, E);
             bool ok = true;
             double t = 0.0;
             if (base + slot < ntake) {
                 // the neighbour's values: registers when this warp computed it
                 // last, else its record
-                double w[8], rho;
+                R w[4], rho;
+                double dq[4];
                 if (((E.nb << 1) | pass) == last) {
-                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
+                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le;
+                    dq[0] = L0; dq[1] = L1; dq[2] = L2; dq[3] = L3;
                     rho = Lrho;
+                } else if (base == 0 && spec && record_set<R>(Sw, Sdq)) {
+                    w[0] = Sw[0]; w[1] = Sw[1]; w[2] = Sw[2]; w[3] = Sw[3];
+                    dq[0] = Sdq[0]; dq[1] = Sdq[1]; dq[2] = Sdq[2]; dq[3] = Sdq[3];
+                    rho = E.rho_old + (R)dq[1];
                 } else {
-                    const size_t rs = (size_t)pass * n + E.nb;
-                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
-                    rho = E.rho_old + w[5];
+                    ok = poll_neighbour<R>(v, (size_t)pass * n + E.nb, w, dq);
+                    rho = E.rho_old + (R)dq[1];
                 }
                 // normalflux (lusgs.f90:144-150) component k, then the edge term
-                const double u = w[0], vv = w[1], p = w[2], et = w[3];
-                const double un = u * E.nx + vv * E.ny;
-                const double o1 = rho * un;
-                const double prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
-                const double pn = p * (k == 2 ? E.nx : E.ny);
-                double o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
+                const R u = w[0], vv = w[1], p = w[2], et = w[3];
+                const R un = u * E.nx + vv * E.ny;
+                const R o1 = rho * un;
+                const R prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
+                const R pn = p * (k == 2 ? E.nx : E.ny);
+                R o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
                 o = o * E.ds;
-                const double diff = o - E.f1;
-                const double dqk = k == 0 ? w[4] : (k == 1 ? w[5] : (k == 2 ? w[6] : w[7]));
-                t = 0.5 * ((E.sign < 0.0 ? -diff : diff) - E.ol * dqk);
+                const R diff = o - E.f1;
+                const R dqk = (R)(k == 0 ? dq[0] : (k == 1 ? dq[1] : (k == 2 ? dq[2] : dq[3])));
+                t = (double)(R(0.5) * ((E.sign < R(0) ? -diff : diff) - E.ol * dqk));
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
             const int nr = min(8, ntake - base);
@@ -590,7 +671,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         }
         // next item's inputs (independent of the sweep), issued once this
         // item's polls are done so they do not queue ahead of them
-        if (kk + 1 < kend) sweep_load(v, Sn, lane, Xn);
+        if (kk + 1 < kend) sweep_load<R>(v, Sn, lane, Xn);
         double r = X.r;
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
@@ -604,13 +685,18 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         // dqc and qc = qold + dqc (lusgs.f90:78-81 / 117-120), component k in lane k
         const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
         const double q = X.o + d;
+        // the next item's first-round neighbour records, while this item finishes
+        spec = false;
+        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass))
+            peek_neighbour<R>(v, (size_t)Sn.y * n + Xn.nb, Sw, Sdq), spec = true;
         // con2prim (pri.f90): rho = q1, then E/rho, rhou/rho, rhov/rho in lanes 0, 2, 3
-        const double rho = __shfl_sync(full, q, 1);
-        const double quo = q / rho;
+        const double rhod = __shfl_sync(full, q, 1);
+        const R rho = (R)rhod;
+        const R quo = (R)q / rho;
         const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
-        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
-        const double qq = u * u + vv * vv;
-        const double p = gm1 * (E0 - 0.5 * rho * qq);
+        const R e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        const R qq = u * u + vv * vv;
+        const R p = gm1 * ((R)E0 - R(0.5) * rho * qq);
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
@@ -619,15 +705,19 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
         if (lane == 0) {
-            double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
-            st_relaxed2(a, Lu, Lv);
-            st_relaxed2(a + 1, Lp, Le);
+            if constexpr (std::is_same<R, double>::value) {
+                double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
+                st_relaxed2(a, Lu, Lv);
+                st_relaxed2(a + 1, Lp, Le);
+            } else {
+                st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, Lu, Lv, Lp, Le);
+            }
         } else if (lane == 1) {
             double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
         } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(E0, rho, Q2, Q3);
+            v.qc[it] = make_double4(E0, rhod, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
@@ -717,8 +807,13 @@ int enqueue_fvres_nc(uns_nc_handle* h, NCView& v, double cfl, int irk, int parti
 }
 
 int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
+    const bool mixed = h->P.precision != UNS_PREC_FP64;  // FP32 sweep arithmetic
     const long long n2 = 2LL * v.nop * 2;  // double2 per record array
-    k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_a, n2);
+    if (mixed)
+        k_fill_unset_f<<<std::min<long long>(nblocks(2LL * v.nop), 4096), kBlock, 0, h->stream>>>((float4*)v.rec_a,
+                                                                                                   2LL * v.nop);
+    else
+        k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_a, n2);
     k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_b, n2);
     UNS_CUDA(cudaGetLastError());
     cudaLaunchConfig_t cfg = {};
@@ -730,12 +825,21 @@ int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->woff));
+    if (mixed) UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs<float>, v, (const int*)h->woff));
+    else UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs<double>, v, (const int*)h->woff));
+    return UNS_OK;
+}
+
+int enqueue_sweep_prep_nc(uns_nc_handle* h, NCView& v) {
+    if (v.nrec <= 0) return UNS_OK;
+    if (h->P.precision != UNS_PREC_FP64) NLAUNCH(k_nc_sweep_prep<float>, v.nrec, v);
+    else NLAUNCH(k_nc_sweep_prep<double>, v.nrec, v);
     return UNS_OK;
 }
 
 int enqueue_lusgs_nc(uns_nc_handle* h, NCView& v) {
-    if (v.nrec > 0) NLAUNCH(k_nc_sweep_prep, v.nrec, v);
+    int rc = enqueue_sweep_prep_nc(h, v);
+    if (rc) return rc;
     return launch_sweeps_nc(h, v);
 }
 
@@ -762,6 +866,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     if (!m || !p || !out) { set_last_error("uns_nc_create: null argument"); return UNS_ERR_ARG; }
     *out = nullptr;
     if (m->nop <= 0 || m->nof <= 0 || !(p->m_inf > 0.0) || p->time_mode < 0 || p->time_mode > 1 ||
+        p->precision < UNS_PREC_FP64 || p->precision > UNS_PREC_MIXED_SWEEP ||
         (p->flux_type != UNS_FLUX_VANLEER && p->flux_type != UNS_FLUX_AUSM) ||
         (p->limiter_type < UNS_LIM_VKN || p->limiter_type > UNS_LIM_BARTH_CORRECTED)) {
         set_last_error("uns_nc_create: bad sizes or parameters");
@@ -864,7 +969,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
         if (nop >= (1 << 30)) { set_last_error("uns_nc_create: too many nodes"); return fail(UNS_ERR_MESH); }
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs, kSweepBlock, 0) != cudaSuccess || per < 1) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs<double>, kSweepBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_nc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
@@ -1067,6 +1172,16 @@ int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_ite
     return check_err_nc(h);
 }
 
+int uns_nc_set_precision(uns_nc_handle* h, int precision) {
+    if (!h || precision < UNS_PREC_FP64 || precision > UNS_PREC_MIXED_SWEEP) return UNS_ERR_ARG;
+    if (h->P.precision != precision) {
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+        h->P.precision = precision;
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    }
+    return UNS_OK;
+}
+
 void* uns_nc_stream(uns_nc_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
@@ -1103,7 +1218,7 @@ int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const cha
             if (!rc) rc = timed(3, [&]() -> int { NLAUNCH(k_nc_node_res, v.nop, v, cfl, rk3 ? irk : 0, rk3 ? (irk == 3) : 1); return UNS_OK; });
         }
         if (!rk3) {
-            if (!rc) rc = timed(4, [&]() -> int { if (v.nrec > 0) NLAUNCH(k_nc_sweep_prep, v.nrec, v); return UNS_OK; });
+            if (!rc) rc = timed(4, [&]() -> int { return enqueue_sweep_prep_nc(h, v); });
             if (!rc) rc = timed(5, [&]() -> int { return launch_sweeps_nc(h, v); });
         }
         if (!rc) rc = timed(6, [&]() -> int {

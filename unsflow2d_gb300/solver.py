@@ -52,6 +52,10 @@ class _Solver:
         assert a.size == self.nstate * 4
         self._call("set_state", _dp(a))
 
+    def set_precision(self, precision: str) -> None:
+        """Switch between "fp64", "mixed" and "mixed_sweep" between calls."""
+        self._call("set_precision", abi.PREC[precision])
+
     def get_state(self) -> np.ndarray:
         out = np.zeros((self.nstate, 4))
         self._call("get_state", _dp(out))
@@ -206,3 +210,46 @@ class NCSolver(_Solver):
         done = C.c_int()
         self._call("iterate", len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), _dp(outi), C.byref(done))
         return out[:done.value], outi[:done.value]
+
+
+def converge(solver, target: float, max_iter: int, switch_drop: float | None = None, chunk: int = 500,
+             on_chunk=None) -> dict:
+    """Run the main loop from iteration 1 until the density residual has dropped
+    by `target` (the device stops at params.min_res) or `max_iter` iterations.
+
+    With `switch_drop`, the solver's current form (e.g. "mixed", FP32 fluxes)
+    runs until the residual has dropped by `switch_drop` or stops falling
+    (the FP32 rounding floor), and the rest runs in FP64 -- the precision
+    ramp that lets the FP32-flux form reach drops below its floor.  Returns
+    the residual history (normalised by iteration 1), the iteration of the
+    switch (or None) and the number of iterations run."""
+    from . import mesh as _mesh
+    kind = solver.kind
+    p = solver.params
+    hist: list[float] = []
+    norm = None
+    prev_cfl = 0.0
+    switched = None
+    it = 1
+    best_prev = np.inf
+    while it <= max_iter:
+        n = min(chunk, max_iter - it + 1)
+        cfl = _mesh.cfl_schedule(p, it, n, kind, prev_cfl)
+        prev_cfl = float(cfl[-1])
+        r = solver.iterate(cfl, first_iter=(it == 1))
+        f = r if kind == "cc" else r[0]
+        if norm is None and len(f):
+            norm = f[0]
+        hist.extend((f / norm).tolist())
+        it += len(f)
+        if on_chunk is not None:
+            on_chunk(it - 1, hist)
+        if len(f) < n or (hist and hist[-1] <= target):
+            break
+        if switch_drop is not None and switched is None:
+            best = min(hist[-len(f):])
+            if best <= switch_drop or (best < 100 * switch_drop and best > 0.9 * best_prev):
+                solver.set_precision("fp64")
+                switched = it
+            best_prev = best
+    return {"history": np.array(hist), "switched_at": switched, "iterations": it - 1}
