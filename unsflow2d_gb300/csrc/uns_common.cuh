@@ -115,24 +115,48 @@ __device__ __forceinline__ bool poll_value(const double* p, double& out, DevErr*
 constexpr unsigned kUnsetF = 0x7FA0DEADu;
 __device__ __forceinline__ bool is_unset(float x) { return (unsigned)__float_as_int(x) == kUnsetF; }
 
-// A mixed-precision record: float4 (u, v, p, e*rho) and double4 dq, all
-// three loads in flight together.
-__device__ __forceinline__ bool poll_record_fd(const float4* a, const double4* b, float w[4], double dq[4],
-                                               DevErr* err) {
-    const double2* pb = reinterpret_cast<const double2*>(b);
+// Reads a float4 record without waiting (an early look or one poll try).
+__device__ __forceinline__ void peek_f4(const float4* a, float w[4]) {
+    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "l"(a) : "memory");
+}
+
+__device__ __forceinline__ bool set_f4(const float w[4]) {
+    return !is_unset(w[0]) && !is_unset(w[1]) && !is_unset(w[2]) && !is_unset(w[3]);
+}
+
+// A float4 record, waiting (bounded) until none of its values is kUnsetF.
+__device__ __forceinline__ bool poll_f4(const float4* a, float w[4], DevErr* err) {
     long long t0 = 0;
     for (int spins = 0;; ++spins) {
-        asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
-                     : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "l"(a) : "memory");
-        double2 x0 = ld_relaxed2(pb), x1 = ld_relaxed2(pb + 1);
-        dq[0] = x0.x; dq[1] = x0.y; dq[2] = x1.x; dq[3] = x1.y;
-        bool ready = !is_unset(w[0]) && !is_unset(w[1]) && !is_unset(w[2]) && !is_unset(w[3]);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) ready = ready && !is_unset(dq[j]);
-        if (ready) return true;
+        peek_f4(a, w);
+        if (set_f4(w)) return true;
         if (!poll_continue(spins, t0, err)) return false;
     }
 }
+
+// LU-SGS normal flux change F(q + dq) - F(q) along (nx, ny), component k, in
+// FP32 and in delta form: from dq and q's state and primitives (fields rho,
+// ru, rv, E, u, v, p, un = u.n, nx, ny of `e`), never as the difference of
+// two O(1) fluxes, so its rounding error is relative to the change itself.
+// F = ((E + p) u.n, rho u.n, rho u.n u + p nx, rho u.n v + p ny).
+template <class Rec>
+__device__ __forceinline__ float dflux_k(const Rec& e, float gm1, const float dq[4], int k) {
+    const float dE = dq[0], dr = dq[1], dru = dq[2], drv = dq[3];
+    const float rn = e.rho + dr;
+    const float du = (dru - e.u * dr) / rn, dv = (drv - e.v * dr) / rn;
+    const float u2 = e.u + du, v2 = e.v + dv;
+    const float dp = gm1 * (dE - 0.5f * (dru * u2 + e.ru * du + drv * v2 + e.rv * dv));
+    const float dun = du * e.nx + dv * e.ny;
+    const float un2 = e.un + dun;
+    const float df1 = dr * un2 + e.rho * dun;  // change of rho u.n
+    const float run = e.rho * e.un;
+    if (k == 0) return (dE + dp) * un2 + (e.E + e.p) * dun;
+    if (k == 1) return df1;
+    if (k == 2) return df1 * u2 + run * du + dp * e.nx;
+    return df1 * v2 + run * dv + dp * e.ny;
+}
+
 __device__ __forceinline__ void st_relaxed4f(float4* p, float a, float b, float c, float d) {
     asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" : : "l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
                  : "memory");

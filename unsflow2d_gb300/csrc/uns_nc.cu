@@ -71,7 +71,7 @@ struct NCView {
     const int* rec_nb;
     const int* rec_sign;
     int nrec;
-    double4* rec;    // per record, per LU-SGS call: 3 x double4, see k_nc_sweep_prep
+    double4* rec;    // per record, per LU-SGS call: 3 x double4 (k_nc_sweep_prep) or 4 x float4 (k_nc_sweep_prep_mixed)
     double* diag;    // LU-SGS diagonal cv/dt + 0.5*omega*la (lusgs.f90:36)
     double4* rec_a;  // sweep records [pass * nop + node]: (u, v, p, e*rho) of qc
     double4* rec_b;  //   and dqc; rho is rebuilt as qold.rho + dqc.rho
@@ -455,13 +455,10 @@ constexpr double kOmega = 1.5;  // lusgs.f90:28
 
 // Per LU-SGS call: everything a sweep item needs from an edge that does not
 // change during the sweeps, laid out contiguously in schedule order so a
-// lane fetches it with three vector loads and no index chasing:
+// lane fetches it with three 32-byte loads and no index chasing:
 //   rec[3r]   normalflux(qold(nb)) on the edge (lusgs.f90:137-155)
 //   rec[3r+1] (nx, ny, ds, omega * la)
 //   rec[3r+2] (qold(nb).rho, sign, nb as integer bits, 0)
-// R = double: the reference arithmetic.  R = float (mixed precision): the
-// flux arithmetic in FP32, records of float4.
-template <class R>
 __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     if (stopped(v)) return;
     int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -470,24 +467,30 @@ __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     const double2 n = v.fn[c];
     const double ds = v.farea[c];
     const double4 q = v.qold[nb];
-    if constexpr (std::is_same<R, double>::value) {
-        double o[4];
-        normalflux_nc(v.g, q, n.x, n.y, ds, o);
-        v.rec[3 * (size_t)r] = m4(o);
-        v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
-        v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
-    } else {
-        const float rho = (float)q.y, E = (float)q.x;
-        const float u = (float)q.z / rho, vv = (float)q.w / rho;
-        const float p = (float)v.g.gamma1 * (E - 0.5f * rho * (u * u + vv * vv));
-        const float nx = (float)n.x, ny = (float)n.y, dsf = (float)ds;
-        const float un = u * nx + vv * ny;
-        const float o1 = rho * un;
-        float4* rf = reinterpret_cast<float4*>(v.rec);
-        rf[3 * (size_t)r] = make_float4((E + p) * un * dsf, o1 * dsf, (o1 * u + p * nx) * dsf, (o1 * vv + p * ny) * dsf);
-        rf[3 * (size_t)r + 1] = make_float4(nx, ny, dsf, (float)(kOmega * v.fla[c]));
-        rf[3 * (size_t)r + 2] = make_float4(rho, (float)v.rec_sign[r], __int_as_float(nb), 0.f);
-    }
+    double o[4];
+    normalflux_nc(v.g, q, n.x, n.y, ds, o);
+    v.rec[3 * (size_t)r] = m4(o);
+    v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
+    v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
+}
+
+// Mixed-precision sweeps (delta form): per record, in FP32, the neighbour's
+// old state and primitives and the edge geometry, from which a lane forms
+// normalflux(qold + dqc) - normalflux(qold) directly from dqc:
+//   [rho, rho*u, rho*v, E] [u, v, p, u.n] [nx, ny, ds, omega*la] [sign, nb, 0, 0]
+__global__ void __launch_bounds__(kBlock) k_nc_sweep_prep_mixed(NCView v) {
+    if (stopped(v)) return;
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= v.nrec) return;
+    const int c = v.rec_edge[r], nb = v.rec_nb[r];
+    const double2 n = v.fn[c];
+    const double4 q = v.qold[nb];
+    Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
+    float4* rf = reinterpret_cast<float4*>(v.rec) + 4 * (size_t)r;
+    rf[0] = make_float4((float)q.y, (float)q.z, (float)q.w, (float)q.x);
+    rf[1] = make_float4((float)P.u, (float)P.v, (float)P.p, (float)(P.u * n.x + P.v * n.y));
+    rf[2] = make_float4((float)n.x, (float)n.y, (float)v.farea[c], (float)(kOmega * v.fla[c]));
+    rf[3] = make_float4((float)v.rec_sign[r], __int_as_float(nb), 0.f, 0.f);
 }
 
 // normalflux (lusgs.f90:137-155) from primitives a sweep has published.
@@ -512,78 +515,50 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
 // arithmetic is spread over the lanes: the four flux components of up to
 // eight edges in one pass, the per-variable sums and divides in lanes 0..3,
 // and the three divisions of con2prim in lanes 0, 2 and 3 at once.
-template <class R>
 struct SweepIn {
-    R f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
+    double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
     int nb;
     double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
 };
 
-template <class R>
-__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn<R>& x) {
-    if constexpr (std::is_same<R, double>::value) {
-        const double4* p = v.rec + 3 * (size_t)rec;
-        x.f1 = reinterpret_cast<const double*>(p)[k];
-        double4 b = p[1], c = p[2];
-        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-        x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
-    } else {
-        const float4* p = reinterpret_cast<const float4*>(v.rec) + 3 * (size_t)rec;
-        x.f1 = reinterpret_cast<const float*>(p)[k];
-        float4 b = p[1], c = p[2];
-        x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-        x.rho_old = c.x; x.sign = c.y; x.nb = __float_as_int(c.z);
-    }
+__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
+    const double4* p = v.rec + 3 * (size_t)rec;
+    x.f1 = reinterpret_cast<const double*>(p)[k];
+    double4 b = p[1], c = p[2];
+    x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+    x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
 }
 
-template <class R>
-__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn<R>& x) {
-    if ((lane >> 2) < S.w) sweep_load_edge<R>(v, S.z + (lane >> 2), lane & 3, x);
+// The node's own diagonal, qold and res (variable `lane`) in lanes 0..3;
+// benign operands elsewhere, so the warp-wide divides meet no 0 or inf.
+__device__ __forceinline__ void own_load(const NCView& v, const int4& S, int lane, double& D, double& o, double& r) {
     if (lane < 4) {
-        x.D = v.diag[S.x];
-        x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
-        if (S.y == 0) x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
-    } else {  // benign operands: the warp-wide divides must not meet 0 or inf
-        x.D = 1.0;
-        x.o = 1.0;
-        x.r = 0.0;
-    }
-}
-
-// The (u, v, p, e*rho) half of a record: double4 (FP64) or float4 (mixed).
-template <class R>
-__device__ __forceinline__ bool poll_neighbour(const NCView& v, size_t rs, R w[4], double dq[4]) {
-    if constexpr (std::is_same<R, double>::value) {
-        double x[8];
-        bool ok = poll_record2(v.rec_a + rs, v.rec_b + rs, x, v.err);
-        w[0] = x[0]; w[1] = x[1]; w[2] = x[2]; w[3] = x[3];
-        dq[0] = x[4]; dq[1] = x[5]; dq[2] = x[6]; dq[3] = x[7];
-        return ok;
+        D = v.diag[S.x];
+        o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
+        if (S.y == 0) r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
     } else {
-        return poll_record_fd(reinterpret_cast<const float4*>(v.rec_a) + rs, v.rec_b + rs, w, dq, v.err);
+        D = 1.0;
+        o = 1.0;
+        r = 0.0;
     }
 }
 
-// One unconditional read of a neighbour record, issued early; the values
-// are checked (record_set) only when the item that needs them starts.
-template <class R>
-__device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, R w[4], double dq[4]) {
+__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
+    if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
+    own_load(v, S, lane, x.D, x.o, x.r);
+}
+
+// One unconditional read of a neighbour record, issued early; the values are
+// checked (record_set) only when the item that needs them starts.
+__device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, double w[4], double dq[4]) {
+    const double2* pa = reinterpret_cast<const double2*>(v.rec_a + rs);
     const double2* pb = reinterpret_cast<const double2*>(v.rec_b + rs);
-    double2 x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
-    if constexpr (std::is_same<R, double>::value) {
-        const double2* pa = reinterpret_cast<const double2*>(v.rec_a + rs);
-        double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1);
-        w[0] = x0.x; w[1] = x0.y; w[2] = x1.x; w[3] = x1.y;
-    } else {
-        const float4* pa = reinterpret_cast<const float4*>(v.rec_a) + rs;
-        asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
-                     : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "l"(pa) : "memory");
-    }
+    double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1), x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
+    w[0] = x0.x; w[1] = x0.y; w[2] = x1.x; w[3] = x1.y;
     dq[0] = x2.x; dq[1] = x2.y; dq[2] = x3.x; dq[3] = x3.y;
 }
 
-template <class R>
-__device__ __forceinline__ bool record_set(const R w[4], const double dq[4]) {
+__device__ __forceinline__ bool record_set(const double w[4], const double dq[4]) {
     bool ready = true;
 #pragma unroll
     for (int j = 0; j < 4; ++j) ready = ready && !is_unset(w[j]) && !is_unset(dq[j]);
@@ -595,15 +570,13 @@ __device__ __forceinline__ bool record_set(const R w[4], const double dq[4]) {
 // order, loading the next item's inputs while it works on the current one.
 // Per item, for each edge whose neighbour precedes the node in this pass
 // (reference v2f order): the neighbour's values come from registers when the
-// warp itself computed that neighbour last, else from its polled record; the
-// edge term 0.5*(sign*(F(qc) - F(qold)) - omega*la*dqc) is formed per
-// component; lanes 0..3 add the terms in edge order (the reference's
-// summation order) and divide by the diagonal; the new state is spread to all
-// lanes, which keep its primitives for the next item while lanes 0 and 1
-// publish the record.  R = double: every operation and operand order is the
-// reference's.  R = float (mixed precision): the flux arithmetic and the
-// primitives are FP32; the sums, the diagonal division and dqc stay FP64.
-template <class R>
+// warp itself computed that neighbour last, else from its record (read early
+// or polled); the edge term 0.5*(sign*(F(qc) - F(qold)) - omega*la*dqc) is
+// formed per component; lanes 0..3 add the terms in edge order (the
+// reference's summation order) and divide by the diagonal; the new state is
+// spread to all lanes, which keep its primitives for the next item while
+// lanes 0 and 1 publish the record.  Every operation and operand order is the
+// reference's.
 __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -611,59 +584,54 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
     const int slot = lane >> 2, k = lane & 3;
     if (stopped(v)) return;
     const int n = v.nop;
-    const R gm1 = (R)(v.g.gamma - 1.0);
+    const double gm1 = v.g.gamma - 1.0;
     const int kbeg = woff[gw], kend = woff[gw + 1];
     if (kbeg >= kend) return;
     const int4 none = make_int4(0, 0, 0, 0);
     int4 S = v.sched[kbeg];
     int4 Sn = kbeg + 1 < kend ? v.sched[kbeg + 1] : none;
-    SweepIn<R> X = {}, Xn = {};
-    sweep_load<R>(v, S, lane, X);
+    SweepIn X = {}, Xn = {};
+    sweep_load(v, S, lane, X);
     int last = -1;  // code of the warp's previous item; its values below, in every lane
-    R Lrho = 0, Lu = 0, Lv = 0, Lp = 0, Le = 0;
-    double L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
-    // early look at the current item's first-round neighbour record, loaded
+    double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
+    // early read of the current item's first-round neighbour record, issued
     // during the previous item (usually already published)
-    R Sw[4] = {0, 0, 0, 0};
-    double Sdq[4] = {0.0, 0.0, 0.0, 0.0};
+    double Sw[4] = {0.0, 0.0, 0.0, 0.0}, Sdq[4] = {0.0, 0.0, 0.0, 0.0};
     bool spec = false;
     for (int kk = kbeg; kk < kend; ++kk) {
         const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
         const int it = S.x, pass = S.y, ntake = S.w;
         double cres = 0.0;  // lanes 0..3: sum over edges of component k
         for (int base = 0; base < ntake; base += 8) {
-            SweepIn<R> E = X;
-            if (base > 0 && base + slot < ntake) sweep_load_edge<R>(v, S.z + base + slot, k, E);
+            SweepIn E = X;
+            if (base > 0 && base + slot < ntake) sweep_load_edge(v, S.z + base + slot, k, E);
             bool ok = true;
             double t = 0.0;
             if (base + slot < ntake) {
-                // the neighbour's values: registers when this warp computed it
-                // last, else its record
-                R w[4], rho;
-                double dq[4];
+                double w[8], rho;
                 if (((E.nb << 1) | pass) == last) {
-                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le;
-                    dq[0] = L0; dq[1] = L1; dq[2] = L2; dq[3] = L3;
+                    w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
                     rho = Lrho;
-                } else if (base == 0 && spec && record_set<R>(Sw, Sdq)) {
+                } else if (base == 0 && spec && record_set(Sw, Sdq)) {
                     w[0] = Sw[0]; w[1] = Sw[1]; w[2] = Sw[2]; w[3] = Sw[3];
-                    dq[0] = Sdq[0]; dq[1] = Sdq[1]; dq[2] = Sdq[2]; dq[3] = Sdq[3];
-                    rho = E.rho_old + (R)dq[1];
+                    w[4] = Sdq[0]; w[5] = Sdq[1]; w[6] = Sdq[2]; w[7] = Sdq[3];
+                    rho = E.rho_old + w[5];
                 } else {
-                    ok = poll_neighbour<R>(v, (size_t)pass * n + E.nb, w, dq);
-                    rho = E.rho_old + (R)dq[1];
+                    const size_t rs = (size_t)pass * n + E.nb;
+                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
+                    rho = E.rho_old + w[5];
                 }
                 // normalflux (lusgs.f90:144-150) component k, then the edge term
-                const R u = w[0], vv = w[1], p = w[2], et = w[3];
-                const R un = u * E.nx + vv * E.ny;
-                const R o1 = rho * un;
-                const R prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
-                const R pn = p * (k == 2 ? E.nx : E.ny);
-                R o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
+                const double u = w[0], vv = w[1], p = w[2], et = w[3];
+                const double un = u * E.nx + vv * E.ny;
+                const double o1 = rho * un;
+                const double prod = (k == 0 ? et + p : o1) * (k == 0 ? un : (k == 2 ? u : vv));
+                const double pn = p * (k == 2 ? E.nx : E.ny);
+                double o = k == 1 ? o1 : (k == 0 ? prod : prod + pn);
                 o = o * E.ds;
-                const R diff = o - E.f1;
-                const R dqk = (R)(k == 0 ? dq[0] : (k == 1 ? dq[1] : (k == 2 ? dq[2] : dq[3])));
-                t = (double)(R(0.5) * ((E.sign < R(0) ? -diff : diff) - E.ol * dqk));
+                const double diff = o - E.f1;
+                const double dqk = pick4(k, w[4], w[5], w[6], w[7]);
+                t = 0.5 * ((E.sign < 0.0 ? -diff : diff) - E.ol * dqk);
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
             const int nr = min(8, ntake - base);
@@ -671,15 +639,12 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         }
         // next item's inputs (independent of the sweep), issued once this
         // item's polls are done so they do not queue ahead of them
-        if (kk + 1 < kend) sweep_load<R>(v, Sn, lane, Xn);
+        if (kk + 1 < kend) sweep_load(v, Sn, lane, Xn);
         double r = X.r;
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
-            if ((it << 1) == last) {
-                r = pick4(lane, L0, L1, L2, L3);
-            } else {
-                ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
-            }
+            if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
+            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
         }
         if (__ballot_sync(full, !ok)) return;
         // dqc and qc = qold + dqc (lusgs.f90:78-81 / 117-120), component k in lane k
@@ -687,16 +652,17 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         const double q = X.o + d;
         // the next item's first-round neighbour records, while this item finishes
         spec = false;
-        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass))
-            peek_neighbour<R>(v, (size_t)Sn.y * n + Xn.nb, Sw, Sdq), spec = true;
+        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
+            peek_neighbour(v, (size_t)Sn.y * n + Xn.nb, Sw, Sdq);
+            spec = true;
+        }
         // con2prim (pri.f90): rho = q1, then E/rho, rhou/rho, rhov/rho in lanes 0, 2, 3
-        const double rhod = __shfl_sync(full, q, 1);
-        const R rho = (R)rhod;
-        const R quo = (R)q / rho;
+        const double rho = __shfl_sync(full, q, 1);
+        const double quo = q / rho;
         const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
-        const R e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
-        const R qq = u * u + vv * vv;
-        const R p = gm1 * ((R)E0 - R(0.5) * rho * qq);
+        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        const double qq = u * u + vv * vv;
+        const double p = gm1 * (E0 - 0.5 * rho * qq);
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
@@ -705,19 +671,134 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
         if (lane == 0) {
-            if constexpr (std::is_same<R, double>::value) {
-                double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
-                st_relaxed2(a, Lu, Lv);
-                st_relaxed2(a + 1, Lp, Le);
-            } else {
-                st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, Lu, Lv, Lp, Le);
-            }
+            double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
+            st_relaxed2(a, Lu, Lv);
+            st_relaxed2(a + 1, Lp, Le);
         } else if (lane == 1) {
             double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
         } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(E0, rhod, Q2, Q3);
+            v.qc[it] = make_double4(E0, rho, Q2, Q3);
+        }
+        S = Sn;
+        Sn = Snn;
+        X = Xn;
+    }
+}
+
+// ------------------------------------------------------------ mixed (delta form)
+// The FP32 sweep cannot form F(qold + dqc) - F(qold) as a difference of two
+// O(1) fluxes: near convergence that difference drowns in FP32 rounding and
+// the solve stalls.  It forms the change directly from dqc (dflux_k), so its
+// FP32 error is relative to the change itself; items publish dqc only (FP32
+// for the edge terms, FP64 for the node's own backward step) and form no
+// primitives.
+struct SweepInM {
+    float rho, ru, rv, E, u, v, p, un, nx, ny, ds, ol, sign;  // the slot's record
+    int nb;
+    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
+};
+
+__device__ __forceinline__ void sweep_load_edge_m(const NCView& v, int rec, SweepInM& x) {
+    const float4* p = reinterpret_cast<const float4*>(v.rec) + 4 * (size_t)rec;
+    float4 a = p[0], b = p[1], c = p[2], d = p[3];
+    x.rho = a.x; x.ru = a.y; x.rv = a.z; x.E = a.w;
+    x.u = b.x; x.v = b.y; x.p = b.z; x.un = b.w;
+    x.nx = c.x; x.ny = c.y; x.ds = c.z; x.ol = c.w;
+    x.sign = d.x; x.nb = __float_as_int(d.y);
+}
+
+__device__ __forceinline__ void sweep_load_m(const NCView& v, const int4& S, int lane, SweepInM& x) {
+    if ((lane >> 2) < S.w) sweep_load_edge_m(v, S.z + (lane >> 2), x);
+    own_load(v, S, lane, x.D, x.o, x.r);
+}
+
+// lusgs sweeps in the mixed form: the schedule, lanes, hand-offs and FP64
+// sums / diagonal division of k_nc_lusgs; FP32 delta-form edge terms.
+__global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, const int* __restrict__ woff) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
+    const int slot = lane >> 2, k = lane & 3;
+    if (stopped(v)) return;
+    const int n = v.nop;
+    const float gm1 = (float)(v.g.gamma - 1.0);
+    const float4* recf = reinterpret_cast<const float4*>(v.rec_a);
+    const int kbeg = woff[gw], kend = woff[gw + 1];
+    if (kbeg >= kend) return;
+    const int4 none = make_int4(0, 0, 0, 0);
+    int4 S = v.sched[kbeg];
+    int4 Sn = kbeg + 1 < kend ? v.sched[kbeg + 1] : none;
+    SweepInM X = {}, Xn = {};
+    sweep_load_m(v, S, lane, X);
+    int last = -1;
+    float LF[4] = {0.f, 0.f, 0.f, 0.f};             // previous item's dqc (FP32)
+    double L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;  // and in FP64
+    float Sf[4] = {0.f, 0.f, 0.f, 0.f};
+    bool spec = false;
+    for (int kk = kbeg; kk < kend; ++kk) {
+        const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
+        const int it = S.x, pass = S.y, ntake = S.w;
+        double cres = 0.0;
+        for (int base = 0; base < ntake; base += 8) {
+            SweepInM E = X;
+            if (base > 0 && base + slot < ntake) sweep_load_edge_m(v, S.z + base + slot, E);
+            bool ok = true;
+            double t = 0.0;
+            if (base + slot < ntake) {
+                float dq[4];
+                if (((E.nb << 1) | pass) == last) {
+                    dq[0] = LF[0]; dq[1] = LF[1]; dq[2] = LF[2]; dq[3] = LF[3];
+                } else if (base == 0 && spec && set_f4(Sf)) {
+                    dq[0] = Sf[0]; dq[1] = Sf[1]; dq[2] = Sf[2]; dq[3] = Sf[3];
+                } else {
+                    ok = poll_f4(recf + (size_t)pass * n + E.nb, dq, v.err);
+                }
+                const float df = dflux_k(E, gm1, dq, k);
+                const float dqk = k == 0 ? dq[0] : (k == 1 ? dq[1] : (k == 2 ? dq[2] : dq[3]));
+                t = (double)(0.5f * ((E.sign < 0.f ? -df : df) * E.ds - E.ol * dqk));
+            }
+            if (__ballot_sync(full, !ok)) return;
+            const int nr = min(8, ntake - base);
+            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
+        }
+        if (kk + 1 < kend) sweep_load_m(v, Sn, lane, Xn);
+        double r = X.r;
+        bool ok = true;
+        if (pass == 1 && lane < 4) {  // own forward dqc
+            if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
+            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
+        }
+        if (__ballot_sync(full, !ok)) return;
+        const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
+        const double q = X.o + d;
+        spec = false;
+        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
+            peek_f4(recf + (size_t)Sn.y * n + Xn.nb, Sf);
+            spec = true;
+        }
+        const float df = (float)d;
+        LF[0] = __shfl_sync(full, df, 0);
+        LF[1] = __shfl_sync(full, df, 1);
+        LF[2] = __shfl_sync(full, df, 2);
+        LF[3] = __shfl_sync(full, df, 3);
+        L0 = __shfl_sync(full, d, 0);
+        L1 = __shfl_sync(full, d, 1);
+        L2 = __shfl_sync(full, d, 2);
+        L3 = __shfl_sync(full, d, 3);
+        const double Q0 = __shfl_sync(full, q, 0), Q1 = __shfl_sync(full, q, 1), Q2 = __shfl_sync(full, q, 2),
+                     Q3 = __shfl_sync(full, q, 3);
+        last = (it << 1) | pass;
+        const size_t slotr = (size_t)pass * n + it;
+        if (lane == 0) {
+            st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, LF[0], LF[1], LF[2], LF[3]);
+        } else if (lane == 1) {
+            double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
+            st_relaxed2(b, L0, L1);
+            st_relaxed2(b + 1, L2, L3);
+        } else if (lane == 2 && pass == 1) {
+            v.qc[it] = make_double4(Q0, Q1, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
@@ -825,15 +906,15 @@ int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (mixed) UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs<float>, v, (const int*)h->woff));
-    else UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs<double>, v, (const int*)h->woff));
+    if (mixed) UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs_mixed, v, (const int*)h->woff));
+    else UNS_CUDA(cudaLaunchKernelEx(&cfg, k_nc_lusgs, v, (const int*)h->woff));
     return UNS_OK;
 }
 
 int enqueue_sweep_prep_nc(uns_nc_handle* h, NCView& v) {
     if (v.nrec <= 0) return UNS_OK;
-    if (h->P.precision != UNS_PREC_FP64) NLAUNCH(k_nc_sweep_prep<float>, v.nrec, v);
-    else NLAUNCH(k_nc_sweep_prep<double>, v.nrec, v);
+    if (h->P.precision != UNS_PREC_FP64) NLAUNCH(k_nc_sweep_prep_mixed, v.nrec, v);
+    else NLAUNCH(k_nc_sweep_prep, v.nrec, v);
     return UNS_OK;
 }
 
@@ -969,7 +1050,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
         if (nop >= (1 << 30)) { set_last_error("uns_nc_create: too many nodes"); return fail(UNS_ERR_MESH); }
         int dev = 0, nsm = 0, per = 0;
         if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs<double>, kSweepBlock, 0) != cudaSuccess || per < 1) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_nc_lusgs, kSweepBlock, 0) != cudaSuccess || per < 1) {
             set_last_error("uns_nc_create: cannot size the cooperative LU-SGS launch");
             return fail(UNS_ERR_CUDA);
         }
