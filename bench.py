@@ -51,6 +51,14 @@ WORKLOADS = {
                      params=dict(m_inf=0.8, aoa_deg=1.25, flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0,
                                  min_res=0.0, precision="mixed"),
                      desc="as nc with FP32 face reconstruction + flux, FP64 accumulation"),
+    "nc_mixed_sweep": dict(kind="nc", ni=1024, nj=512, dwall=1e-3,
+                           params=dict(m_inf=0.8, aoa_deg=1.25, flux="ausm", limiter="barth_corrected", time="lusgs",
+                                       cfl_max=50.0, min_res=0.0, precision="mixed_sweep"),
+                           desc="as nc with FP32 delta-form arithmetic inside the LU-SGS sweeps only (FP64 residual)"),
+    "cc_small": dict(kind="cc", ni=128, nj=64, dwall=1e-3,
+                     params=dict(m_inf=0.5, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0),
+                     desc="CCFVM Euler, 128x64 O-mesh split to 16,384 triangles, M0.5 a2, Roe, GG + VKN, RK3 CFL 0.9, "
+                          "FP64 (the reference's CPU-sized case; CFL 1.0 leaves RK3 undefined there)"),
     "cc": dict(kind="cc", ni=2048, nj=1024, dwall=1e-3,
                params=dict(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0),
                desc="CCFVM Euler, 2048x1024 O-mesh split to 4,194,304 triangles, M0.75 a2, Roe, GG + VKN, RK3, FP64"),
@@ -123,6 +131,70 @@ def launches_per_iter(kind: str, rk3: bool, laminar: bool) -> dict:
     if kind == "nc":
         return {"grad_lim": n, "edge": n, "node_res": n}
     return {"face_conv": n, "cell_res": n, "viscous": n if laminar else 0, "cirs": n}
+
+
+# ---------------------------------------------------------------- accuracy
+def lift_drag(fx: float, fy: float, aoa_deg: float) -> tuple[float, float]:
+    """C_L, C_D of the flux-based wall force (unit chord; rho, |V| = 1)."""
+    a = math.radians(aoa_deg)
+    return (fy * math.cos(a) - fx * math.sin(a)) / 0.5, (fx * math.cos(a) + fy * math.sin(a)) / 0.5
+
+
+def accuracy_vs_fp64(w: dict, m, solver, hist: np.ndarray) -> dict:
+    """A mixed-form run against FP64 over the same iterations from freestream:
+    the L2 residual norm histories, the final states and (CC) C_L / C_D."""
+    from unsflow2d_gb300.solver import CCSolver, NCSolver
+    kind = w["kind"]
+    ref_params = {k: v for k, v in w["params"].items() if k != "precision"}
+    p64 = abi.make_params(**ref_params)
+    ref = (NCSolver if kind == "nc" else CCSolver)(m, p64)
+    r = ref.iterate(cfl_list(p64, kind, 1, len(hist)), first_iter=True)
+    h64 = np.asarray(r if kind == "cc" else r[0])
+    q32, q64 = solver.get_state(), ref.get_state()
+    out = {"iterations": int(len(hist)),
+           "residual_l2_final": {"mixed": float(hist[-1]), "fp64": float(h64[-1]),
+                                 "rel_diff": float(abs(hist[-1] - h64[-1]) / h64[-1])},
+           "residual_l2_max_log10_diff": float(np.max(np.abs(np.log10(hist) - np.log10(h64)))),
+           "state_rel_l2_diff": float(np.linalg.norm(q32 - q64) / np.linalg.norm(q64))}
+    if kind == "cc":
+        c32 = lift_drag(*solver.forces(), w["params"]["aoa_deg"])
+        c64 = lift_drag(*ref.forces(), w["params"]["aoa_deg"])
+        out["CL"] = {"mixed": c32[0], "fp64": c64[0], "abs_diff": abs(c32[0] - c64[0])}
+        out["CD"] = {"mixed": c32[1], "fp64": c64[1], "abs_diff": abs(c32[1] - c64[1])}
+    ref.close()
+    return out
+
+
+# ---------------------------------------------------------------- convergence
+# Time to a 1e-8 drop of the normalised residual, from freestream, on the
+# 128x64 mesh of the workload's family (the scheme has no multigrid: the
+# 1024x512 NCFVM case drops only ~3e-2 in 4000 LU-SGS iterations, so a 1e-8
+# drop there is hours of iterations; 128x64 takes ~7000).  FP64, and the fast
+# form that still converges: NCFVM FP32 sweeps with the FP64 residual,
+# CCFVM FP32 fluxes until their rounding floor, then FP64.
+CONVERGE_MESH = (128, 64)
+
+
+def time_to_drop(w: dict, target: float = 1e-8) -> dict:
+    from unsflow2d_gb300.solver import CCSolver, NCSolver, converge
+    kind = w["kind"]
+    Mesh = mesh.CCMesh if kind == "cc" else mesh.NCMesh
+    m = Mesh.airfoil(*CONVERGE_MESH, 0.12, 20.0, w["dwall"])
+    base = {k: v for k, v in w["params"].items() if k not in ("min_res", "precision")}
+    forms = [("fp64", None)] + ([("mixed_sweep", None)] if kind == "nc" else [("mixed", 1e-4)])
+    out = {"mesh": f"{CONVERGE_MESH[0]}x{CONVERGE_MESH[1]}", "target_drop": target,
+           "units": int(m.arrays["nop"] if kind == "nc" else m.arrays["noc"])}
+    for prec, switch in forms:
+        p = abi.make_params(precision=prec, min_res=target, **base)
+        s = (NCSolver if kind == "nc" else CCSolver)(m, p)
+        t0 = time.perf_counter()
+        r = converge(s, target, 60000 if kind == "cc" else 20000, switch_drop=switch)
+        dt = time.perf_counter() - t0
+        h = r["history"]
+        out[prec] = {"seconds": round(dt, 3), "iterations": int(r["iterations"]), "reached": bool(h[-1] <= target),
+                     "final_drop": float(h[-1]), "fp64_from_iteration": r["switched_at"]}
+        s.close()
+    return out
 
 
 # ---------------------------------------------------------------- clocks
@@ -204,6 +276,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     units = units_of(w, m)
     kind = w["kind"]
     it = 0
+    hist: list[float] = []
 
     def iterate(n):
         nonlocal it
@@ -213,6 +286,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
         f = r if kind == "cc" else r[0]
         if len(f) != n or not np.isfinite(f).all():
             raise RuntimeError(f"solver stopped or diverged: {len(f)} of {n} iterations, last norm {f[-1:]}")
+        hist.extend(np.asarray(f).tolist())
         return r
 
     iterate(args.warmup)
@@ -229,6 +303,11 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     ms = e0.elapsed_time(e1)
     tot_units, secs = replicas.reduce_timing(dist, units * args.steps, ms / 1e3, device=str(dev))
     value = tot_units / secs / 1e6
+
+    # Mixed forms: the same iterations in FP64 from the same start, compared.
+    accuracy = None
+    if p.precision != abi.PREC["fp64"] and rank == 0:
+        accuracy = accuracy_vs_fp64(w, m, solver, np.array(hist))
 
     # End to end through the per-routine C-ABI (the calls a Fortran driver
     # makes), with the state in pinned host memory copied in and out each step.
@@ -326,6 +405,10 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     }
     if not args.no_cpu_baseline and args.gpus == 1:
         out["cpu_baseline"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
+    if accuracy is not None:
+        out["accuracy_vs_fp64"] = accuracy
+    if not args.no_converge:
+        out["time_to_1e-8"] = time_to_drop(w)
     return out
 
 
@@ -398,6 +481,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--mesh", default=None, help="override the O-mesh size, e.g. 512x256 (profiling runs)")
+    ap.add_argument("--no-converge", action="store_true", help="skip the time-to-1e-8 leg")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

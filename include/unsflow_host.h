@@ -54,6 +54,14 @@ int uns_host_read_flo_nc(const char* path, uns_params* p, char* grid, int gridle
 double uns_host_cfl_cc(const uns_params* p, int iter, double prev);
 double uns_host_cfl_nc(const uns_params* p, int iter);
 
+/* save_flow / read_flow (CCFVM/solution.F90:88-114, NCFVM/common.f90:58-84):
+ * the conserved state of the first n cells (nodes), one '(4e20.10)' line
+ * each, as [n][4] row-major.  The reference defines them but never calls
+ * them; uns_host_*_main reads FLO.DAT from flo.inp's directory when flo.inp's
+ * Start is 2 and writes FLO.DAT into outdir at the end of the run. */
+int uns_host_save_flow(const char* path, const double* qc, int n);
+int uns_host_read_flow(const char* path, double* qc, int n);
+
 /* The reference main program (CCFVM/main.F90:4-170, NCFVM/main.f90:266-374)
  * on the GPU library: reads flo.inp, the geometry named there (relative to
  * flo.inp's directory), runs to MaxIter / MinRes and writes FLO.RES into

@@ -109,7 +109,7 @@ typedef struct {
     int32_t max_iter;    /* MaxIter                                         */
     double min_res;      /* MinRes                                          */
     int32_t scr_interval;/* ScrInt                                          */
-    int32_t pad_;
+    int32_t istart;      /* Start: 1 scratch, 2 restart from FLO.DAT        */
 } uns_params;
 
 /* Cell-centred mesh after the caller's geometric preprocessing

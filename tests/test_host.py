@@ -173,6 +173,30 @@ def test_flo_inp_reader_and_validation(tmp_path):
     assert e.value.code == abi.UNS_ERR_IO
 
 
+def test_flo_dat_round_trip_and_format(tmp_path):
+    """save_flow / read_flow: '(4e20.10)' lines, ten significant digits."""
+    lib = abi.host_lib()
+    rng = np.random.default_rng(3)
+    q = rng.standard_normal((7, 4)) * 10.0 ** rng.integers(-30, 30, (7, 4))
+    q[0, 0] = 0.0
+    f = tmp_path / "FLO.DAT"
+    D = C.POINTER(C.c_double)
+    abi.check(lib.uns_host_save_flow(str(f).encode(), q.ctypes.data_as(D), 7), lib, "save_flow")
+    lines = f.read_text().splitlines()
+    assert len(lines) == 7 and all(len(x) == 80 for x in lines)
+    assert lines[0][:20] == "    0.0000000000E+00"
+    assert re.fullmatch(r"( *-?0\.\d{10}E[+-]\d{2}){4}", lines[1])
+    back = np.zeros((7, 4))
+    abi.check(lib.uns_host_read_flow(str(f).encode(), back.ctypes.data_as(D), 7), lib, "read_flow")
+    assert np.allclose(back, q, rtol=5e-10, atol=0)
+    # list-directed input also takes Fortran D exponents; a short file is an I/O error
+    f.write_text("1.5D0 2 3 4\n")
+    one = np.zeros((1, 4))
+    abi.check(lib.uns_host_read_flow(str(f).encode(), one.ctypes.data_as(D), 1), lib, "read_flow")
+    assert one.tolist() == [[1.5, 2.0, 3.0, 4.0]]
+    assert lib.uns_host_read_flow(str(f).encode(), back.ctypes.data_as(D), 2) == abi.UNS_ERR_IO
+
+
 def test_cfl_schedules():
     p = abi.make_params(cfl_type="tanh", cfl_max=0.9, cfl_ramp_steps=500)
     c = mesh.cfl_schedule(p, 1, 600)

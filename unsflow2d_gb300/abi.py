@@ -47,16 +47,16 @@ class Params(C.Structure):
                 ("time_mode", C.c_int32), ("cfl_type", C.c_int32), ("cfl_min", C.c_double),
                 ("cfl_max", C.c_double), ("cfl_ramp_steps", C.c_int32), ("limiter_type", C.c_int32),
                 ("precision", C.c_int32), ("max_iter", C.c_int32), ("min_res", C.c_double),
-                ("scr_interval", C.c_int32), ("pad_", C.c_int32)]
+                ("scr_interval", C.c_int32), ("istart", C.c_int32)]
 
 
 def make_params(m_inf=0.5, aoa_deg=2.0, rey=5000.0, t_wall=300.0, flow="inviscid", iwall=1,
                 flux="roe", grad="gg", ilimit=1, irs=0, time="rk3", cfl_type="tanh", cfl_min=0.1,
                 cfl_max=0.9, cfl_ramp_steps=500, limiter="vkn", precision="fp64", max_iter=2000,
-                min_res=1e-8, scr_interval=100) -> Params:
+                min_res=1e-8, scr_interval=100, istart=1) -> Params:
     return Params(m_inf, aoa_deg, rey, t_wall, FLOW[flow], iwall, FLUX[flux], GRAD[grad], ilimit, irs,
                   TIME[time], CFLT[cfl_type], cfl_min, cfl_max, cfl_ramp_steps, LIMITER[limiter],
-                  PREC[precision], max_iter, min_res, scr_interval, 0)
+                  PREC[precision], max_iter, min_res, scr_interval, istart)
 
 
 _D = C.POINTER(C.c_double)
@@ -240,6 +240,7 @@ def host_lib() -> C.CDLL:
             "uns_host_cfl_nc": ([C.POINTER(Params), i32], dp),
             "uns_host_cc_main": ([C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_int), _D], i32),
             "uns_host_nc_main": ([C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_int), _D], i32),
+            "uns_host_save_flow": ([C.c_char_p, _D, i32], i32), "uns_host_read_flow": ([C.c_char_p, _D, i32], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)

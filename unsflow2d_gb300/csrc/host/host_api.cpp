@@ -177,6 +177,39 @@ double uns_host_cfl_nc(const uns_params* p, int iter) {
     return 0.5 * p->cfl_max * (1.0 + std::tanh((double)iter * 7.0 / 500.0 - 3.5));
 }
 
+int uns_host_save_flow(const char* path, const double* qc, int n) {
+    if (!path || !qc || n < 0) return fail(UNS_ERR_ARG, "uns_host_save_flow: bad argument");
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(UNS_ERR_IO, std::string("cannot write ") + path);
+    for (int i = 0; i < n; ++i)  // write(50,'(4e20.10)') qc(1:nvar)
+        std::fprintf(f, "%s%s%s%s\n", fort_e(qc[4 * i], 20, 10).c_str(), fort_e(qc[4 * i + 1], 20, 10).c_str(),
+                     fort_e(qc[4 * i + 2], 20, 10).c_str(), fort_e(qc[4 * i + 3], 20, 10).c_str());
+    return std::fclose(f) == 0 ? UNS_OK : fail(UNS_ERR_IO, std::string("cannot write ") + path);
+}
+
+int uns_host_read_flow(const char* path, double* qc, int n) {
+    if (!path || !qc || n < 0) return fail(UNS_ERR_ARG, "uns_host_read_flow: bad argument");
+    FILE* f = std::fopen(path, "r");
+    if (!f) return fail(UNS_ERR_IO, std::string("cannot open ") + path);
+    for (int i = 0; i < 4 * n; ++i) {  // list-directed read(50,*): Fortran E or D exponents
+        char tok[64];
+        if (std::fscanf(f, "%63s", tok) != 1) {
+            std::fclose(f);
+            return fail(UNS_ERR_IO, std::string(path) + ": fewer than " + std::to_string(n) + " states");
+        }
+        for (char* c = tok; *c; ++c)
+            if (*c == 'D' || *c == 'd') *c = 'e';
+        char* end = nullptr;
+        qc[i] = std::strtod(tok, &end);
+        if (end == tok || *end) {
+            std::fclose(f);
+            return fail(UNS_ERR_IO, std::string(path) + ": bad number '" + tok + "'");
+        }
+    }
+    std::fclose(f);
+    return UNS_OK;
+}
+
 int uns_host_cc_main(const char* flo_inp, const char* outdir, int mode, int* iters_out, double* fres_out) {
     if (!flo_inp || !outdir) return fail(UNS_ERR_ARG, "null argument");
     uns_params P;
@@ -189,6 +222,18 @@ int uns_host_cc_main(const char* flo_inp, const char* outdir, int mode, int* ite
     uns_cc_mesh view = mesh.view();
     uns_cc_handle* h = nullptr;
     if ((rc = uns_cc_create(&view, &P, &h))) return fail(rc, uns_last_error());
+    const int nst = view.noc + view.nbf;
+    std::vector<double> state(4 * (size_t)nst);
+    if (P.istart == 2) {  // read_flow (CCFVM/solution.F90:103-114): interior cells
+        g_err.clear();
+        if ((rc = uns_cc_get_state(h, state.data())) ||
+            (rc = uns_host_read_flow(join(dir_of(flo_inp), "FLO.DAT").c_str(), state.data(), view.noc)) ||
+            (rc = uns_cc_set_state(h, state.data()))) {
+            std::string e = g_err.empty() ? uns_last_error() : g_err;
+            uns_cc_destroy(h);
+            return fail(rc, e);
+        }
+    }
     std::string res_path = std::string(outdir) + "/FLO.RES";
     FILE* fo = std::fopen(res_path.c_str(), "w");
     if (!fo) { uns_cc_destroy(h); return fail(UNS_ERR_IO, "cannot write " + res_path); }
@@ -232,7 +277,10 @@ int uns_host_cc_main(const char* flo_inp, const char* outdir, int mode, int* ite
         }
     }
     std::fclose(fo);
-    std::string e = rc ? std::string(uns_last_error()) : std::string();
+    g_err.clear();
+    if (!rc && !(rc = uns_cc_get_state(h, state.data())))  // save_flow (CCFVM/solution.F90:88-99)
+        rc = uns_host_save_flow((std::string(outdir) + "/FLO.DAT").c_str(), state.data(), view.noc);
+    std::string e = rc ? (g_err.empty() ? std::string(uns_last_error()) : g_err) : std::string();
     uns_cc_destroy(h);
     if (iters_out) *iters_out = iter;
     if (fres_out) *fres_out = fres;
@@ -251,6 +299,16 @@ int uns_host_nc_main(const char* flo_inp, const char* outdir, int mode, int* ite
     uns_nc_mesh view = mesh.view();
     uns_nc_handle* h = nullptr;
     if ((rc = uns_nc_create(&view, &P, &h))) return fail(rc, uns_last_error());
+    std::vector<double> state(4 * (size_t)view.nop);
+    if (P.istart == 2) {  // read_flow (NCFVM/common.f90:73-84)
+        g_err.clear();
+        if ((rc = uns_host_read_flow(join(dir_of(flo_inp), "FLO.DAT").c_str(), state.data(), view.nop)) ||
+            (rc = uns_nc_set_state(h, state.data()))) {
+            std::string e = g_err.empty() ? uns_last_error() : g_err;
+            uns_nc_destroy(h);
+            return fail(rc, e);
+        }
+    }
     std::string res_path = std::string(outdir) + "/FLO.RES";
     FILE* fo = std::fopen(res_path.c_str(), "w");
     if (!fo) { uns_nc_destroy(h); return fail(UNS_ERR_IO, "cannot write " + res_path); }
@@ -289,7 +347,10 @@ int uns_host_nc_main(const char* flo_inp, const char* outdir, int mode, int* ite
         }
     }
     std::fclose(fo);
-    std::string e = rc ? std::string(uns_last_error()) : std::string();
+    g_err.clear();
+    if (!rc && !(rc = uns_nc_get_state(h, state.data())))  // save_flow (NCFVM/common.f90:58-69)
+        rc = uns_host_save_flow((std::string(outdir) + "/FLO.DAT").c_str(), state.data(), view.nop);
+    std::string e = rc ? (g_err.empty() ? std::string(uns_last_error()) : g_err) : std::string();
     uns_nc_destroy(h);
     if (iters_out) *iters_out = iter;
     if (fres_out) *fres_out = fres;

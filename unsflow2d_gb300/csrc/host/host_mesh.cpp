@@ -832,6 +832,7 @@ int read_flo_inp_cc(const std::string& path, uns_params& p, std::string& grid, s
         grid = L[18][1];
         // Validation as CCFVM/read_input.F90:53-119.
         if (istart != 1 && istart != 2) { err = "Unknown start option"; return UNS_ERR_ARG; }
+        p.istart = istart;
         if (flow == "inviscid") p.flow_type = UNS_FLOW_INVISCID;
         else if (flow == "laminar") p.flow_type = UNS_FLOW_LAMINAR;
         else if (flow == "rans") { err = "RANS not available"; return UNS_ERR_ARG; }
@@ -900,6 +901,7 @@ int read_flo_inp_nc(const std::string& path, uns_params& p, std::string& grid, s
         int vortex = std::stoi(L[16][1]);
         grid = L[17][1];
         if (istart != 1 && istart != 2) { err = "Unknown start option"; return UNS_ERR_ARG; }
+        p.istart = istart;
         if (flow == "inviscid") p.flow_type = UNS_FLOW_INVISCID;
         else if (flow == "laminar" || flow == "rans") { err = "NCFVM hot path is inviscid"; return UNS_ERR_ARG; }
         else { err = "Unknown flow type " + flow; return UNS_ERR_ARG; }
