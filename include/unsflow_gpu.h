@@ -114,6 +114,28 @@ int uns_nc_residue(uns_nc_handle* h, double* fres_raw, double* fresi, int* iresi
 int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
                    double* fresi, int* done_iters);
 
+/* =========================================================== batches ====*/
+/* Many independent CCFVM instances (different meshes, flow conditions,
+ * fluxes) advanced together.  No reference counterpart: the reference runs
+ * one case per process.  One CUDA graph holds every instance's captured
+ * main-loop iteration as a parallel branch; each launch advances all of them
+ * by one iteration, so small meshes fill the GPU together.  Instances keep
+ * their own state, CFL schedule, residual history and stop test (an
+ * instance whose residual has dropped to its min_res skips its kernels).
+ * The handles stay owned by the caller, must outlive the batch and must not
+ * be used on their own while a batch call runs. */
+typedef struct uns_cc_batch uns_cc_batch;
+int uns_cc_batch_create(uns_cc_handle* const* handles, int n, uns_cc_batch** out);
+int uns_cc_batch_destroy(uns_cc_batch* b);
+/* The cudaStream_t batch launches go to (for the caller's CUDA events). */
+void* uns_cc_batch_stream(uns_cc_batch* b);
+/* As uns_cc_iterate for every instance i: cfl[i*niter + k] is its CFL of
+ * iteration k, fres_raw[i*niter + k] receives its raw residual norm and
+ * done_iters[i] the iterations it executed.  Rebuilds the graph when an
+ * instance's precision (uns_cc_set_precision) or first_iter changed. */
+int uns_cc_batch_iterate(uns_cc_batch* b, int niter, const double* cfl, int first_iter, double* fres_raw,
+                         int* done_iters);
+
 /* ========================================================= precision ====*/
 /* Switches the arithmetic form (UNS_PREC_*) between calls; waits for the
  * handle's stream, and the next uns_*_iterate captures a new graph.  No

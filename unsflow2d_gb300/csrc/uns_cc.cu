@@ -1163,6 +1163,7 @@ struct uns_cc_handle {
     double* d_fres1 = nullptr;
     double* d_scalar = nullptr;  // [4] scratch for host-visible scalars
     int graph_first = -1;
+    int gen = 0;           // bumped whenever the captured iteration changes (precision, capacity)
     double cfl_cur = 0.0;  // CFL passed to the last time_step call
 
     template <class T>
@@ -1729,6 +1730,25 @@ int uns_cc_forces(uns_cc_handle* h, double* fx, double* fy) {
     return UNS_OK;
 }
 
+// One main-loop iteration of a handle captured as a graph, wired to the
+// handle's device-side CFL schedule, iteration counter, history and stop flag.
+static int capture_iteration(uns_cc_handle* h, int first_iter, cudaGraph_t* out) {
+    CCView v = h->v;
+    v.cfl_sched = h->d_cfl;
+    v.iter = h->d_iter;
+    v.done = h->d_done;
+    v.fres_hist = h->d_hist;
+    v.fres1 = h->d_fres1;
+    v.first_iter = first_iter ? 1 : 0;
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    UNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_iteration(h, v, 0.0);
+    cudaError_t ce = cudaStreamEndCapture(h->stream, out);
+    if (rc) return rc;
+    if (ce != cudaSuccess) { set_last_error(std::string("graph capture: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
+    return UNS_OK;
+}
+
 int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
     if (!h || niter < 0 || (niter > 0 && (!cfl || !fres_raw))) return UNS_ERR_ARG;
     if (done_iters) *done_iters = 0;
@@ -1740,6 +1760,7 @@ int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_ite
         UNS_CUDA(cudaMalloc(&h->d_cfl, sizeof(double) * niter));
         UNS_CUDA(cudaMalloc(&h->d_hist, sizeof(double) * niter));
         h->cfl_cap = niter;
+        ++h->gen;
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     }
     // The smoothing sweeps are launched only while their coefficient is
@@ -1782,21 +1803,10 @@ int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_ite
     UNS_CUDA(cudaMemsetAsync(h->d_hist, 0, sizeof(double) * niter, h->stream));
     if (!h->graph || h->graph_first != (first_iter ? 1 : 0)) {
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
-        CCView v = h->v;
-        v.cfl_sched = h->d_cfl;
-        v.iter = h->d_iter;
-        v.done = h->d_done;
-        v.fres_hist = h->d_hist;
-        v.fres1 = h->d_fres1;
-        v.first_iter = first_iter ? 1 : 0;
         cudaGraph_t graph;
-        UNS_CUDA(cudaStreamSynchronize(h->stream));
-        UNS_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        int rc = enqueue_iteration(h, v, 0.0);
-        cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+        int rc = capture_iteration(h, first_iter, &graph);
         if (rc) return rc;
-        if (ce != cudaSuccess) { set_last_error(std::string("graph capture: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
-        ce = cudaGraphInstantiate(&h->graph, graph, 0);
+        cudaError_t ce = cudaGraphInstantiate(&h->graph, graph, 0);
         cudaGraphDestroy(graph);
         if (ce != cudaSuccess) { set_last_error(std::string("graph instantiate: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
         h->graph_first = first_iter ? 1 : 0;
@@ -1815,7 +1825,130 @@ int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (h->P.precision != precision) {
         UNS_CUDA(cudaStreamSynchronize(h->stream));
         h->P.precision = precision;
+        ++h->gen;
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    }
+    return UNS_OK;
+}
+
+// ---------------------------------------------------------------- batches
+// Independent instances advanced together: one CUDA graph whose parallel
+// branches are the instances' captured iterations, so one launch advances
+// every instance by one iteration and small meshes share the GPU.  Each
+// instance keeps its own device state, CFL schedule, history and stop flag;
+// an instance that has converged skips its kernels on the device.
+struct uns_cc_batch {
+    std::vector<uns_cc_handle*> hs;
+    std::vector<int> gens;  // each handle's `gen` when the graph was built
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int first = -1;
+};
+
+int uns_cc_batch_create(uns_cc_handle* const* handles, int n, uns_cc_batch** out) {
+    if (!handles || n <= 0 || !out) { set_last_error("uns_cc_batch_create: bad arguments"); return UNS_ERR_ARG; }
+    *out = nullptr;
+    std::vector<uns_cc_handle*> hs(handles, handles + n);
+    std::vector<uns_cc_handle*> sorted = hs;
+    std::sort(sorted.begin(), sorted.end());
+    if (!sorted[0] || std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+        set_last_error("uns_cc_batch_create: null or repeated handle");
+        return UNS_ERR_ARG;
+    }
+    auto* b = new uns_cc_batch();
+    b->hs = hs;
+    b->gens.assign(n, -1);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        set_last_error("uns_cc_batch_create: cudaStreamCreate failed");
+        return UNS_ERR_CUDA;
+    }
+    *out = b;
+    return UNS_OK;
+}
+
+void* uns_cc_batch_stream(uns_cc_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+int uns_cc_batch_destroy(uns_cc_batch* b) {
+    if (!b) return UNS_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return UNS_OK;
+}
+
+int uns_cc_batch_iterate(uns_cc_batch* b, int niter, const double* cfl, int first_iter, double* fres_raw,
+                         int* done_iters) {
+    if (!b || niter < 0 || (niter > 0 && (!cfl || !fres_raw || !done_iters))) return UNS_ERR_ARG;
+    const int n = (int)b->hs.size();
+    if (niter == 0) {
+        for (int i = 0; i < n; ++i) done_iters[i] = 0;
+        return UNS_OK;
+    }
+    for (int i = 0; i < n; ++i) {
+        uns_cc_handle* h = b->hs[i];
+        for (int k = 0; k < niter; ++k)
+            if (h->P.irs && epsirs_of(h, cfl[(size_t)i * niter + k]) > 0.0) {
+                set_last_error("uns_cc_batch_iterate: residual smoothing above CFLmax is not batched");
+                return UNS_ERR_ARG;
+            }
+        if (niter > h->cfl_cap) {
+            UNS_CUDA(cudaStreamSynchronize(h->stream));
+            if (h->d_cfl) cudaFree(h->d_cfl);
+            if (h->d_hist) cudaFree(h->d_hist);
+            h->d_cfl = nullptr; h->d_hist = nullptr;
+            UNS_CUDA(cudaMalloc(&h->d_cfl, sizeof(double) * niter));
+            UNS_CUDA(cudaMalloc(&h->d_hist, sizeof(double) * niter));
+            h->cfl_cap = niter;
+            ++h->gen;
+            if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+        }
+        UNS_CUDA(cudaStreamSynchronize(h->stream));
+    }
+    bool rebuild = !b->exec || b->first != (first_iter ? 1 : 0);
+    for (int i = 0; i < n && !rebuild; ++i) rebuild = b->gens[i] != b->hs[i]->gen;
+    if (rebuild) {
+        if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+        cudaGraph_t parent;
+        UNS_CUDA(cudaGraphCreate(&parent, 0));
+        for (int i = 0; i < n; ++i) {
+            cudaGraph_t child;
+            int rc = capture_iteration(b->hs[i], first_iter, &child);
+            if (rc) { cudaGraphDestroy(parent); return rc; }
+            cudaGraphNode_t node;
+            cudaError_t ce = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, child);
+            cudaGraphDestroy(child);
+            if (ce != cudaSuccess) {
+                cudaGraphDestroy(parent);
+                set_last_error(std::string("batch graph: ") + cudaGetErrorString(ce));
+                return UNS_ERR_CUDA;
+            }
+            b->gens[i] = b->hs[i]->gen;
+        }
+        cudaError_t ce = cudaGraphInstantiate(&b->exec, parent, 0);
+        cudaGraphDestroy(parent);
+        if (ce != cudaSuccess) { set_last_error(std::string("batch graph instantiate: ") + cudaGetErrorString(ce)); return UNS_ERR_CUDA; }
+        b->first = first_iter ? 1 : 0;
+    }
+    for (int i = 0; i < n; ++i) {
+        uns_cc_handle* h = b->hs[i];
+        UNS_CUDA(cudaMemcpyAsync(h->d_cfl, cfl + (size_t)i * niter, sizeof(double) * niter, cudaMemcpyHostToDevice, b->stream));
+        UNS_CUDA(cudaMemsetAsync(h->d_iter, 0, sizeof(int), b->stream));
+        UNS_CUDA(cudaMemsetAsync(h->d_done, 0, sizeof(int), b->stream));
+        UNS_CUDA(cudaMemsetAsync(h->d_hist, 0, sizeof(double) * niter, b->stream));
+    }
+    for (int k = 0; k < niter; ++k) UNS_CUDA(cudaGraphLaunch(b->exec, b->stream));
+    for (int i = 0; i < n; ++i) {
+        uns_cc_handle* h = b->hs[i];
+        UNS_CUDA(cudaMemcpyAsync(fres_raw + (size_t)i * niter, h->d_hist, sizeof(double) * niter, cudaMemcpyDeviceToHost,
+                                 b->stream));
+        UNS_CUDA(cudaMemcpyAsync(done_iters + i, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    }
+    UNS_CUDA(cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < n; ++i) {
+        int rc = check_dev_err(b->hs[i]);
+        if (rc) return rc;
     }
     return UNS_OK;
 }

@@ -212,6 +212,46 @@ class NCSolver(_Solver):
         return out[:done.value], outi[:done.value]
 
 
+class CCBatch:
+    """Independent CCSolver instances advanced together by one graph launch
+    per iteration (uns_cc_batch_*)."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        self._lib = abi.gpu_lib()
+        arr = (C.c_void_p * len(self.solvers))(*[s._h.value for s in self.solvers])
+        h = C.c_void_p()
+        abi.check(self._lib.uns_cc_batch_create(arr, len(self.solvers), C.byref(h)), self._lib, "uns_cc_batch_create")
+        self._h = h
+
+    def iterate(self, cfl: np.ndarray, first_iter: bool) -> tuple[list[np.ndarray], np.ndarray]:
+        """cfl: [instances, niter].  Returns each instance's raw residual norms
+        of the iterations it ran, and those counts."""
+        cfl = np.ascontiguousarray(cfl, dtype=np.float64)
+        n, niter = cfl.shape
+        assert n == len(self.solvers)
+        out = np.zeros((n, niter))
+        done = (C.c_int * n)()
+        rc = self._lib.uns_cc_batch_iterate(self._h, niter, _dp(cfl), 1 if first_iter else 0, _dp(out), done)
+        abi.check(rc, self._lib, "uns_cc_batch_iterate")
+        d = np.array(list(done))
+        return [out[i, :d[i]] for i in range(n)], d
+
+    def stream(self) -> int:
+        return self._lib.uns_cc_batch_stream(self._h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.uns_cc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def converge(solver, target: float, max_iter: int, switch_drop: float | None = None, chunk: int = 500,
              on_chunk=None) -> dict:
     """Run the main loop from iteration 1 until the density residual has dropped
