@@ -4,7 +4,8 @@
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 --fmad=false \
 //        -o fp64_issue unsflow2d_gb300/microbench/fp64_issue.cu && ./fp64_issue
 //
-// Prints, for FP64 add / mul / fma / divide and FP32 add / divide, the
+// Prints, for FP64 add / mul / fma / divide, FP32 add / divide and an
+// FP64 -> FP32 conversion, the
 // cycles per dependent operation of one thread and the whole-GPU rate at
 // 1, 4 and 8 warps per SM sub-partition, with 1 and 32 active lanes (does an
 // FP64 warp-instruction cost less with fewer active lanes?), and the latency
@@ -37,11 +38,17 @@ __global__ void k_chain(double* out, double a, int active, long long* cyc) {
 #pragma unroll 16
             for (int i = 0; i < kN; ++i) y = y + b;
             x = y;
-        } else {
+        } else if (OP == 5) {
             float y = (float)x, b = (float)a;
 #pragma unroll 4
             for (int i = 0; i < kN / 8; ++i) y = b / y;
             x = y;
+        } else {  // independent FP64 -> FP32 conversions feeding one FP32 sum
+            const long long bits = __double_as_longlong(a) + threadIdx.x;
+            float acc = 0.f;
+#pragma unroll 16
+            for (int i = 0; i < kN; ++i) acc += (float)__longlong_as_double(bits + ((long long)i << 20));
+            x = acc;
         }
     }
     long long t1 = clock64();
@@ -67,7 +74,8 @@ int main() {
     cudaMalloc(&cyc, sizeof(long long));
     struct Op { const char* name; void (*f)(double*, double, int, long long*); int ops; };
     Op ops[] = {{"f64 add", k_chain<0>, kN}, {"f64 mul", k_chain<1>, kN}, {"f64 fma", k_chain<2>, kN},
-                {"f64 div", k_chain<3>, kN / 8}, {"f32 add", k_chain<4>, kN}, {"f32 div", k_chain<5>, kN / 8}};
+                {"f64 div", k_chain<3>, kN / 8}, {"f32 add", k_chain<4>, kN}, {"f32 div", k_chain<5>, kN / 8},
+                {"cvt f64>f32 (independent) + f32 add", k_chain<6>, kN}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
