@@ -113,8 +113,19 @@ struct CCView {
     int* done;
     double* fres_hist;
     double* fres1;
+    // FP32 copies read by the FP32-flux (mixed) form, so that its kernels do
+    // their arithmetic in FP32 without per-value FP64->FP32 conversions
+    // (which issue on the FP64 unit).  Geometry is rounded once from FP64.
+    const float4* fgeof;  // per face: fc - cen[in] (x, y), fc - cen[out] (x, y; 0 on boundary faces)
+    const float4* fnaf;   // per face: nx, ny, area, 0
+    const float4* lswf;   // LSQ weights
+    float4* qpf;          // [ntot] rho, u, v, p (ghost cells: always kept)
+    float4* fqf;          // [nof] face primitives of avg_c2v
+    float* flaf;          // [nof] face spectral radius
+    float4* packf;        // [4 * noc] per cell: primitives, gx, gy, phi
     Gas g;
     int grad_type, ilimit, irs, laminar, first_iter;
+    int mixed;            // UNS_PREC_MIXED: keep the FP32 copies, run the FP32 kernels
     double cfl_max, min_res;
 };
 
@@ -140,6 +151,7 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
             Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
             v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
             v.qT[i] = P.t;
+            if (v.mixed) v.qpf[i] = make_float4((float)P.rho, (float)P.u, (float)P.v, (float)P.p);
             if ((flags & BEGIN_POS) && (P.rho <= 0.0 || P.p <= 0.0)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
         }
         if (flags & BEGIN_OLD) v.qold[i] = q;
@@ -214,6 +226,10 @@ __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     double ll = v.farea[f] * (fabs(un) + a0);
     ll = ll + v.g.vll * v.fmu[f] / q.x;
     v.fla[f] = ll;
+    if (v.mixed) {
+        v.fqf[f] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+        v.flaf[f] = (float)ll;
+    }
 }
 
 // Diamond-path face gradient (gradient.F90:474-556, gradtrixy :572-612).
@@ -288,6 +304,18 @@ __device__ __forceinline__ double4 d4(const double o[4]) { return make_double4(o
 // order (interior faces, then boundary faces).
 enum { CG_DT = 1, CG_GRAD = 2, CG_LIM = 4 };
 
+// atomicMin of an order-encoded double with one atomic per converged group of
+// lanes: the minimum 64-bit key is the minimum high word, then the minimum low
+// word among the lanes that hold it.  Same result as one atomic per lane
+// (min is exact and order-free), without 32 same-address atomics per warp.
+__device__ __forceinline__ void warp_atomic_min_u64(unsigned long long* dst, unsigned long long e) {
+    const unsigned mask = __activemask();
+    const unsigned hi = (unsigned)(e >> 32), lo = (unsigned)e;
+    const unsigned mh = __reduce_min_sync(mask, hi);
+    const unsigned ml = __reduce_min_sync(mask, hi == mh ? lo : 0xffffffffu);
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicMin(dst, ((unsigned long long)mh << 32) | ml);
+}
+
 __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, double cfl_in) {
     if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,7 +329,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
         v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
-        atomicMin(v.dtmin, enc_ord(dt));
+        warp_atomic_min_u64(v.dtmin, enc_ord(dt));
     }
     double gx[4], gy[4];
     if (flags & CG_GRAD) {
@@ -424,6 +452,132 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
     }
 }
 
+// k_cell_grad in the mixed form: the same gathers, face orders and formulas
+// with the gradient and the Venkatakrishnan limiter in FP32 on the FP32
+// copies.  dt, la and diag come from the FP32 face radii; the FP64 gx, gy,
+// phi and dt stay the stored state (phi is a running minimum across
+// iterations), and the per-cell pack feeds k_face_conv<float>.
+__global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags, double cfl_in) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+    if (flags & CG_DT) {
+        float la = 0.f;
+        for (int k = k0; k < k1; ++k) la = la + v.flaf[v.cf[k] & FACE_MASK];
+        const float cvf = (float)v.cv[i];
+        const float dt = (float)cur_cfl(v, cfl_in) * cvf / la;
+        v.la[i] = (double)la;
+        v.dt[i] = (double)dt;
+        v.diag[i] = (double)(cvf / dt + 0.75f * la);
+        warp_atomic_min_u64(v.dtmin, enc_ord((double)dt));
+    }
+    if (!(flags & (CG_GRAD | CG_LIM))) return;
+    const float4 q4 = v.qpf[i];
+    const float qi[4] = {q4.x, q4.y, q4.z, q4.w};
+    float gx[4], gy[4];
+    if (flags & CG_GRAD) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { gx[j] = 0.f; gy[j] = 0.f; }
+        if (v.grad_type == UNS_GRAD_GG) {
+            for (int k = k0; k < k1; ++k) {
+                int e = v.cf[k], f = e & FACE_MASK;
+                const float4 na = v.fnaf[f];
+                const float4 q = v.fqf[f];
+                // outward from this cell: + for the `in` side of an interior face
+                const float s = (f < v.nfi && !(e & SIDE_BIT)) ? 1.f : -1.f;
+                const float dx = s * (na.x * na.z), dy = s * (na.y * na.z);
+                gx[0] += q.x * dx; gx[1] += q.y * dx; gx[2] += q.z * dx; gx[3] += q.w * dx;
+                gy[0] += q.x * dy; gy[1] += q.y * dy; gy[2] += q.z * dy; gy[3] += q.w * dy;
+            }
+            const float r = 1.f / (float)v.cv[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { gx[j] *= r; gy[j] *= r; }
+        } else if (v.grad_type == UNS_GRAD_GGFC) {
+            for (int k = k0; k < k1; ++k) {
+                int f = v.cf[k] & FACE_MASK;
+                const float s = (float)v.fasum[f];
+                const double4 a = v.fgx[f], b = v.fgy[f];
+                gx[0] += (float)a.x * s; gx[1] += (float)a.y * s; gx[2] += (float)a.z * s; gx[3] += (float)a.w * s;
+                gy[0] += (float)b.x * s; gy[1] += (float)b.y * s; gy[2] += (float)b.z * s; gy[3] += (float)b.w * s;
+            }
+            const float r = 1.f / (float)v.cov[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { gx[j] *= r; gy[j] *= r; }
+        } else {  // LSQR
+            for (int k = k0; k < k1; ++k) {
+                int e = v.cf[k], f = e & FACE_MASK;
+                const float4 w = v.lswf[f];
+                const int2 nb = v.fnb[f];
+                const float4 a = v.qpf[nb.x], b = v.qpf[nb.y];
+                const float d[4] = {b.x - a.x, b.y - a.y, b.z - a.z, b.w - a.w};
+                if (f < v.nfi && (e & SIDE_BIT)) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) { gx[j] -= d[j] * w.z; gy[j] -= d[j] * w.w; }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) { gx[j] += d[j] * w.x; gy[j] += d[j] * w.y; }
+                }
+            }
+        }
+        v.gx[i] = make_double4(gx[0], gx[1], gx[2], gx[3]);
+        v.gy[i] = make_double4(gy[0], gy[1], gy[2], gy[3]);
+    } else {  // limiter alone: the stored FP64 gradient
+        const double4 a = v.gx[i], b = v.gy[i];
+        gx[0] = (float)a.x; gx[1] = (float)a.y; gx[2] = (float)a.z; gx[3] = (float)a.w;
+        gy[0] = (float)b.x; gy[1] = (float)b.y; gy[2] = (float)b.z; gy[3] = (float)b.w;
+    }
+    const double4 p0 = v.phi[i];
+    float ph[4] = {(float)p0.x, (float)p0.y, (float)p0.z, (float)p0.w};
+    if (flags & CG_LIM) {
+        float tol[4], umax[4], umin[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float hi = (float)dec_ord(v.minmax[j]), lo = (float)dec_ord(v.minmax[4 + j]);
+            tol[j] = 0.05f * (hi - lo);
+            tol[j] = tol[j] * tol[j];
+            umax[j] = qi[j];
+            umin[j] = qi[j];
+        }
+        for (int k = k0; k < k1; ++k) {
+            int e = v.cf[k], f = e & FACE_MASK;
+            float4 u;
+            if (f < v.nfi) {
+                const int2 nb = v.fnb[f];
+                u = v.qpf[(e & SIDE_BIT) ? nb.x : nb.y];
+            } else {
+                u = v.fqf[f];  // the face average of avg_c2v, as limiter.F90 uses on boundary faces
+            }
+            umax[0] = rmax(umax[0], u.x); umin[0] = rmin(umin[0], u.x);
+            umax[1] = rmax(umax[1], u.y); umin[1] = rmin(umin[1], u.y);
+            umax[2] = rmax(umax[2], u.z); umin[2] = rmin(umin[2], u.z);
+            umax[3] = rmax(umax[3], u.w); umin[3] = rmin(umin[3], u.w);
+        }
+        for (int k = k0; k < k1; ++k) {
+            int e = v.cf[k], f = e & FACE_MASK;
+            const float4 gd = v.fgeof[f];
+            const float d0 = (e & SIDE_BIT) ? gd.z : gd.x, d1 = (e & SIDE_BIT) ? gd.w : gd.y;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float D_L = gx[j] * d0 + gy[j] * d1;
+                float phi0 = 1.f;
+                if (D_L != 0.f) {  // limiter.F90:286-294 with a = (umax or umin) - qi, b = D_L
+                    const float a = (D_L > 0.f ? umax[j] : umin[j]) - qi[j];
+                    const float nr = a * a + 2.f * a * D_L + tol[j];
+                    const float dr = a * a + 2.f * D_L * D_L + a * D_L + tol[j];
+                    phi0 = __fdividef(nr, dr);
+                }
+                ph[j] = rmin(ph[j], phi0);
+            }
+        }
+        v.phi[i] = make_double4(ph[0], ph[1], ph[2], ph[3]);
+    }
+    v.packf[4 * (size_t)i] = q4;
+    v.packf[4 * (size_t)i + 1] = make_float4(gx[0], gx[1], gx[2], gx[3]);
+    v.packf[4 * (size_t)i + 2] = make_float4(gy[0], gy[1], gy[2], gy[3]);
+    v.packf[4 * (size_t)i + 3] = make_float4(ph[0], ph[1], ph[2], ph[3]);
+}
+
 // Convective face flux (fvresidual.F90:27-171).  Boundary faces also write
 // their ghost cell (farfield: Riemann state; wall: slip / no-slip mirror).
 // R = double for the FP64 form, float for FP32 face arithmetic.
@@ -453,6 +607,32 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
     if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    if constexpr (std::is_same<R, float>::value) {
+        if (f < v.nfi) {  // interior face of the mixed form: FP32 packs and geometry only
+            const int2 nb = v.fnb[f];
+            const float4* A = v.packf + 4 * (size_t)nb.x;
+            const float4* B = v.packf + 4 * (size_t)nb.y;
+            const float4 qa = A[0], ga = A[1], ha = A[2], pa = A[3];
+            const float4 qb = B[0], gb = B[1], hb = B[2], pb = B[3];
+            const float4 d = v.fgeof[f], na = v.fnaf[f];
+            const float zhi = 1.f / 3.f, zlo = 1.f - 1.f / 3.f;
+            const float qi[4] = {qa.x, qa.y, qa.z, qa.w}, qo[4] = {qb.x, qb.y, qb.z, qb.w};
+            const float gxi[4] = {ga.x, ga.y, ga.z, ga.w}, gyi[4] = {ha.x, ha.y, ha.z, ha.w};
+            const float gxo[4] = {gb.x, gb.y, gb.z, gb.w}, gyo[4] = {hb.x, hb.y, hb.z, hb.w};
+            const float phi_i[4] = {pa.x, pa.y, pa.z, pa.w}, phi_o[4] = {pb.x, pb.y, pb.z, pb.w};
+            V4<float> ql, qr, F;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
+                const float beta = qo[j] - qi[j];
+                ql[j] = qi[j] + 0.5f * phi_i[j] * (zhi * beta + zlo * (gxi[j] * d.x + gyi[j] * d.y));
+                qr[j] = qo[j] + 0.5f * phi_o[j] * (zhi * -beta + zlo * (gxo[j] * d.z + gyo[j] * d.w));
+            }
+            bool ok = flux_dispatch<float>(v, na.x, na.y, na.z, ql, qr, F);
+            if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+            v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
+            return;
+        }
+    }
     int2 nb = v.fnb[f];
     int in = nb.x, out = nb.y;
     double2 n = v.fn[f];
@@ -513,6 +693,7 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
         Prim P = con2prim(g, C[0], C[1], C[2], C[3]);
         v.qp[out] = make_double4(P.rho, P.u, P.v, P.p);
         v.qT[out] = P.t;
+        v.qpf[out] = make_float4((float)P.rho, (float)P.u, (float)P.v, (float)P.p);
     } else if (bc == 1001) {
         double4 c = v.qc[in];
         Prim P = con2prim(g, c.x, c.y, c.z, c.w);
@@ -543,6 +724,7 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
         v.qc[out] = gq;
         v.qp[out] = gp;
         v.qT[out] = gT;
+        v.qpf[out] = make_float4((float)gp.x, (float)gp.y, (float)gp.z, (float)gp.w);
         for (int j = 0; j < 4; ++j) ql[j] = (R)qcl[j];
         qr[0] = (R)gp.x; qr[1] = (R)gp.y; qr[2] = (R)gp.z; qr[3] = (R)gp.w;
         bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
@@ -762,8 +944,34 @@ __global__ void k_check_pos(CCView v) {
 
 __global__ void k_initialize(CCView v, double4 qinf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < v.ntot) { v.qc[i] = qinf; v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0; }
+    if (i < v.ntot) {
+        v.qc[i] = qinf; v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0;
+        v.qpf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     if (i < v.noc) v.phi[i] = make_double4(1.0, 1.0, 1.0, 1.0);
+}
+
+// Rebuilds every FP32 copy from the FP64 state, so a handle switched to the
+// mixed form between calls starts from consistent copies.
+__global__ void k_mirror_f32(CCView v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < v.ntot) {
+        double4 q = v.qp[i];
+        float4 qf = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+        v.qpf[i] = qf;
+        if (i < v.noc) {
+            double4 a = v.gx[i], b = v.gy[i], c = v.phi[i];
+            v.packf[4 * (size_t)i] = qf;
+            v.packf[4 * (size_t)i + 1] = make_float4((float)a.x, (float)a.y, (float)a.z, (float)a.w);
+            v.packf[4 * (size_t)i + 2] = make_float4((float)b.x, (float)b.y, (float)b.z, (float)b.w);
+            v.packf[4 * (size_t)i + 3] = make_float4((float)c.x, (float)c.y, (float)c.z, (float)c.w);
+        }
+    }
+    if (i < v.nof) {
+        double4 q = v.fq[i];
+        v.fqf[i] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+        v.flaf[i] = (float)v.fla[i];
+    }
 }
 
 // lusgs2 sweeps (lusgs.F90:245-318), one level of the dependency DAG per
@@ -1227,11 +1435,18 @@ int enqueue_minmax(uns_cc_handle* h, CCView& v) {
     return UNS_OK;
 }
 
+// k_cell_grad, or its FP32 form for a handle in the mixed form.
+#define LAUNCH_CELL_GRAD(v, flags, cfl)                                                 \
+    do {                                                                               \
+        if ((v).mixed) LAUNCH(k_cell_grad_mixed, (v).noc, (v), (int)(flags), (cfl));   \
+        else LAUNCH(k_cell_grad, (v).noc, (v), (int)(flags), (cfl));                   \
+    } while (0)
+
 int enqueue_gradient(uns_cc_handle* h, CCView& v, int extra_flags, double cfl, bool do_reduce) {
     if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
     int flags = CG_GRAD | extra_flags | (v.ilimit ? CG_LIM : 0);
     if (v.ilimit && do_reduce) { int rc = enqueue_minmax(h, v); if (rc) return rc; }
-    LAUNCH(k_cell_grad, v.noc, v, flags, cfl);
+    LAUNCH_CELL_GRAD(v, flags, cfl);
     return UNS_OK;
 }
 
@@ -1308,7 +1523,7 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
     LAUNCH(k_vertex_avg, v.nop, v);
     LAUNCH(k_face_prim_spec, v.nof, v);
     if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
-    LAUNCH(k_cell_grad, v.noc, v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.0);
+    LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.0);
     if (h->P.time_mode == UNS_TIME_RK3) {
         for (int irk = 1; irk <= 3; ++irk) {
             bool fused = false;
@@ -1430,6 +1645,16 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
         }
         lsw[f] = make_double4(wx0, wy0, wx1, wy1);
     }
+    // FP32 geometry of the mixed form, rounded once from the FP64 values.
+    std::vector<float4> fgeof(nof), fnaf(nof), lswf(nof);
+    for (int f = 0; f < nof; ++f) {
+        int in = m->fin[f], o = m->fout[f];
+        double xl = m->fcx[f] - m->cx[in], yl = m->fcy[f] - m->cy[in];
+        double xr = f < nfi ? m->fcx[f] - m->cx[o] : 0.0, yr = f < nfi ? m->fcy[f] - m->cy[o] : 0.0;
+        fgeof[f] = make_float4((float)xl, (float)yl, (float)xr, (float)yr);
+        fnaf[f] = make_float4((float)m->fnx[f], (float)m->fny[f], (float)m->farea[f], 0.f);
+        lswf[f] = make_float4((float)lsw[f].x, (float)lsw[f].y, (float)lsw[f].z, (float)lsw[f].w);
+    }
     std::vector<int> rc2f_off(m->c2f_off, m->c2f_off + noc + 1);
     std::vector<int> rc2f(m->c2f, m->c2f + rc2f_off[noc]);
 
@@ -1440,6 +1665,7 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     v.grad_type = p->grad_type; v.ilimit = p->ilimit; v.irs = p->irs;
     v.laminar = p->flow_type == UNS_FLOW_LAMINAR;
     v.cfl_max = p->cfl_max; v.min_res = p->min_res;
+    v.mixed = p->precision == UNS_PREC_MIXED;
 #define UP(field, vec) if ((rc = h->upload(*(std::remove_const<std::remove_pointer<decltype(v.field)>::type>::type**)&v.field, vec.data(), vec.size()))) return fail(rc)
 #define AL(field, n) if ((rc = h->alloc(v.field, (n)))) return fail(rc)
     UP(pxy, pxy); UP(cen, cen);
@@ -1461,6 +1687,8 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     AL(fF, nof); AL(fV, nof); AL(fgx, nof); AL(fgy, nof); AL(fgT, nof); AL(fasum, nof);
     AL(fwall, nbf); AL(fwallv, nbf);
     AL(diag, noc); AL(rec_a, 2 * (size_t)noc); AL(rec_b, 2 * (size_t)noc);
+    UP(fgeof, fgeof); UP(fnaf, fnaf); UP(lswf, lswf);
+    AL(qpf, ntot); AL(fqf, nof); AL(flaf, nof); AL(packf, 4 * (size_t)noc);
     AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
     h->nparts = nblocks(noc);
     AL(partial, h->nparts);
@@ -1640,7 +1868,7 @@ int uns_cc_time_step(uns_cc_handle* h, double cfl, double* dtglobal) {
     h->cfl_cur = cfl;  // cirs of this iteration uses the same CFL
     k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
     UNS_CUDA(cudaGetLastError());
-    LAUNCH(k_cell_grad, v.noc, v, (int)CG_DT, cfl);
+    LAUNCH_CELL_GRAD(v, CG_DT, cfl);
     if (dtglobal) {
         unsigned long long e = 0;
         UNS_CUDA(cudaMemcpyAsync(&e, v.dtmin, 8, cudaMemcpyDeviceToHost, h->stream));
@@ -1668,7 +1896,7 @@ int uns_cc_limit(uns_cc_handle* h) {
     CCView v = h->v;
     int rc = enqueue_minmax(h, v);
     if (rc) return rc;
-    LAUNCH(k_cell_grad, v.noc, v, (int)CG_LIM, 0.0);
+    LAUNCH_CELL_GRAD(v, CG_LIM, 0.0);
     return UNS_OK;
 }
 
@@ -1825,6 +2053,11 @@ int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (h->P.precision != precision) {
         UNS_CUDA(cudaStreamSynchronize(h->stream));
         h->P.precision = precision;
+        h->v.mixed = precision == UNS_PREC_MIXED;
+        if (h->v.mixed) {
+            CCView& v = h->v;
+            LAUNCH(k_mirror_f32, std::max(v.ntot, v.nof), v);
+        }
         ++h->gen;
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     }
@@ -1990,7 +2223,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
         if (!rc) rc = timed(1, [&]() -> int { LAUNCH(k_vertex_avg, v.nop, v); return UNS_OK; });
         if (!rc) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
         if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
-        if (!rc) rc = timed(4, [&]() -> int { LAUNCH(k_cell_grad, v.noc, v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), cfl); return UNS_OK; });
+        if (!rc) rc = timed(4, [&]() -> int { LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), cfl); return UNS_OK; });
         for (int irk = 1; irk <= (rk3 ? 3 : 1) && !rc; ++irk) {
             rc = timed(5, [&]() -> int {
                 if (h->P.precision == UNS_PREC_MIXED) LAUNCH(k_face_conv<float>, v.nof, v);
