@@ -44,6 +44,11 @@ int uns_cc_set_state(uns_cc_handle* h, const double* qc);
 int uns_cc_get_state(uns_cc_handle* h, double* qc);
 /* Any UNS_CC_* field (unsflow_types.h) copied to host memory. */
 int uns_cc_get_field(uns_cc_handle* h, int field, double* out);
+/* Overwrites UNS_CC_QC, UNS_CC_QP (all noc+nbf cells, ghosts included, with
+ * T) or UNS_CC_PHI from host memory: the rest of the state a restart or a
+ * frozen-limiter continuation needs besides uns_cc_set_state (no reference
+ * counterpart: the reference restarts from qc alone). */
+int uns_cc_set_field(uns_cc_handle* h, int field, const double* in);
 
 /* con2prim over the interior cells (CCFVM/main.F90:62-67). */
 int uns_cc_con2prim(uns_cc_handle* h);
@@ -135,6 +140,34 @@ void* uns_cc_batch_stream(uns_cc_batch* b);
  * instance's precision (uns_cc_set_precision) or first_iter changed. */
 int uns_cc_batch_iterate(uns_cc_batch* b, int niter, const double* cfl, int first_iter, double* fres_raw,
                          int* done_iters);
+
+/* =========================================================== adjoint ====*/
+/* Discrete adjoint of the CCFVM RK3 iteration (no reference counterpart).
+ * The state s is the conserved state of the noc interior cells plus the
+ * primitives and T of the nbf ghost cells; one iteration maps s to G(s) and
+ * computes the objective J (UNS_OBJ_*) from its last stage's wall fluxes.
+ * At a converged state, lambda = G_s^T lambda + J_s^T gives
+ * dJ/dalpha = J_alpha + G_alpha^T lambda (alpha in radians).  The limiter is
+ * frozen at its current phi; RK3, FP64, no residual smoothing.
+ *
+ * prepare records the linearisation: one forward iteration at `cfl` from the
+ * current state (two for a viscous flow, whose time step reads the previous
+ * iteration's face viscosity), which advances the state by those iterations
+ * (at convergence it does not change), and returns C_L, C_D of the recorded
+ * iteration (either pointer may be NULL). */
+int uns_cc_adjoint_prepare(uns_cc_handle* h, double cfl, double* cl, double* cd);
+/* One transposed iteration: (oq, og) = G_s^T (wq, wg) + seed * J_s^T and
+ * *oalpha = G_alpha^T (wq, wg) + seed * J_alpha.  wq, oq: [noc][4] conserved;
+ * wg, og: [nbf][5] ghost rho, u, v, p, T. */
+int uns_cc_adjoint_vjp(uns_cc_handle* h, int objective, double seed, const double* wq, const double* wg, double* oq,
+                       double* og, double* oalpha);
+/* Reverse accumulation from lambda = 0 until the change of lambda falls to
+ * tol times its first change, or max_iter transposed iterations.  hist[k]
+ * (may be NULL; max_iter entries) receives the change of iteration k. */
+int uns_cc_adjoint_solve(uns_cc_handle* h, int objective, int max_iter, double tol, double* dj_dalpha, double* hist,
+                         int* iters);
+/* The adjoint vector of the last solve: [noc][4] and [nbf][5] (either may be NULL). */
+int uns_cc_adjoint_get(uns_cc_handle* h, double* lambda_q, double* lambda_g);
 
 /* ========================================================= precision ====*/
 /* Switches the arithmetic form (UNS_PREC_*) between calls; waits for the

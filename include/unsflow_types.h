@@ -54,6 +54,10 @@ enum { UNS_LIM_VKN = 0, UNS_LIM_BARTH = 1, UNS_LIM_BARTH_CORRECTED = 2 };
  * residual, FP32 flux arithmetic only inside the LU-SGS sweeps (the implicit
  * operator), so the solve converges as far as the FP64 one. */
 enum { UNS_PREC_FP64 = 0, UNS_PREC_MIXED = 1, UNS_PREC_MIXED_SWEEP = 2 };
+/* Objectives of the discrete adjoint: the flux-based force coefficients
+ * C_L = 2 (Fy1 cos a - Fx1 sin a), C_D = 2 (Fx1 cos a + Fy1 sin a)
+ * (CCFVM/main.F90:348-353). */
+enum { UNS_OBJ_CL = 0, UNS_OBJ_CD = 1 };
 
 /* Field identifiers for the state accessors (uns_cc_get_field,
  * uns_nc_get_field).  Layouts are row-major with the variable index fastest,

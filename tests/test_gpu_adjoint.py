@@ -1,0 +1,165 @@
+"""Discrete adjoint of the CCFVM RK3 iteration (uns_cc_adjoint_*).
+
+At a converged state s* the adjoint runs the iteration G backwards:
+uns_cc_adjoint_vjp returns G_s^T w + seed*J_s^T and G_alpha^T w + seed*J_alpha
+for the flux-based C_L / C_D.  Checked here against central differences of the
+GPU forward iteration itself (same limiter frozen at the converged phi):
+
+* one transposed iteration: <w, dG/ds u> + seed <dJ/ds, u> (central difference,
+  step 1e-6 relative per entry) equals <G_s^T w + seed J_s^T, u> for random
+  w, u, and likewise for the angle of attack;
+* the total derivative dJ/dalpha of the adjoint solve equals the central
+  difference of J between two solutions re-converged at alpha +- 5e-4 deg.
+
+Inviscid (slip wall) and laminar (isothermal and adiabatic no-slip walls)
+flows, the Roe, van Leer and Rusanov fluxes and the three gradients are
+covered.  (The CCFVM AUSM+-up flux is not scaled by the face length -- a
+reference quirk -- and does not converge on these meshes.  A laminar flow
+with a non-GGFC convective gradient alternates two gradient operators inside
+each iteration -- the viscous step recomputes the cell gradient -- and on
+these meshes its residual stalls instead of converging, so it has no
+converged state to differentiate.)
+"""
+import numpy as np
+import pytest
+
+from unsflow2d_gb300 import abi, mesh
+from unsflow2d_gb300.solver import CCSolver
+
+pytestmark = pytest.mark.gpu
+
+CFL = 0.8
+CASES = {
+    "euler_roe_gg": dict(flux="roe", grad="gg", m_inf=0.5, aoa_deg=2.0),
+    "euler_roe_ggfc": dict(flux="roe", grad="ggfc", m_inf=0.5, aoa_deg=2.0),
+    "euler_vanleer_lsqr": dict(flux="vanleer", grad="lsqr", m_inf=0.5, aoa_deg=2.0),
+    "euler_rusanov_gg": dict(flux="rusanov", grad="gg", m_inf=0.5, aoa_deg=2.0),
+    "laminar_roe_ggfc_iso": dict(flow="laminar", iwall=0, rey=5000.0, flux="roe", grad="ggfc", m_inf=0.5, aoa_deg=3.0),
+    "laminar_roe_ggfc_adia": dict(flow="laminar", iwall=1, rey=5000.0, flux="roe", grad="ggfc", m_inf=0.5, aoa_deg=3.0),
+}
+_cache = {}
+
+
+def _converge(s: CCSolver, target: float, chunk: int = 5000, max_iter: int = 300000) -> float:
+    """Iterate until the raw residual norm is at most `target`; returns the last norm."""
+    last, done = np.inf, 0
+    while done < max_iter and last > target:
+        h = s.iterate(np.full(chunk, CFL), first_iter=(done == 0))
+        last = h[-1]
+        done += chunk
+    return last
+
+
+def _frozen(m, kw, aoa=None):
+    k = dict(kw)
+    if aoa is not None:
+        k["aoa_deg"] = aoa
+    return CCSolver(m, abi.make_params(ilimit=0, min_res=1e-30, **k))
+
+
+def _base(name):
+    """Converged state of a case: limiter on while the flow develops, then phi frozen."""
+    if name in _cache:
+        return _cache[name]
+    kw = CASES[name]
+    m = mesh.CCMesh.airfoil(32, 16)
+    p = abi.make_params(min_res=1e-30, **kw)
+    s = CCSolver(m, p)
+    r0 = s.iterate(mesh.cfl_schedule(p, 1, 600, "cc"), first_iter=True)[0]
+    f = _frozen(m, kw)
+    f.set("qc", s.get_state())
+    f.set("qp", s.get("qp"))
+    f.set("phi", s.get("phi"))
+    target = 1e-12 * r0
+    drop = _converge(f, target) / r0
+    state = (f.get_state(), f.get("qp"), f.get("phi"))
+    _cache[name] = (m, kw, f, state, drop, target)
+    return _cache[name]
+
+
+def _prime(s: CCSolver, state):
+    """Load the converged state and run one iteration from it, so the face
+    viscosity that the next iteration's time step reads is the converged
+    one (a fresh handle holds zero there); then load the state again."""
+    _load(s, state)
+    s.iterate(np.array([CFL]), first_iter=True)
+    _load(s, state)
+    return s
+
+
+def _load(s: CCSolver, state, dq=None, dg=None):
+    qc, qp, phi = (x.copy() for x in state)
+    noc = s.noc
+    if dq is not None:
+        qc[:noc] += dq
+        qp[noc:] += dg
+    s.set("qc", qc)
+    s.set("qp", qp)
+    s.set("phi", phi)
+
+
+def _step(s: CCSolver):
+    """One iteration G: returns (interior qc, ghost primitives + T, C_L, C_D)."""
+    s.iterate(np.array([CFL]), first_iter=True)
+    cl, cd = s.cl_cd()
+    return s.get_state()[:s.noc], s.get("qp")[s.noc:], cl, cd
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_vjp_matches_forward_differences(name):
+    m, kw, f, state, drop, _ = _base(name)
+    assert drop <= 1e-12, drop
+    noc, nbf = f.noc, f.nbf
+    qc0, qp0 = state[0][:noc], state[1][noc:]
+    rng = np.random.default_rng(7)
+    uq = rng.standard_normal(qc0.shape) * np.abs(qc0)
+    ug = rng.standard_normal(qp0.shape) * np.abs(qp0)
+    wq = rng.standard_normal((noc, 4))
+    wg = rng.standard_normal((nbf, 5))
+    seed = 0.7
+    g = _prime(_frozen(m, kw), state)
+    h = 1e-6
+    _load(g, state, h * uq, h * ug)
+    qa, ga, cla, cda = _step(g)
+    _load(g, state, -h * uq, -h * ug)
+    qb, gb, clb, cdb = _step(g)
+    a = _frozen(m, kw)
+    _load(a, state)
+    a.adjoint_prepare(CFL)
+    for obj, ja, jb in (("cl", cla, clb), ("cd", cda, cdb)):
+        lhs = (np.sum(wq * (qa - qb)) + np.sum(wg * (ga - gb)) + seed * (ja - jb)) / (2 * h)
+        oq, og, _ = a.adjoint_vjp(obj, seed, wq, wg)
+        rhs = np.sum(oq * uq) + np.sum(og * ug)
+        assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (obj, lhs, rhs)
+    # angle of attack (per radian)
+    da = 1e-4
+    gp_ = _prime(_frozen(m, kw, kw["aoa_deg"] + da), state)
+    gm_ = _prime(_frozen(m, kw, kw["aoa_deg"] - da), state)
+    qa, ga, cla, cda = _step(gp_)
+    qb, gb, clb, cdb = _step(gm_)
+    scale = 2 * np.deg2rad(da)
+    for obj, ja, jb in (("cl", cla, clb), ("cd", cda, cdb)):
+        lhs = (np.sum(wq * (qa - qb)) + np.sum(wg * (ga - gb)) + seed * (ja - jb)) / scale
+        _, _, oa = a.adjoint_vjp(obj, seed, wq, wg)
+        assert abs(lhs - oa) <= 1e-6 * max(abs(lhs), 1e-3), (obj, lhs, oa)
+
+
+@pytest.mark.parametrize("name", ["euler_roe_gg", "laminar_roe_ggfc_iso"])
+def test_total_derivative_matches_reconverged_differences(name):
+    m, kw, f, state, _, target = _base(name)
+    a = _frozen(m, kw)
+    _load(a, state)
+    cl0, cd0 = a.adjoint_prepare(CFL)
+    da = 5e-4
+    res = {}
+    for sgn in (1, -1):
+        s = _frozen(m, kw, kw["aoa_deg"] + sgn * da)
+        _load(s, state)
+        assert _converge(s, target) <= target
+        s.iterate(np.array([CFL]), first_iter=True)
+        res[sgn] = s.cl_cd()
+    for k, obj in enumerate(("cl", "cd")):
+        fd = (res[1][k] - res[-1][k]) / (2 * np.deg2rad(da))
+        d, hist = a.adjoint_solve(obj, max_iter=300000, tol=1e-12)
+        assert len(hist) < 300000 and np.isfinite(d)
+        assert abs(d - fd) <= 2e-5 * abs(fd), (obj, d, fd)

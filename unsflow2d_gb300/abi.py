@@ -28,6 +28,7 @@ TIME = {"rk3": 0, "lusgs": 1}
 CFLT = {"tanh": 0, "ramp": 1}
 LIMITER = {"vkn": 0, "barth": 1, "barth_corrected": 2}
 PREC = {"fp64": 0, "mixed": 1, "mixed_sweep": 2}
+OBJ = {"cl": 0, "cd": 1}
 
 CC_FIELDS = {"qc": 0, "qp": 1, "qold": 2, "res": 3, "grad": 4, "phi": 5, "dt": 6, "la": 7,
              "ptprim": 8, "fqp": 9, "fla": 10, "fmu": 11, "fgrad": 12, "mul": 13}
@@ -212,6 +213,11 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_batch_stream": ([vp], vp),
             "uns_cc_batch_iterate": ([vp, i32, dp, i32, dp, C.POINTER(C.c_int)], i32),
             "uns_cc_set_precision": ([vp, i32], i32), "uns_nc_set_precision": ([vp, i32], i32),
+            "uns_cc_set_field": ([vp, i32, dp], i32),
+            "uns_cc_adjoint_prepare": ([vp, C.c_double, dp, dp], i32),
+            "uns_cc_adjoint_vjp": ([vp, i32, C.c_double, dp, dp, dp, dp, dp], i32),
+            "uns_cc_adjoint_solve": ([vp, i32, i32, C.c_double, dp, dp, C.POINTER(C.c_int)], i32),
+            "uns_cc_adjoint_get": ([vp, dp, dp], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)

@@ -28,6 +28,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "uns_cc_impl.cuh"
 #include "uns_common.cuh"
 #include "uns_phys.cuh"
 #include "uns_sched.hpp"
@@ -37,97 +38,6 @@ using namespace uns;
 
 namespace {
 
-constexpr int SIDE_BIT = 1 << 30;  // cell is the `out` side of this face
-constexpr int FACE_MASK = SIDE_BIT - 1;
-
-struct CCView {
-    int nop, noc, nfi, nbf, nof, ntot;
-    // geometry (read-only)
-    const double2* pxy;
-    const double2* cen;
-    const double* cv;
-    const double* cov;
-    const int2* fnb;      // (in, out)
-    const int2* fpt;      // (p1, p2)
-    const double2* fn;    // unit normal
-    const double* farea;
-    const double2* fcen;
-    const int* fbc;
-    const double4* lsw;   // LSQ weights (wx0, wy0, wx1, wy1) per face
-    const int* nc2c;
-    const int* cf_off;    // index-sorted faces per cell, SIDE_BIT for `out`
-    const int* cf;
-    const int* rc2f_off;  // reference c2f order (LU-SGS)
-    const int* rc2f;
-    const int* v2c_off;
-    const int* v2c;
-    const double* v2c_wt;
-    // state
-    double4* qc;  // [ntot] E, rho, rho u, rho v
-    double4* qp;  // [ntot] rho, u, v, p
-    double* qT;   // [ntot] T
-    double4* qold;
-    double4* res;
-    double4* res0;
-    double4* restmp;
-    double4* gx;
-    double4* gy;
-    double4* phi;
-    double* dt;
-    double* la;
-    double* mul;
-    double4* pp;
-    double* ppT;
-    double4* fq;
-    double* fqT;
-    double* fla;
-    double* fmu;
-    double4* fF;   // convective face flux (boundary: flux into `in`)
-    double4* fV;   // viscous flux * area
-    double4* fgx;  // diamond-path face gradient, rho,u,v,p
-    double4* fgy;
-    double2* fgT;  // face gradient of T
-    double* fasum; // a1 + a2
-    double2* fwall;   // per boundary face: wall convective (flux3, flux4)
-    double2* fwallv;  // per boundary face: wall viscous (-flux3*A, -flux4*A)
-    double* diag;     // lusgs2 diagonal cv/dt + 0.5*omega*la (lusgs.F90:236)
-    // LU-SGS sweep schedule (host-built): per position of the warp lists
-    // (it, pass, first record, records); per record, in the reference c2f
-    // order of the taken faces: face, neighbour, 1 if the face normal points
-    // into the cell (the sweep then uses -n).
-    const int4* sched;
-    const int* rec_face;
-    const int* rec_nb;
-    const int* rec_flip;
-    int nrec;
-    double4* rec;     // per record, per LU-SGS call: 3 x double4 (k_cc_sweep_prep) or 4 x float4 (k_cc_sweep_prep_mixed)
-    double4* rec_a;   // sweep records [pass * noc + cell]: (u, v, p, e*rho) of qold + dq
-    double4* rec_b;   //   and dq (lower / upper); rho is rebuilt as qold.rho + dq.rho
-    unsigned long long* minmax;  // encoded qmax[4], qmin[4]
-    unsigned long long* dtmin;   // encoded dtglobal
-    double* partial;
-    DevErr* err;
-    // iteration control (graph fast path)
-    const double* cfl_sched;
-    int* iter;
-    int* done;
-    double* fres_hist;
-    double* fres1;
-    // FP32 copies read by the FP32-flux (mixed) form, so that its kernels do
-    // their arithmetic in FP32 without per-value FP64->FP32 conversions
-    // (which issue on the FP64 unit).  Geometry is rounded once from FP64.
-    const float4* fgeof;  // per face: fc - cen[in] (x, y), fc - cen[out] (x, y; 0 on boundary faces)
-    const float4* fnaf;   // per face: nx, ny, area, 0
-    const float4* lswf;   // LSQ weights
-    float4* qpf;          // [ntot] rho, u, v, p (ghost cells: always kept)
-    float4* fqf;          // [nof] face primitives of avg_c2v
-    float* flaf;          // [nof] face spectral radius
-    float4* packf;        // [4 * noc] per cell: primitives, gx, gy, phi
-    Gas g;
-    int grad_type, ilimit, irs, laminar, first_iter;
-    int mixed;            // UNS_PREC_MIXED: keep the FP32 copies, run the FP32 kernels
-    double cfl_max, min_res;
-};
 
 __device__ __forceinline__ bool stopped(const CCView& v) { return v.done != nullptr && *((volatile int*)v.done) != 0; }
 __device__ __forceinline__ double cur_cfl(const CCView& v, double cfl) {
@@ -583,23 +493,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
 // R = double for the FP64 form, float for FP32 face arithmetic.
 template <class R>
 __device__ __forceinline__ bool flux_dispatch(const CCView& v, R nx, R ny, R area, V4<R>& ql, V4<R>& qr, V4<R>& F) {
-    const R G = (R)v.g.gamma, G1 = (R)v.g.gamma1;
-    bool ok = true;
-    R hl, hr;
-    switch (v.g.flux) {
-        case UNS_FLUX_ROE: ok = roe_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
-        case UNS_FLUX_RUSANOV: rusanov_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
-        case UNS_FLUX_VANLEER:
-            vanleer_core<R>(G, G1, nx, ny, ql, qr, F, hl, hr);
-            for (int k = 0; k < 4; ++k) F[k] = F[k] * area;
-            break;
-        default: {  // AUSM+-up: the reference scales by |n| of the unit normal
-            ausm_core<R>(G, G1, nx, ny, (R)v.g.mref, ql, qr, F, hl, hr);
-            R an = sqrt(nx * nx + ny * ny);
-            for (int k = 0; k < 4; ++k) F[k] = F[k] * an;
-        }
-    }
-    return ok;
+    return face_flux<R>(v.g, nx, ny, area, ql, qr, F);
 }
 
 template <class R>
@@ -672,65 +566,22 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
     // boundary face
     int bc = v.fbc[f];
     double d0 = fc.x - ci.x, d1 = fc.y - ci.y;
-    double qcl[4];
+    V4<double> qcl;
 #pragma unroll
     for (int j = 0; j < 4; ++j) qcl[j] = qi[j] + phi_i[j] * (gxi[j] * d0 + gyi[j] * d1);
     const Gas& g = v.g;
     double4 Fd = make_double4(0.0, 0.0, 0.0, 0.0);
-    if (bc == 2001) {
-        V4<double> L = {qcl[0], qcl[1], qcl[2], qcl[3]};
-        V4<double> B = farfield_state<double>(g.gamma, g.gamma1, n.x, n.y, g.r_inf, g.u_inf, g.v_inf, g.p_inf, L);
-        for (int j = 0; j < 4; ++j) { ql[j] = (R)L[j]; qr[j] = (R)B[j]; }
-        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
-        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
-        Fd = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
-        // Ghost state = prim2con of the right state the flux routine left
-        // behind (Rusanov leaves it in conserved form, as in the reference).
-        V4<double> R4 = B;
-        if (g.flux == UNS_FLUX_RUSANOV) for (int j = 0; j < 4; ++j) R4[j] = (double)qr[j];
-        V4<double> C = prim2con<double>(g.gamma, R4);
-        v.qc[out] = make_double4(C[0], C[1], C[2], C[3]);
-        Prim P = con2prim(g, C[0], C[1], C[2], C[3]);
-        v.qp[out] = make_double4(P.rho, P.u, P.v, P.p);
-        v.qT[out] = P.t;
-        v.qpf[out] = make_float4((float)P.rho, (float)P.u, (float)P.v, (float)P.p);
-    } else if (bc == 1001) {
-        double4 c = v.qc[in];
-        Prim P = con2prim(g, c.x, c.y, c.z, c.w);
-        double4 gq;
-        double4 gp;
-        double gT;
-        if (g.flow == UNS_FLOW_INVISCID) {  // slip_wall (boundCond.F90:46-81)
-            double un = P.u * n.x + P.v * n.y;
-            gq = make_double4(c.x, c.y, P.rho * P.u - 2.0 * un * n.x, P.rho * P.v - 2.0 * un * n.y);
-            Prim Q = con2prim(g, gq.x, gq.y, gq.z, gq.w);
-            gp = make_double4(Q.rho, Q.u, Q.v, Q.p);
-            gT = Q.t;
-        } else if (g.iwall == 0) {  // isothermal NoSlip_wall (boundCond.F90:19-30)
-            double tg = 2.0 * g.t_wall - P.t;
-            if (tg <= 0.0) tg = 0.01 * g.t_wall;
-            double rhog = P.p / (P.rho * g.znd);
-            gp = make_double4(rhog, -P.u, -P.v, P.p);
-            gT = tg;
-            V4<double> pr = {gp.x, gp.y, gp.z, gp.w};
-            V4<double> C = prim2con<double>(g.gamma, pr);
-            gq = make_double4(C[0], C[1], C[2], C[3]);
-        } else {  // adiabatic NoSlip_wall (boundCond.F90:31-37)
-            gq = make_double4(c.x, c.y, -c.z, -c.w);
-            Prim Q = con2prim(g, gq.x, gq.y, gq.z, gq.w);
-            gp = make_double4(Q.rho, Q.u, Q.v, Q.p);
-            gT = Q.t;
-        }
-        v.qc[out] = gq;
-        v.qp[out] = gp;
-        v.qT[out] = gT;
-        v.qpf[out] = make_float4((float)gp.x, (float)gp.y, (float)gp.z, (float)gp.w);
-        for (int j = 0; j < 4; ++j) ql[j] = (R)qcl[j];
-        qr[0] = (R)gp.x; qr[1] = (R)gp.y; qr[2] = (R)gp.z; qr[3] = (R)gp.w;
-        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
-        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
-        Fd = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
-        v.fwall[f - v.nfi] = make_double2(Fd.z, Fd.w);
+    if (bc == 2001 || bc == 1001) {
+        V4<double> cin = {0.0, 0.0, 0.0, 0.0};
+        if (bc == 1001) { double4 c = v.qc[in]; cin = V4<double>{c.x, c.y, c.z, c.w}; }
+        CCBnd<double> b = cc_boundary<double, R>(g, bc, n.x, n.y, area, qcl, cin, g.u_inf, g.v_inf);
+        if (!b.ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        Fd = make_double4(b.F[0], b.F[1], b.F[2], b.F[3]);
+        v.qc[out] = make_double4(b.gq[0], b.gq[1], b.gq[2], b.gq[3]);
+        v.qp[out] = make_double4(b.gp[0], b.gp[1], b.gp[2], b.gp[3]);
+        v.qT[out] = b.gT;
+        v.qpf[out] = make_float4((float)b.gp[0], (float)b.gp[1], (float)b.gp[2], (float)b.gp[3]);
+        if (bc == 1001) v.fwall[f - v.nfi] = make_double2(Fd.z, Fd.w);
     }
     v.fF[f] = Fd;
 }
@@ -1350,48 +1201,6 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
 }  // namespace
 
 // ====================================================================== handle
-struct uns_cc_handle {
-    uns_params P;
-    Gas g;
-    CCView v;
-    cudaStream_t stream = nullptr;
-    std::vector<void*> allocs;
-    int nparts = 0;
-    // LU-SGS levels
-    int* woff = nullptr;   // LU-SGS warp schedule: per-warp ranges of v.sched
-    int coop_blocks = 0;
-    double4 qinf;
-    // graph fast path
-    cudaGraphExec_t graph = nullptr;
-    double* d_cfl = nullptr;
-    int cfl_cap = 0;
-    int* d_iter = nullptr;
-    int* d_done = nullptr;
-    double* d_hist = nullptr;
-    double* d_fres1 = nullptr;
-    double* d_scalar = nullptr;  // [4] scratch for host-visible scalars
-    int graph_first = -1;
-    int gen = 0;           // bumped whenever the captured iteration changes (precision, capacity)
-    double cfl_cur = 0.0;  // CFL passed to the last time_step call
-
-    template <class T>
-    int alloc(T*& p, size_t n) {
-        void* q = nullptr;
-        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
-        UNS_CUDA(cudaMalloc(&q, bytes));
-        UNS_CUDA(cudaMemsetAsync(q, 0, bytes, stream));
-        allocs.push_back(q);
-        p = (T*)q;
-        return UNS_OK;
-    }
-    template <class T>
-    int upload(T*& p, const T* src, size_t n) {
-        int rc = alloc(p, n);
-        if (rc) return rc;
-        if (n) UNS_CUDA(cudaMemcpyAsync(p, src, n * sizeof(T), cudaMemcpyHostToDevice, stream));
-        return UNS_OK;
-    }
-};
 
 namespace {
 
@@ -1541,6 +1350,50 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
 }
 
 }  // namespace
+
+namespace uns {
+
+int cc_check_dev_err(uns_cc_handle* h) { return check_dev_err(h); }
+
+// The RK3 main-loop body of enqueue_iteration / enqueue_fvresidual with the
+// limiter frozen (the view's ilimit cleared, so phi keeps its values) and a
+// fixed CFL, calling `hook` where the adjoint records its linearisation
+// points.  Residual smoothing is not part of it (the caller checks that its
+// eps is 0).
+int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx) {
+    CCView v = h->v;
+    v.ilimit = 0;
+    v.cfl_sched = nullptr;
+    v.iter = nullptr;
+    v.done = nullptr;
+    int rc;
+    LAUNCH(k_begin, v.ntot, v, (int)(BEGIN_PRIM | BEGIN_OLD | BEGIN_POS));
+    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH(k_face_prim_spec, v.nof, v);
+    if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
+    LAUNCH(k_cell_grad, v.noc, v, (int)(CG_DT | CG_GRAD), cfl);
+    if ((rc = hook(h, REC_AFTER_START, 0, ctx))) return rc;
+    for (int irk = 1; irk <= 3; ++irk) {
+        if ((rc = hook(h, REC_BEFORE_FACE_CONV, irk, ctx))) return rc;
+        LAUNCH(k_face_conv<double>, v.nof, v);
+        if (v.laminar) {
+            if ((rc = hook(h, REC_BEFORE_CELL_MUL, irk, ctx))) return rc;
+            LAUNCH(k_cell_mul, v.noc, v);
+            if (v.grad_type != UNS_GRAD_GGFC) {
+                CCView w = v;
+                w.grad_type = UNS_GRAD_GGFC;
+                LAUNCH(k_face_ggfc, w.nof, w);
+                LAUNCH(k_cell_grad, w.noc, w, (int)CG_GRAD, cfl);
+            }
+            LAUNCH(k_face_visc, v.nof, v);
+            if ((rc = hook(h, REC_AFTER_FACE_VISC, irk, ctx))) return rc;
+        }
+        LAUNCH(k_cell_res, v.noc, v, irk, 0);
+    }
+    return check_dev_err(h);
+}
+
+}  // namespace uns
 
 // ====================================================================== C-ABI
 extern "C" {
@@ -1752,6 +1605,7 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
 int uns_cc_destroy(uns_cc_handle* h) {
     if (!h) return UNS_OK;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    cc_adj_free(h);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     for (void* p : h->allocs) cudaFree(p);
     if (h->d_cfl) cudaFree(h->d_cfl);
@@ -1842,6 +1696,38 @@ int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
             return UNS_OK;
         }
         default: set_last_error("uns_cc_get_field: unknown field"); return UNS_ERR_ARG;
+    }
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return UNS_OK;
+}
+
+int uns_cc_set_field(uns_cc_handle* h, int field, const double* in) {
+    if (!h || !in) return UNS_ERR_ARG;
+    CCView& v = h->v;
+    switch (field) {
+        case UNS_CC_QC:
+            UNS_CUDA(cudaMemcpyAsync(v.qc, in, sizeof(double4) * v.ntot, cudaMemcpyHostToDevice, h->stream));
+            break;
+        case UNS_CC_QP: {
+            std::vector<double4> A(v.ntot);
+            std::vector<double> B(v.ntot);
+            std::vector<float4> F(v.ntot);
+            for (int i = 0; i < v.ntot; ++i) {
+                const double* o = in + (size_t)i * 5;
+                A[i] = make_double4(o[0], o[1], o[2], o[3]);
+                B[i] = o[4];
+                F[i] = make_float4((float)o[0], (float)o[1], (float)o[2], (float)o[3]);
+            }
+            UNS_CUDA(cudaMemcpyAsync(v.qp, A.data(), sizeof(double4) * v.ntot, cudaMemcpyHostToDevice, h->stream));
+            UNS_CUDA(cudaMemcpyAsync(v.qT, B.data(), sizeof(double) * v.ntot, cudaMemcpyHostToDevice, h->stream));
+            UNS_CUDA(cudaMemcpyAsync(v.qpf, F.data(), sizeof(float4) * v.ntot, cudaMemcpyHostToDevice, h->stream));
+            UNS_CUDA(cudaStreamSynchronize(h->stream));
+            return UNS_OK;
+        }
+        case UNS_CC_PHI:
+            UNS_CUDA(cudaMemcpyAsync(v.phi, in, sizeof(double4) * v.noc, cudaMemcpyHostToDevice, h->stream));
+            break;
+        default: set_last_error("uns_cc_set_field: field cannot be set"); return UNS_ERR_ARG;
     }
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     return UNS_OK;

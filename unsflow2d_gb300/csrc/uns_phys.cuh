@@ -6,6 +6,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "unsflow_types.h"
+
 namespace uns {
 
 template <class R>
@@ -284,6 +286,126 @@ __device__ __forceinline__ V4<R> farfield_state(R G, R G1, R nx, R ny, R rinf, R
         qb[3] = qb[0] * ab * ab / G;
     }
     return qb;
+}
+
+// con2prim on any arithmetic type: the operations of con2prim above, so the
+// double instantiation rounds identically.
+template <class S>
+struct PrimT {
+    S rho, u, v, e, p, t;
+};
+template <class S>
+__device__ __forceinline__ PrimT<S> con2prim_t(const Gas& g, S E, S r, S ru, S rv) {
+    PrimT<S> o;
+    o.rho = r;
+    o.u = ru / r;
+    o.v = rv / r;
+    o.e = E / o.rho;
+    S q = o.u * o.u + o.v * o.v;
+    o.p = (g.gamma - 1.0) * (E - 0.5 * o.rho * q);
+    o.t = o.p / (o.rho * g.znd);
+    return o;
+}
+
+// Conversion between the boundary-state and flux arithmetic types (identity
+// when they agree, a rounding cast between double and float).
+template <class To, class From>
+struct Cvt {
+    __device__ __forceinline__ static To f(From x) { return (To)x; }
+};
+template <class T>
+struct Cvt<T, T> {
+    __device__ __forceinline__ static T f(T x) { return x; }
+};
+
+// Convective flux of the selected scheme (fvresidual.F90 flux selection).
+template <class R>
+__device__ __forceinline__ bool face_flux(const Gas& g, R nx, R ny, R area, V4<R>& ql, V4<R>& qr, V4<R>& F) {
+    const R G = (R)g.gamma, G1 = (R)g.gamma1;
+    bool ok = true;
+    R hl, hr;
+    switch (g.flux) {
+        case UNS_FLUX_ROE: ok = roe_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
+        case UNS_FLUX_RUSANOV: rusanov_flux<R>(G, G1, nx, ny, area, ql, qr, F); break;
+        case UNS_FLUX_VANLEER:
+            vanleer_core<R>(G, G1, nx, ny, ql, qr, F, hl, hr);
+            for (int k = 0; k < 4; ++k) F[k] = F[k] * area;
+            break;
+        default: {  // AUSM+-up: the reference scales by |n| of the unit normal
+            ausm_core<R>(G, G1, nx, ny, (R)g.mref, ql, qr, F, hl, hr);
+            R an = sqrt(nx * nx + ny * ny);
+            for (int k = 0; k < 4; ++k) F[k] = F[k] * an;
+        }
+    }
+    return ok;
+}
+
+// One CCFVM boundary face (fvresidual.F90:27-100): the ghost state of the
+// farfield (farfield_flux, boundCond.F90:112-209) or wall (slip_wall
+// :46-81, NoSlip_wall :2-37) and the face flux between the reconstructed
+// interior state qcl and that ghost.  S is the arithmetic of the states, R of
+// the flux.  The wall ghost reads the current conserved state cin of the
+// interior cell; the farfield ghost depends on uinf, vinf (the angle of
+// attack).  Other bc values carry no flux (F = 0) and no ghost update (upd).
+template <class S>
+struct CCBnd {
+    V4<S> F, gq, gp;
+    S gT;
+    bool ok, upd;
+};
+template <class S, class R>
+__device__ __forceinline__ CCBnd<S> cc_boundary(const Gas& g, int bc, double nx, double ny, double area,
+                                                const V4<S>& qcl, const V4<S>& cin, S uinf, S vinf) {
+    CCBnd<S> o;
+    o.ok = true;
+    o.upd = false;
+    o.F = V4<S>{S(0.0), S(0.0), S(0.0), S(0.0)};
+    o.gq = o.F;
+    o.gp = o.F;
+    o.gT = S(0.0);
+    V4<R> ql, qr, F;
+    if (bc == 2001) {
+        V4<S> B = farfield_state<S>(S(g.gamma), S(g.gamma1), S(nx), S(ny), S(g.r_inf), uinf, vinf, S(g.p_inf), qcl);
+        for (int j = 0; j < 4; ++j) { ql[j] = Cvt<R, S>::f(qcl[j]); qr[j] = Cvt<R, S>::f(B[j]); }
+        o.ok = face_flux<R>(g, (R)nx, (R)ny, (R)area, ql, qr, F);
+        for (int j = 0; j < 4; ++j) o.F[j] = Cvt<S, R>::f(F[j]);
+        // Ghost state = prim2con of the right state the flux routine left
+        // behind (Rusanov leaves it in conserved form, as in the reference).
+        V4<S> R4 = B;
+        if (g.flux == UNS_FLUX_RUSANOV)
+            for (int j = 0; j < 4; ++j) R4[j] = Cvt<S, R>::f(qr[j]);
+        o.gq = prim2con<S>(S(g.gamma), R4);
+        PrimT<S> P = con2prim_t<S>(g, o.gq[0], o.gq[1], o.gq[2], o.gq[3]);
+        o.gp = V4<S>{P.rho, P.u, P.v, P.p};
+        o.gT = P.t;
+        o.upd = true;
+    } else if (bc == 1001) {
+        PrimT<S> P = con2prim_t<S>(g, cin[0], cin[1], cin[2], cin[3]);
+        if (g.flow == UNS_FLOW_INVISCID) {  // slip_wall (boundCond.F90:46-81)
+            S un = P.u * nx + P.v * ny;
+            o.gq = V4<S>{cin[0], cin[1], P.rho * P.u - 2.0 * un * nx, P.rho * P.v - 2.0 * un * ny};
+            PrimT<S> Q = con2prim_t<S>(g, o.gq[0], o.gq[1], o.gq[2], o.gq[3]);
+            o.gp = V4<S>{Q.rho, Q.u, Q.v, Q.p};
+            o.gT = Q.t;
+        } else if (g.iwall == 0) {  // isothermal NoSlip_wall (boundCond.F90:19-30)
+            S tg = 2.0 * g.t_wall - P.t;
+            if (tg <= S(0.0)) tg = S(0.01 * g.t_wall);
+            S rhog = P.p / (P.rho * g.znd);
+            o.gp = V4<S>{rhog, -P.u, -P.v, P.p};
+            o.gT = tg;
+            o.gq = prim2con<S>(S(g.gamma), o.gp);
+        } else {  // adiabatic NoSlip_wall (boundCond.F90:31-37)
+            o.gq = V4<S>{cin[0], cin[1], -cin[2], -cin[3]};
+            PrimT<S> Q = con2prim_t<S>(g, o.gq[0], o.gq[1], o.gq[2], o.gq[3]);
+            o.gp = V4<S>{Q.rho, Q.u, Q.v, Q.p};
+            o.gT = Q.t;
+        }
+        for (int j = 0; j < 4; ++j) { ql[j] = Cvt<R, S>::f(qcl[j]); qr[j] = Cvt<R, S>::f(o.gp[j]); }
+        o.ok = face_flux<R>(g, (R)nx, (R)ny, (R)area, ql, qr, F);
+        for (int j = 0; j < 4; ++j) o.F[j] = Cvt<S, R>::f(F[j]);
+        o.upd = true;
+    }
+    return o;
 }
 
 // Venkatakrishnan limiter function (CCFVM/limiter.F90:286-294)

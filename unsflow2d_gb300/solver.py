@@ -135,6 +135,45 @@ class CCSolver(_Solver):
         self._call("forces", C.byref(fx), C.byref(fy))
         return fx.value, fy.value
 
+    def set(self, field: str, values: np.ndarray) -> None:
+        """Overwrite "qc", "qp" (ghosts included, with T) or "phi"."""
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        assert a.shape == self._field_shape(field), (field, a.shape)
+        self._call("set_field", self.fields[field], _dp(a))
+
+    def cl_cd(self) -> tuple[float, float]:
+        """Flux-based C_L, C_D of the last residual (CCFVM/main.F90:348-353)."""
+        fx, fy = self.forces()
+        a = np.deg2rad(self.params.aoa_deg)
+        return 2.0 * (fy * np.cos(a) - fx * np.sin(a)), 2.0 * (fx * np.cos(a) + fy * np.sin(a))
+
+    # discrete adjoint (no reference counterpart)
+    def adjoint_prepare(self, cfl: float) -> tuple[float, float]:
+        """Record the linearisation at the current (converged) state; returns C_L, C_D."""
+        cl, cd = C.c_double(), C.c_double()
+        self._call("adjoint_prepare", C.c_double(cfl), C.byref(cl), C.byref(cd))
+        return cl.value, cd.value
+
+    def adjoint_vjp(self, objective: str, seed: float, wq: np.ndarray, wg: np.ndarray):
+        """One transposed iteration: returns (G_s^T w + seed J_s^T, G_alpha^T w + seed J_alpha)."""
+        wq = np.ascontiguousarray(wq, dtype=np.float64).reshape(self.noc, 4)
+        wg = np.ascontiguousarray(wg, dtype=np.float64).reshape(self.nbf, 5)
+        oq, og, oa = np.zeros((self.noc, 4)), np.zeros((self.nbf, 5)), C.c_double()
+        self._call("adjoint_vjp", abi.OBJ[objective], C.c_double(seed), _dp(wq), _dp(wg), _dp(oq), _dp(og), C.byref(oa))
+        return oq, og, oa.value
+
+    def adjoint_solve(self, objective: str, max_iter: int = 20000, tol: float = 1e-10):
+        """Reverse accumulation to convergence; returns (dJ/dalpha per radian, change history)."""
+        hist = np.zeros(max_iter)
+        d, it = C.c_double(), C.c_int()
+        self._call("adjoint_solve", abi.OBJ[objective], max_iter, C.c_double(tol), C.byref(d), _dp(hist), C.byref(it))
+        return d.value, hist[:it.value]
+
+    def adjoint_get(self) -> tuple[np.ndarray, np.ndarray]:
+        lq, lg = np.zeros((self.noc, 4)), np.zeros((self.nbf, 5))
+        self._call("adjoint_get", _dp(lq), _dp(lg))
+        return lq, lg
+
     def iteration(self, cfl: float) -> float:
         """One main-loop iteration (CCFVM/main.F90:60-115) through the per-routine entry points."""
         self.con2prim()
