@@ -71,10 +71,56 @@ WORKLOADS = {
                      params=dict(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9,
                                  min_res=0.0, precision="mixed"),
                      desc="as cc with FP32 face reconstruction + flux, FP64 accumulation"),
+    "cc_adjoint": dict(kind="cc", ni=512, nj=256, dwall=2e-5, adjoint=True,
+                       params=dict(m_inf=0.5, aoa_deg=3.0, rey=5000.0, flow="laminar", iwall=0, flux="roe",
+                                   grad="ggfc", time="rk3", cfl_max=0.9, min_res=0.0),
+                       desc="CCFVM laminar Navier-Stokes, Re 5000, M0.5 a3, Pr 0.72, Sutherland, 512x256 O-mesh with "
+                            "2e-5c first wall spacing split to 262,144 triangles, Roe, GG-FC + VKN, RK3, FP64; "
+                            "plus the discrete adjoint's transposed iteration (d C_L / d alpha)"),
 }
 
 # Kernels launched per iteration (our own; memsets excluded).
 LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 12, ("cc", "lusgs"): 12}
+
+
+def cc_launches(p) -> int:
+    """Kernels one CCFVM iteration launches (enqueue_iteration)."""
+    if p.time_mode != abi.TIME["rk3"] or p.flow_type != abi.FLOW["laminar"]:
+        return LAUNCHES[("cc", "rk3" if p.time_mode == abi.TIME["rk3"] else "lusgs")]
+    ggfc = p.grad_type == abi.GRAD["ggfc"]
+    # reset_minmax, begin, vertex_avg, face_prim_spec, [face_ggfc], cell_grad,
+    # 3 x (face_conv, cell_mul, [face_ggfc, (reset_minmax, begin), cell_grad], face_visc, cell_res), res_final
+    per_stage = 4 + (0 if ggfc else 2 + (2 if p.ilimit else 0))
+    return 5 + (1 if ggfc else 0) + 3 * per_stage + 1
+
+
+def adjoint_cost(solver, cfl: float, prof: dict) -> dict:
+    """Device time of one transposed iteration of the discrete adjoint against
+    one forward iteration and one residual evaluation, at the current state
+    and CFL of the run (the per-iteration cost does not depend on convergence)."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cl, cd = solver.adjoint_prepare(cfl)
+    prep = time.perf_counter() - t0
+    solver.adjoint_solve("cl", max_iter=50, tol=0.0)  # warm-up (graph capture path)
+    t = {}
+    for n in (50, 250):
+        t0 = time.perf_counter()
+        solver.adjoint_solve("cl", max_iter=n, tol=0.0)
+        t[n] = time.perf_counter() - t0
+    per = (t[250] - t[50]) / 200 * 1e3
+    fwd = sum(prof.values())
+    stage = sum(prof.get(k, 0.0) for k in ("face_conv", "viscous", "cell_res", "cirs")) / 3.0
+    once = sum(v for k, v in prof.items() if k not in ("face_conv", "viscous", "cell_res", "cirs", "residue"))
+    resid = once + stage
+    return {"ms_per_transposed_iteration": round(per, 4), "ms_per_forward_iteration": round(fwd, 4),
+            "ms_per_residual_evaluation": round(resid, 4),
+            "ratio_to_forward_iteration": round(per / fwd, 3), "ratio_to_residual_evaluation": round(per / resid, 3),
+            "prepare_s": round(prep, 3), "objective": "C_L", "CL": cl, "CD": cd,
+            "timing": "host clock around uns_cc_adjoint_solve graphs of 50 and 250 transposed iterations (difference); "
+                      "forward phases from CUDA events; a residual evaluation = con2prim, averages, gradient once + "
+                      "one stage of flux, viscous flux and gather"}
 
 
 def peaks():
@@ -481,7 +527,8 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
                    "l2": f"inputs larger than L2: ~{ws_mb:.0f} MB of per-iteration arrays vs 129 MB L2, no flush",
                    "setup_s": round(setup_s, 2)},
         "e2e": e2e,
-        "gpu_launches": LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")] * args.steps,
+        "gpu_launches": (cc_launches(p) if kind == "cc" else
+                         LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")]) * args.steps,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -496,6 +543,8 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
         out["cpu_baseline"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
     if accuracy is not None:
         out["accuracy_vs_fp64"] = accuracy
+    if w.get("adjoint"):
+        out["adjoint"] = adjoint_cost(solver, float(cfl_list(p, kind, it + 1, 1)[0]), prof)
     if not args.no_converge:
         out["time_to_1e-8"] = time_to_drop(w)
     return out
