@@ -57,11 +57,18 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
     unsigned long long emn[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
     if (i < v.noc) {
         double4 q = v.qc[i];
-        if (flags & BEGIN_PRIM) {
+        if ((flags & BEGIN_PRIM) && v.mixed) {  // con2prim in FP32 from the rounded state
+            const float E = (float)q.x, r = (float)q.y, ru = (float)q.z, rv = (float)q.w;
+            const float u = ru / r, w = rv / r;
+            const float p = (float)v.g.gamma1 * (E - 0.5f * r * (u * u + w * w));
+            v.qpf[i] = make_float4(r, u, w, p);
+            v.qp[i] = make_double4(r, u, w, p);
+            if (v.laminar || v.grad_type == UNS_GRAD_GGFC) v.qT[i] = (double)(p / (r * (float)v.g.znd));
+            if ((flags & BEGIN_POS) && (r <= 0.f || p <= 0.f)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
+        } else if (flags & BEGIN_PRIM) {
             Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
             v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
             v.qT[i] = P.t;
-            if (v.mixed) v.qpf[i] = make_float4((float)P.rho, (float)P.u, (float)P.v, (float)P.p);
             if ((flags & BEGIN_POS) && (P.rho <= 0.0 || P.p <= 0.0)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
         }
         if (flags & BEGIN_OLD) v.qold[i] = q;
@@ -103,6 +110,27 @@ __global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
     if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nop) return;
+    if (v.mixed) {  // FP32 from the FP32 primitives; FP64 copies only where an FP64 kernel reads them
+        const bool dbl = v.laminar || v.grad_type == UNS_GRAD_GGFC;
+        float wt = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+        double c4 = 0.0;
+        for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
+            const int c = __ldg(&v.v2c[k]);
+            const float w = __ldg(&v.v2c_wtf[k]);
+            const float4 q = v.qpf[c];
+            wt = wt + w;
+            c0 = c0 + q.x * w; c1 = c1 + q.y * w; c2 = c2 + q.z * w; c3 = c3 + q.w * w;
+            if (dbl) c4 = c4 + v.qT[c] * (double)w;
+        }
+        const float r = 1.f / wt;
+        const float4 pp = make_float4(c0 * r, c1 * r, c2 * r, c3 * r);
+        v.ppf[i] = pp;
+        if (dbl) {
+            v.pp[i] = make_double4(pp.x, pp.y, pp.z, pp.w);
+            v.ppT[i] = c4 / (double)wt;
+        }
+        return;
+    }
     double wt = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0;
     for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
         int c = __ldg(&v.v2c[k]);
@@ -125,6 +153,22 @@ __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    if (v.mixed) {  // FP32; the FP64 face radius stays (the LU-SGS prep reads it)
+        const int2 p = v.fpt[f];
+        const float4 a = v.ppf[p.x], b = v.ppf[p.y], na = v.fnaf[f];
+        const float4 q = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z), 0.5f * (a.w + b.w));
+        v.fqf[f] = q;
+        const float a0 = sqrtf((float)v.g.gamma * q.w / q.x);
+        float ll = na.z * (fabsf(q.y * na.x + q.z * na.y) + a0);
+        if (v.laminar) {
+            ll = ll + (float)(v.g.vll * v.fmu[f]) / q.x;
+            v.fq[f] = make_double4(q.x, q.y, q.z, q.w);
+            v.fqT[f] = 0.5 * (v.ppT[p.x] + v.ppT[p.y]);
+        }
+        v.flaf[f] = ll;
+        v.fla[f] = (double)ll;
+        return;
+    }
     int2 p = v.fpt[f];
     double4 a = v.pp[p.x], b = v.pp[p.y];
     double4 q = make_double4(0.5 * (a.x + b.x), 0.5 * (a.y + b.y), 0.5 * (a.z + b.z), 0.5 * (a.w + b.w));
@@ -136,10 +180,6 @@ __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     double ll = v.farea[f] * (fabs(un) + a0);
     ll = ll + v.g.vll * v.fmu[f] / q.x;
     v.fla[f] = ll;
-    if (v.mixed) {
-        v.fqf[f] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
-        v.flaf[f] = (float)ll;
-    }
 }
 
 // Diamond-path face gradient (gradient.F90:474-556, gradtrixy :572-612).
@@ -238,6 +278,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         double cfl = cur_cfl(v, cfl_in);
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
+        v.dcv[i] = dt / v.cv[i];
         v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
         warp_atomic_min_u64(v.dtmin, enc_ord(dt));
     }
@@ -364,9 +405,11 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 
 // k_cell_grad in the mixed form: the same gathers, face orders and formulas
 // with the gradient and the Venkatakrishnan limiter in FP32 on the FP32
-// copies.  dt, la and diag come from the FP32 face radii; the FP64 gx, gy,
-// phi and dt stay the stored state (phi is a running minimum across
-// iterations), and the per-cell pack feeds k_face_conv<float>.
+// copies.  dt, la and diag come from the FP32 face radii.  The per-cell pack
+// (primitives, gradient, phi) is the gradient and limiter state of record in
+// this form (phi is a running minimum across iterations); k_unpack_f32
+// writes it back to the FP64 arrays when a caller reads them or the handle
+// leaves the form.
 __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags, double cfl_in) {
     if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -379,6 +422,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
         const float dt = (float)cur_cfl(v, cfl_in) * cvf / la;
         v.la[i] = (double)la;
         v.dt[i] = (double)dt;
+        v.dcv[i] = (double)(dt / cvf);
         v.diag[i] = (double)(cvf / dt + 0.75f * la);
         warp_atomic_min_u64(v.dtmin, enc_ord((double)dt));
     }
@@ -430,15 +474,13 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
                 }
             }
         }
-        v.gx[i] = make_double4(gx[0], gx[1], gx[2], gx[3]);
-        v.gy[i] = make_double4(gy[0], gy[1], gy[2], gy[3]);
-    } else {  // limiter alone: the stored FP64 gradient
-        const double4 a = v.gx[i], b = v.gy[i];
-        gx[0] = (float)a.x; gx[1] = (float)a.y; gx[2] = (float)a.z; gx[3] = (float)a.w;
-        gy[0] = (float)b.x; gy[1] = (float)b.y; gy[2] = (float)b.z; gy[3] = (float)b.w;
+    } else {  // limiter alone: the gradient of record
+        const float4 a = v.packf[4 * (size_t)i + 1], b = v.packf[4 * (size_t)i + 2];
+        gx[0] = a.x; gx[1] = a.y; gx[2] = a.z; gx[3] = a.w;
+        gy[0] = b.x; gy[1] = b.y; gy[2] = b.z; gy[3] = b.w;
     }
-    const double4 p0 = v.phi[i];
-    float ph[4] = {(float)p0.x, (float)p0.y, (float)p0.z, (float)p0.w};
+    const float4 p0 = v.packf[4 * (size_t)i + 3];
+    float ph[4] = {p0.x, p0.y, p0.z, p0.w};
     if (flags & CG_LIM) {
         float tol[4], umax[4], umin[4];
 #pragma unroll
@@ -480,7 +522,6 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
                 ph[j] = rmin(ph[j], phi0);
             }
         }
-        v.phi[i] = make_double4(ph[0], ph[1], ph[2], ph[3]);
     }
     v.packf[4 * (size_t)i] = q4;
     v.packf[4 * (size_t)i + 1] = make_float4(gx[0], gx[1], gx[2], gx[3]);
@@ -534,10 +575,19 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
     double2 fc = v.fcen[f];
     double2 ci = v.cen[in];
     double qi[4], gxi[4], gyi[4], phi_i[4];
-    d4get(v.qp[in], qi);
-    d4get(v.gx[in], gxi);
-    d4get(v.gy[in], gyi);
-    d4get(v.phi[in], phi_i);
+    if constexpr (std::is_same<R, float>::value) {  // boundary face of the mixed form: the pack of record
+        const float4* A = v.packf + 4 * (size_t)in;
+        const float4 a0 = A[0], a1 = A[1], a2 = A[2], a3 = A[3];
+        qi[0] = a0.x; qi[1] = a0.y; qi[2] = a0.z; qi[3] = a0.w;
+        gxi[0] = a1.x; gxi[1] = a1.y; gxi[2] = a1.z; gxi[3] = a1.w;
+        gyi[0] = a2.x; gyi[1] = a2.y; gyi[2] = a2.z; gyi[3] = a2.w;
+        phi_i[0] = a3.x; phi_i[1] = a3.y; phi_i[2] = a3.z; phi_i[3] = a3.w;
+    } else {
+        d4get(v.qp[in], qi);
+        d4get(v.gx[in], gxi);
+        d4get(v.gy[in], gyi);
+        d4get(v.phi[in], phi_i);
+    }
     V4<R> ql, qr, F;
     if (f < v.nfi) {
         double2 co = v.cen[out];
@@ -656,15 +706,20 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
         v.res[i] = d4(r);
         if (irk > 0) {
             double a = rk3_a(irk), b = rk3_b(irk);
-            double dtbyarea = v.dt[i] / v.cv[i];
+            double dtbyarea = v.dcv[i];  // dt / cv, formed once per time step
             double o[4], c[4], q[4];
-            d4get(v.qold[i], o);
             d4get(v.qc[i], c);
+            if (v.mixed && irk == 1) {  // a = 0, b = 1
 #pragma unroll
-            for (int j = 0; j < 4; ++j) q[j] = a * o[j] + b * (c[j] - dtbyarea * r[j]);
+                for (int j = 0; j < 4; ++j) q[j] = c[j] - dtbyarea * r[j];
+            } else {
+                d4get(v.qold[i], o);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) q[j] = a * o[j] + b * (c[j] - dtbyarea * r[j]);
+            }
             v.qc[i] = d4(q);
         }
-        rr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+        if (partial) rr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
     }
     if (partial) {
         __shared__ double s[kBlock / 32];
@@ -799,7 +854,10 @@ __global__ void k_initialize(CCView v, double4 qinf) {
         v.qc[i] = qinf; v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0;
         v.qpf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    if (i < v.noc) v.phi[i] = make_double4(1.0, 1.0, 1.0, 1.0);
+    if (i < v.noc) {
+        v.phi[i] = make_double4(1.0, 1.0, 1.0, 1.0);
+        v.packf[4 * (size_t)i + 3] = make_float4(1.f, 1.f, 1.f, 1.f);
+    }
 }
 
 // Rebuilds every FP32 copy from the FP64 state, so a handle switched to the
@@ -823,6 +881,22 @@ __global__ void k_mirror_f32(CCView v) {
         v.fqf[i] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
         v.flaf[i] = (float)v.fla[i];
     }
+    if (i < v.nop) {
+        double4 q = v.pp[i];
+        v.ppf[i] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
+    }
+}
+
+// The gradient and phi of record of the mixed form (the per-cell pack)
+// written back to the FP64 arrays.
+__global__ void k_unpack_f32(CCView v) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    const float4* A = v.packf + 4 * (size_t)i;
+    const float4 a = A[1], b = A[2], c = A[3];
+    v.gx[i] = make_double4(a.x, a.y, a.z, a.w);
+    v.gy[i] = make_double4(b.x, b.y, b.z, b.w);
+    v.phi[i] = make_double4(c.x, c.y, c.z, c.w);
 }
 
 // lusgs2 sweeps (lusgs.F90:245-318), one level of the dependency DAG per
@@ -1541,7 +1615,8 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     AL(fwall, nbf); AL(fwallv, nbf);
     AL(diag, noc); AL(rec_a, 2 * (size_t)noc); AL(rec_b, 2 * (size_t)noc);
     UP(fgeof, fgeof); UP(fnaf, fnaf); UP(lswf, lswf);
-    AL(qpf, ntot); AL(fqf, nof); AL(flaf, nof); AL(packf, 4 * (size_t)noc);
+    AL(qpf, ntot); AL(fqf, nof); AL(flaf, nof); AL(packf, 4 * (size_t)noc); AL(ppf, nop); AL(dcv, noc);
+    { std::vector<float> t(m->v2c_wt, m->v2c_wt + m->v2c_off[nop]); UP(v2c_wtf, t); }
     AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
     h->nparts = nblocks(noc);
     AL(partial, h->nparts);
@@ -1643,6 +1718,7 @@ int uns_cc_get_state(uns_cc_handle* h, double* qc) {
 int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
     if (!h || !out) return UNS_ERR_ARG;
     const CCView& v = h->v;
+    if (v.mixed && (field == UNS_CC_GRAD || field == UNS_CC_PHI)) LAUNCH(k_unpack_f32, v.noc, v);
     auto d2h = [&](void* dst, const void* src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
     };
@@ -1725,7 +1801,9 @@ int uns_cc_set_field(uns_cc_handle* h, int field, const double* in) {
             return UNS_OK;
         }
         case UNS_CC_PHI:
+            if (v.mixed) LAUNCH(k_unpack_f32, v.noc, v);
             UNS_CUDA(cudaMemcpyAsync(v.phi, in, sizeof(double4) * v.noc, cudaMemcpyHostToDevice, h->stream));
+            if (v.mixed) LAUNCH(k_mirror_f32, std::max(std::max(v.ntot, v.nof), v.nop), v);
             break;
         default: set_last_error("uns_cc_set_field: field cannot be set"); return UNS_ERR_ARG;
     }
@@ -1939,11 +2017,11 @@ int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (h->P.precision != precision) {
         UNS_CUDA(cudaStreamSynchronize(h->stream));
         h->P.precision = precision;
-        h->v.mixed = precision == UNS_PREC_MIXED;
-        if (h->v.mixed) {
-            CCView& v = h->v;
-            LAUNCH(k_mirror_f32, std::max(v.ntot, v.nof), v);
-        }
+        CCView& v = h->v;
+        const int was_mixed = v.mixed;
+        v.mixed = precision == UNS_PREC_MIXED;
+        if (v.mixed && !was_mixed) LAUNCH(k_mirror_f32, std::max(std::max(v.ntot, v.nof), v.nop), v);
+        if (was_mixed && !v.mixed) LAUNCH(k_unpack_f32, v.noc, v);
         ++h->gen;
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
     }

@@ -98,7 +98,10 @@ struct CCView {
     float4* qpf;          // [ntot] rho, u, v, p (ghost cells: always kept)
     float4* fqf;          // [nof] face primitives of avg_c2v
     float* flaf;          // [nof] face spectral radius
-    float4* packf;        // [4 * noc] per cell: primitives, gx, gy, phi
+    float4* packf;        // [4 * noc] per cell: primitives, gx, gy, phi (the gradient and phi of record in the mixed form)
+    float4* ppf;          // [nop] vertex-averaged primitives
+    const float* v2c_wtf; // pseudo-Laplacian weights
+    double* dcv;          // [noc] dt / cv of the current time step (both forms)
     Gas g;
     int grad_type, ilimit, irs, laminar, first_iter;
     int mixed;            // UNS_PREC_MIXED: keep the FP32 copies, run the FP32 kernels
