@@ -734,6 +734,72 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
     }
 }
 
+// The residual gather of the mixed form: FP64 accumulation of the face
+// fluxes in the cell's face order (the first face initialises the sum), the
+// RK stage with fused multiply-adds, and the FP64 norm partial reduced with
+// one FP64 add per cell before the warp stage (FP64 issue, not bytes, bounds
+// this kernel on GB300).
+__global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, int partial) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0;
+    if (i < v.noc) {
+        const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+        double r[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int k = k0; k < k1; ++k) {
+            const int e = v.cf[k], f = e & FACE_MASK;
+            const double4 F = v.fF[f];
+            const bool neg = f < v.nfi && (e & SIDE_BIT);
+            if (k == k0) {  // sign flip on the bits: no FP64 instruction
+                const long long m = neg ? (long long)0x8000000000000000ULL : 0LL;
+                r[0] = __longlong_as_double(__double_as_longlong(F.x) ^ m);
+                r[1] = __longlong_as_double(__double_as_longlong(F.y) ^ m);
+                r[2] = __longlong_as_double(__double_as_longlong(F.z) ^ m);
+                r[3] = __longlong_as_double(__double_as_longlong(F.w) ^ m);
+            } else {
+                const double s = neg ? -1.0 : 1.0;
+                r[0] = __fma_rn(s, F.x, r[0]); r[1] = __fma_rn(s, F.y, r[1]); r[2] = __fma_rn(s, F.z, r[2]); r[3] = __fma_rn(s, F.w, r[3]);
+            }
+        }
+        if (v.laminar) {
+            for (int k = k0; k < k1; ++k) {
+                const int e = v.cf[k], f = e & FACE_MASK;
+                const double4 V = v.fV[f];
+                const double s = (f < v.nfi && (e & SIDE_BIT)) ? 1.0 : -1.0;
+                r[0] = __fma_rn(s, V.x, r[0]); r[1] = __fma_rn(s, V.y, r[1]); r[2] = __fma_rn(s, V.z, r[2]); r[3] = __fma_rn(s, V.w, r[3]);
+            }
+        }
+        v.res[i] = d4(r);
+        if (irk > 0) {
+            const double D = v.dcv[i];
+            double c[4], q[4];
+            d4get(v.qc[i], c);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) q[j] = __fma_rn(-D, r[j], c[j]);
+            if (irk > 1) {
+                const double a = rk3_a(irk), b = rk3_b(irk);
+                double o[4];
+                d4get(v.qold[i], o);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) q[j] = __fma_rn(a, o[j], b * q[j]);
+            }
+            v.qc[i] = d4(q);
+        }
+        if (partial) rr = __fma_rn(r[3], r[3], __fma_rn(r[2], r[2], __fma_rn(r[1], r[1], r[0] * r[0])));
+    }
+    if (partial) {
+        __shared__ double sh[kBlock];
+        sh[threadIdx.x] = rr;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = sh[threadIdx.x];
+            for (int k = threadIdx.x + 32; k < kBlock; k += 32) t = t + sh[k];
+            t = warp_sum(t);
+            if (threadIdx.x == 0) v.partial[blockIdx.x] = t;
+        }
+    }
+}
+
 // One Jacobi sweep of cirs (ImpResiSmoothening.F90:626-643).
 __global__ void __launch_bounds__(kBlock) k_cirs(CCView v, const double4* src, double4* dst, double eps) {
     if (stopped(v)) return;
@@ -1358,7 +1424,8 @@ int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int par
     // ((0*x + r) * 1 == r for finite x), so they are launched only for eps > 0.
     bool smooth = v.irs && eps > 0.0;
     *fused = !smooth && irk > 0;
-    LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    else LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
     if (smooth) {
         UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
         LAUNCH(k_cirs, v.noc, v, (const double4*)v.res0, v.restmp, eps);
@@ -2206,7 +2273,11 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
                 return UNS_OK;
             });
             int fuse = (rk3 && !smooth) ? irk : 0;
-            if (!rc) rc = timed(7, [&]() -> int { LAUNCH(k_cell_res, v.noc, v, fuse, smooth ? 0 : 1); return UNS_OK; });
+            if (!rc) rc = timed(7, [&]() -> int {
+                if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, smooth ? 0 : 1);
+                else LAUNCH(k_cell_res, v.noc, v, fuse, smooth ? 0 : 1);
+                return UNS_OK;
+            });
             if (!rc && smooth) rc = timed(8, [&]() -> int {
                 UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
                 LAUNCH(k_cirs, v.noc, v, (const double4*)v.res0, v.restmp, eps);
