@@ -132,9 +132,10 @@ def peaks():
 
 
 # ---------------------------------------------------------------- bytes model
-def algorithmic_bytes(kind: str, m: dict) -> dict:
+def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
     """Unique bytes each kernel must move per launch: every array it touches
-    counted once at its full size, no credit for reuse (the design doc table)."""
+    counted once at its full size, no credit for reuse (the design doc table).
+    mixed: the CCFVM mixed form's kernels, which read FP32 copies."""
     if kind == "nc":
         N, E = m["nop"], m["nof"]
         B = int((m["fbc"] != 0).sum())
@@ -154,6 +155,25 @@ def algorithmic_bytes(kind: str, m: dict) -> dict:
         }
     N, F, P = m["noc"], m["nfi"] + m["nbf"], m["nop"]
     G = m["nbf"]
+    if mixed:
+        nnz = len(m["v2c"])
+        return {
+            # qc read; qold, qpf, qp written; ghost qp read for the limiter range
+            "begin": 32 * N + 32 * N + 16 * N + 32 * N + 32 * G,
+            # offsets, (cell, FP32 weight) per entry, FP32 primitives, FP32 vertex values
+            "vertex_avg": 4 * P + 8 * nnz + 16 * (N + G) + 16 * P,
+            # points, FP32 vertex values, FP32 normal+length; FP32 face values + radius, FP64 radius
+            "face_prim_spec": 8 * F + 16 * P + 16 * F + 16 * F + 4 * F + 8 * F,
+            # face lists, FP32 radii / normals / face values / offsets, neighbours, cv; la, dt, dt/cv, diag;
+            # FP32 primitives; pack (phi read, 64 B written)
+            "cell_grad": 4 * N + 8 * F + 4 * F + 16 * F + 16 * F + 16 * F + 8 * F + 8 * N + 32 * N + 16 * N + 16 * N + 64 * N,
+            # neighbours, FP32 offsets + normal/length, two 64-byte packs (each cell once), FP64 flux written;
+            # boundary: ghost writes and wall force
+            "face_conv": 8 * F + 32 * F + 64 * N + 32 * F + 72 * G,
+            # face lists, FP64 fluxes, qc read+write, qold, res, dt/cv
+            "cell_res": 16 * N + 32 * F + 32 * N * 4 + 8 * N,
+            "residue": 8 * ((N + 255) // 256),
+        }
     return {
         "begin": 32 * N + 32 * N + 8 * N + 32 * N + 40 * G,
         "vertex_avg": 40 * (N + G) + 4 * P + 12 * len(m["v2c"]) + 40 * P,
@@ -171,8 +191,10 @@ def algorithmic_bytes(kind: str, m: dict) -> dict:
 # a quarter-size case (reads grow in proportion to the units; see the
 # summaries under profiles/): scaled here to the benchmark's size.
 TRAFFIC_PER_UNIT = {
-    ("nc", "lusgs_sweeps"): (103.81e6 / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
-    ("cc", "face_conv"): (57.09e6 / 393728, "faces", "profiles/cc_face_conv_512x256_full.md"),
+    ("nc", "lusgs_sweeps", False): (103.81e6 / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
+    ("cc", "face_conv", False): (57.09e6 / 393728, "faces", "profiles/cc_face_conv_512x256_full.md"),
+    ("cc", "face_conv", True): (156.69e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
+    ("cc", "cell_res", True): (178.49e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
 }
 
 
@@ -368,7 +390,7 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     tot_w, secs_w = replicas.reduce_timing(dist, cells * args.steps, wall, device=str(dev))
     nbytes = 0
     for m in meshes:
-        b = algorithmic_bytes("cc", m.arrays)
+        b = algorithmic_bytes("cc", m.arrays, True)
         nl = launches_per_iter("cc", True, False)
         nbytes += sum(v * max(nl.get(k, 1), 1) for k, v in b.items() if k not in ("face_ggfc", "residue"))
     achieved = nbytes / (ms / 1e3 / args.steps) / 1e9
@@ -495,7 +517,8 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
 
     # Per-kernel device times (CUDA events on the library stream) -> roofline.
     prof = solver.profile(float(cfl_list(p, kind, it + 1, 1)[0]), reps=3)
-    nbytes = algorithmic_bytes(kind, m.arrays)
+    mixed_cc = kind == "cc" and p.precision == abi.PREC["mixed"]
+    nbytes = algorithmic_bytes(kind, m.arrays, mixed_cc)
     peak, peak_src = peaks()
     dom = max(prof, key=prof.get)
     nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"])
@@ -506,7 +529,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
                    "alg_MB_per_launch": round(nbytes.get(k, 0) / 1e6, 2),
                    "GBps": round(nbytes[k] / (per_launch[k] * 1e-3) / 1e9, 1) if k in nbytes and v > 0 else None}
                for k, v in prof.items()}
-    tr = TRAFFIC_PER_UNIT.get((kind, rl_kernel))
+    tr = TRAFFIC_PER_UNIT.get((kind, rl_kernel, mixed_cc))
     traffic = None
     if tr is not None:
         nunits = m["nop"] if tr[1] == "nodes" else (m["nfi"] + m["nbf"] if tr[1] == "faces" else m["noc"])
