@@ -94,7 +94,7 @@ def cc_launches(p) -> int:
     return 5 + (1 if ggfc else 0) + 3 * per_stage + 1
 
 
-def adjoint_cost(solver, cfl: float, prof: dict) -> dict:
+def adjoint_cost(solver, w: dict, cfl: float, prof: dict) -> dict:
     """Device time of one transposed iteration of the discrete adjoint against
     one forward iteration and one residual evaluation, at the current state
     and CFL of the run (the per-iteration cost does not depend on convergence)."""
@@ -110,6 +110,16 @@ def adjoint_cost(solver, cfl: float, prof: dict) -> dict:
         solver.adjoint_solve("cl", max_iter=n, tol=0.0)
         t[n] = time.perf_counter() - t0
     per = (t[250] - t[50]) / 200 * 1e3
+    # dC_L / d(wall-node y) of all wall nodes and the 16 Hicks-Henne amplitudes:
+    # one-iteration geometry partials on 16 displaced meshes, weighted by the
+    # adjoint vector (unsflow2d_gb300.shape)
+    from unsflow2d_gb300 import shape
+    lq, lg = solver.adjoint_get()
+    case = shape.ShapeCase(w["ni"], w["nj"], w["params"], (solver.get_state(), solver.get("qp"), solver.get("phi")), cfl,
+                           mesh_kw=dict(dwall=w["dwall"]))
+    t0 = time.perf_counter()
+    bumps = case.bump_gradient("cl", lq, lg)
+    shape_s = time.perf_counter() - t0
     fwd = sum(prof.values())
     stage = sum(prof.get(k, 0.0) for k in ("face_conv", "viscous", "cell_res", "cirs")) / 3.0
     once = sum(v for k, v in prof.items() if k not in ("face_conv", "viscous", "cell_res", "cirs", "residue"))
@@ -118,6 +128,7 @@ def adjoint_cost(solver, cfl: float, prof: dict) -> dict:
             "ms_per_residual_evaluation": round(resid, 4),
             "ratio_to_forward_iteration": round(per / fwd, 3), "ratio_to_residual_evaluation": round(per / resid, 3),
             "prepare_s": round(prep, 3), "objective": "C_L", "CL": cl, "CD": cd,
+            "shape_gradient_s": round(shape_s, 2), "n_bumps": int(len(bumps)), "wall_nodes": int(w["ni"]),
             "timing": "host clock around uns_cc_adjoint_solve graphs of 50 and 250 transposed iterations (difference); "
                       "forward phases from CUDA events; a residual evaluation = con2prim, averages, gradient once + "
                       "one stage of flux, viscous flux and gather"}
@@ -567,7 +578,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     if accuracy is not None:
         out["accuracy_vs_fp64"] = accuracy
     if w.get("adjoint"):
-        out["adjoint"] = adjoint_cost(solver, float(cfl_list(p, kind, it + 1, 1)[0]), prof)
+        out["adjoint"] = adjoint_cost(solver, w, float(cfl_list(p, kind, it + 1, 1)[0]), prof)
     if not args.no_converge:
         out["time_to_1e-8"] = time_to_drop(w)
     return out

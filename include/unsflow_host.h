@@ -28,6 +28,13 @@ const char* uns_host_last_error(void);
  * about mid-chord; geometric radial spacing from dwall at the wall. */
 int uns_host_cc_airfoil(int ni, int nj, double thickness, double rfar, double dwall, uns_host_cc** out);
 int uns_host_nc_airfoil(int ni, int nj, double thickness, double rfar, double dwall, uns_host_nc** out);
+/* The CCFVM airfoil mesh with wall node i (the point of index i, at the
+ * surface parameter 2 pi i / ni from the trailing edge over the upper
+ * surface) displaced by dy[i] in y, its radial line following with weight
+ * 1 - s (s = 0 at the wall, 1 at the farfield): the shape perturbations of
+ * the adjoint's wall-node and Hicks-Henne derivatives. */
+int uns_host_cc_airfoil_dy(int ni, int nj, double thickness, double rfar, double dwall, const double* dy,
+                           uns_host_cc** out);
 /* geometry.inp readers (CCFVM/read_input.F90:123-213, NCFVM/read_input.f90:
  * 479-512) followed by geometric. */
 int uns_host_cc_read(const char* path, uns_host_cc** out);

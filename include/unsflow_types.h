@@ -77,7 +77,10 @@ enum {
     UNS_CC_FLA = 10,   /* [nfi+nbf]     face spectral radius                 */
     UNS_CC_FMU = 11,   /* [nfi+nbf]     face viscosity                       */
     UNS_CC_FGRAD = 12, /* [nfi+nbf][5][2] diamond-path face gradients        */
-    UNS_CC_MUL = 13    /* [noc]         Sutherland viscosity                 */
+    UNS_CC_MUL = 13,   /* [noc]         Sutherland viscosity                 */
+    UNS_CC_FWALL = 14  /* [nbf][4]      wall force terms of the last residual:
+                        *               convective (x, y), viscous (x, y);
+                        *               Fx1 = sum(conv x - visc x) over walls */
 };
 enum {
     UNS_NC_QC = 0,     /* [nop][4] */

@@ -31,7 +31,7 @@ PREC = {"fp64": 0, "mixed": 1, "mixed_sweep": 2}
 OBJ = {"cl": 0, "cd": 1}
 
 CC_FIELDS = {"qc": 0, "qp": 1, "qold": 2, "res": 3, "grad": 4, "phi": 5, "dt": 6, "la": 7,
-             "ptprim": 8, "fqp": 9, "fla": 10, "fmu": 11, "fgrad": 12, "mul": 13}
+             "ptprim": 8, "fqp": 9, "fla": 10, "fmu": 11, "fgrad": 12, "mul": 13, "fwall": 14}
 NC_FIELDS = {"qc": 0, "qp": 1, "qold": 2, "res": 3, "grad": 4, "phi": 5, "dt": 6, "la": 7, "fla": 8}
 
 
@@ -236,6 +236,7 @@ def host_lib() -> C.CDLL:
         sig = {
             "uns_host_last_error": ([], C.c_char_p),
             "uns_host_cc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),
+            "uns_host_cc_airfoil_dy": ([i32, i32, dp, dp, dp, _D, pp], i32),
             "uns_host_nc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),
             "uns_host_cc_read": ([C.c_char_p, pp], i32), "uns_host_nc_read": ([C.c_char_p, pp], i32),
             "uns_host_cc_write": ([vp, C.c_char_p], i32), "uns_host_nc_write": ([vp, C.c_char_p], i32),

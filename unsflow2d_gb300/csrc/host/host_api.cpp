@@ -67,6 +67,18 @@ int uns_host_cc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns
     return UNS_OK;
 }
 
+int uns_host_cc_airfoil_dy(int ni, int nj, double t, double rfar, double dwall, const double* dy, uns_host_cc** out) {
+    if (!out) return fail(UNS_ERR_ARG, "null out");
+    AirfoilSpec s{ni, nj, t, rfar, dwall, dy};
+    auto* m = new uns_host_cc();
+    std::string err;
+    int rc = gen_airfoil_cc(s, m->raw, err);
+    if (!rc) rc = geometric_cc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
 int uns_host_nc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns_host_nc** out) {
     if (!out) return fail(UNS_ERR_ARG, "null out");
     AirfoilSpec s{ni, nj, t, rfar, dwall};

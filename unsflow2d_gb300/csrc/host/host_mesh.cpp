@@ -81,6 +81,7 @@ int build_ogrid(const AirfoilSpec& s, OGrid& g, std::string& err) {
             else frac = ((std::pow(q, j) - 1.0) / (q - 1.0)) / qJ;
             g.x[(size_t)j * I + i] = xw + (xf - xw) * frac;
             g.y[(size_t)j * I + i] = yw + (yf - yw) * frac;
+            if (s.dy) g.y[(size_t)j * I + i] = g.y[(size_t)j * I + i] + s.dy[i] * (1.0 - frac);
         }
     }
     return UNS_OK;

@@ -77,6 +77,11 @@ struct AirfoilSpec {
     double thickness = 0.12;     // symmetric 4-digit thickness / chord
     double rfar = 20.0;          // farfield radius [chord]
     double dwall = 1e-3;         // first radial spacing at the wall [chord]
+    // Optional wall-node y displacements [ni] (shape perturbations): node i
+    // of the wall moves by dy[i] and the points of its radial line follow
+    // with weight 1 - s, s the line's fractional arc position (0 at the
+    // wall, 1 at the farfield), so the farfield stays fixed.
+    const double* dy = nullptr;
 };
 
 // Analytic airfoil O-mesh, quads split into two triangles.

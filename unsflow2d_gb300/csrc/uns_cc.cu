@@ -1814,6 +1814,17 @@ int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
         case UNS_CC_MUL: UNS_CUDA(d2h(out, v.mul, sizeof(double) * v.noc)); break;
         case UNS_CC_PTPRIM: return interleave(v.pp, v.ppT, v.nop, 5);
         case UNS_CC_FQP: return interleave(v.fq, v.fqT, v.nof, 5);
+        case UNS_CC_FWALL: {
+            std::vector<double2> A(v.nbf), B(v.nbf);
+            UNS_CUDA(d2h(A.data(), v.fwall, sizeof(double2) * v.nbf));
+            UNS_CUDA(d2h(B.data(), v.fwallv, sizeof(double2) * v.nbf));
+            UNS_CUDA(cudaStreamSynchronize(h->stream));
+            for (int b = 0; b < v.nbf; ++b) {
+                out[4 * (size_t)b] = A[b].x; out[4 * (size_t)b + 1] = A[b].y;
+                out[4 * (size_t)b + 2] = v.laminar ? B[b].x : 0.0; out[4 * (size_t)b + 3] = v.laminar ? B[b].y : 0.0;
+            }
+            return UNS_OK;
+        }
         case UNS_CC_GRAD: {
             std::vector<double4> X(v.noc), Y(v.noc);
             UNS_CUDA(d2h(X.data(), v.gx, sizeof(double4) * v.noc));

@@ -67,6 +67,17 @@ class CCMesh(_HostMesh):
     """Cell-centred mesh (CCFVM geometry.inp + CCFVM/geometric.F90)."""
     kind = "cc"
 
+    @classmethod
+    def airfoil_dy(cls, ni: int, nj: int, dy, thickness: float = 0.12, rfar: float = 20.0, dwall: float = 1e-3):
+        """The airfoil mesh with wall node i displaced by dy[i] in y (radial lines follow)."""
+        lib = abi.host_lib()
+        h = C.c_void_p()
+        d = np.ascontiguousarray(dy, dtype=np.float64)
+        assert d.shape == (ni,)
+        abi.check(lib.uns_host_cc_airfoil_dy(ni, nj, thickness, rfar, dwall, d.ctypes.data_as(C.POINTER(C.c_double)),
+                                             C.byref(h)), lib, "cc airfoil dy")
+        return cls(h.value)
+
     @property
     def ncells(self) -> int:
         return self.arrays["noc"]

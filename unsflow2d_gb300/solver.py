@@ -103,7 +103,7 @@ class CCSolver(_Solver):
         return {"qc": (self.nstate, 4), "qp": (self.nstate, 5), "qold": (self.noc, 4), "res": (self.noc, 4),
                 "grad": (self.noc, 4, 2), "phi": (self.noc, 4), "dt": (self.noc,), "la": (self.noc,),
                 "ptprim": (m["nop"], 5), "fqp": (nof, 5), "fla": (nof,), "fmu": (nof,),
-                "fgrad": (nof, 5, 2), "mul": (self.noc,)}[f]
+                "fgrad": (nof, 5, 2), "mul": (self.noc,), "fwall": (self.nbf, 4)}[f]
 
     # one method per reference subroutine
     def con2prim(self): self._call("con2prim")
