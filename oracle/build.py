@@ -15,8 +15,8 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent
 OUT = HERE / "_build" / "liboracle.so"
-SOURCES = [HERE / "oracle_cc.cpp", HERE / "oracle_nc.cpp"]
-DEPS = SOURCES + [HERE / "oracle.h", ROOT / "include" / "unsflow_types.h", Path(__file__)]
+SOURCES = [HERE / "oracle_cc.cpp", HERE / "oracle_cc_cs.cpp", HERE / "oracle_nc.cpp"]
+DEPS = SOURCES + [HERE / "oracle_cc_body.inc", HERE / "oracle.h", ROOT / "include" / "unsflow_types.h", Path(__file__)]
 
 
 def build(force: bool = False) -> Path:

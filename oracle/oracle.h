@@ -47,6 +47,22 @@ int oracle_cc_get(oracle_cc* o, int field, double* out);
 /* Test hook: overwrite QC, QP (all cells incl. ghosts), GRAD or PHI. */
 int oracle_cc_set(oracle_cc* o, int field, const double* in);
 
+/* Complex-step instance of the CCFVM oracle (oracle_cc_cs.cpp): the same
+ * routines on a complex scalar whose branches follow the real part.  Inputs
+ * carry re + i*im; for im = h*u with h ~ 1e-30, Im(output)/h is the exact
+ * directional derivative.  aoa_im adds i*aoa_im to the angle of attack (rad). */
+typedef struct oracle_cc_cs oracle_cc_cs;
+oracle_cc_cs* oracle_cc_cs_create(const uns_cc_mesh* m, const uns_params* p, double aoa_im);
+void oracle_cc_cs_free(oracle_cc_cs* o);
+/* UNS_CC_QC [noc+nbf][4], UNS_CC_QP [noc+nbf][5], UNS_CC_PHI [noc][4]; im may be NULL. */
+int oracle_cc_cs_set(oracle_cc_cs* o, int field, const double* re, const double* im);
+/* UNS_CC_QC or UNS_CC_QP. */
+int oracle_cc_cs_get(oracle_cc_cs* o, int field, double* re, double* im);
+/* One RK3 main-loop iteration (as oracle_cc_iteration, without the norm). */
+int oracle_cc_cs_iteration(oracle_cc_cs* o, double cfl);
+/* Fx1, Fy1 of the last residual: fx[0] + i fx[1], fy[0] + i fy[1]. */
+int oracle_cc_cs_forces(oracle_cc_cs* o, double* fx, double* fy);
+
 /* ------------------------------------------------------------ NCFVM */
 oracle_nc* oracle_nc_create(const uns_nc_mesh* m, const uns_params* p);
 void oracle_nc_free(oracle_nc* o);

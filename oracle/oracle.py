@@ -48,6 +48,10 @@ def lib() -> C.CDLL:
             "oracle_nc_fvresidual": ([vp, C.c_double], i32), "oracle_nc_rk_stage": ([vp, i32], i32),
             "oracle_nc_lusgs": ([vp, C.c_double], i32), "oracle_nc_residue": ([vp, dp, dp, ip], i32),
             "oracle_nc_iteration": ([vp, C.c_double, dp, dp], i32), "oracle_nc_get": ([vp, i32, dp], i32),
+            "oracle_cc_cs_create": ([C.POINTER(abi.CCMeshView), C.POINTER(abi.Params), C.c_double], vp),
+            "oracle_cc_cs_free": ([vp], None), "oracle_cc_cs_set": ([vp, i32, dp, dp], i32),
+            "oracle_cc_cs_get": ([vp, i32, dp, dp], i32), "oracle_cc_cs_iteration": ([vp, C.c_double], i32),
+            "oracle_cc_cs_forces": ([vp, dp, dp], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(L, fn)
@@ -197,3 +201,51 @@ class OracleNC(_Oracle):
         f, fi = C.c_double(), C.c_double()
         self._call("iteration", C.c_double(cfl), C.byref(f), C.byref(fi))
         return f.value, fi.value
+
+
+class OracleCCComplexStep:
+    """The CCFVM oracle on complex-step numbers (oracle_cc_cs.cpp): one main-loop
+    iteration from a state x + i*im, returning real and imaginary parts.  With
+    im = h*u (h ~ 1e-30) Im(G)/h is the exact derivative of the iteration in
+    direction u; aoa_im perturbs the angle of attack (radians) the same way."""
+
+    def __init__(self, mesh, params, aoa_im: float = 0.0):
+        self._L = lib()
+        arr = mesh.arrays if hasattr(mesh, "arrays") else mesh
+        view, self._keep = abi.cc_view_from_arrays(arr)
+        self._h = self._L.oracle_cc_cs_create(C.byref(view), C.byref(params), C.c_double(aoa_im))
+        self.noc, self.nbf = arr["noc"], arr["nbf"]
+        self.nstate = self.noc + self.nbf
+
+    def set(self, field: str, re: np.ndarray, im: np.ndarray | None = None) -> None:
+        re = np.ascontiguousarray(re, dtype=np.float64)
+        im = np.zeros_like(re) if im is None else np.ascontiguousarray(im, dtype=np.float64)
+        if self._L.oracle_cc_cs_set(self._h, abi.CC_FIELDS[field], _dp(re), _dp(im)):
+            raise OracleError(f"oracle_cc_cs_set {field}")
+
+    def get(self, field: str) -> np.ndarray:
+        shape = (self.nstate, 4) if field == "qc" else (self.nstate, 5)
+        re, im = np.zeros(shape), np.zeros(shape)
+        if self._L.oracle_cc_cs_get(self._h, abi.CC_FIELDS[field], _dp(re), _dp(im)):
+            raise OracleError(f"oracle_cc_cs_get {field}")
+        return re + 1j * im
+
+    def iteration(self, cfl: float) -> None:
+        if self._L.oracle_cc_cs_iteration(self._h, C.c_double(cfl)):
+            raise OracleError("oracle_cc_cs_iteration")
+
+    def forces(self) -> tuple[complex, complex]:
+        fx, fy = np.zeros(2), np.zeros(2)
+        self._L.oracle_cc_cs_forces(self._h, _dp(fx), _dp(fy))
+        return complex(fx[0], fx[1]), complex(fy[0], fy[1])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.oracle_cc_cs_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

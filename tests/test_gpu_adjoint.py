@@ -8,6 +8,9 @@ GPU forward iteration itself (same limiter frozen at the converged phi):
 * one transposed iteration: <w, dG/ds u> + seed <dJ/ds, u> (central difference,
   step 1e-6 relative per entry) equals <G_s^T w + seed J_s^T, u> for random
   w, u, and likewise for the angle of attack;
+* the same transposed iteration against complex-step derivatives (step
+  1e-30 i) of one iteration of the CPU oracle's complex-step instance at the
+  converged state, which have no cancellation error: agreement to 1e-8;
 * the total derivative dJ/dalpha of the adjoint solve equals the central
   difference of J between two solutions re-converged at alpha +- 5e-4 deg.
 
@@ -163,3 +166,55 @@ def test_total_derivative_matches_reconverged_differences(name):
         d, hist = a.adjoint_solve(obj, max_iter=300000, tol=1e-12)
         assert len(hist) < 300000 and np.isfinite(d)
         assert abs(d - fd) <= 2e-5 * abs(fd), (obj, d, fd)
+
+
+@pytest.mark.parametrize("name", ["euler_roe_gg", "laminar_roe_ggfc_iso"])
+def test_vjp_matches_complex_step(name):
+    from oracle import OracleCCComplexStep
+    m, kw, f, state, _, _ = _base(name)
+    noc, nbf = f.noc, f.nbf
+    qc, qp, phi = state
+    rng = np.random.default_rng(11)
+    uq = rng.standard_normal((noc, 4)) * np.abs(qc[:noc])
+    ug = rng.standard_normal((nbf, 5)) * np.abs(qp[noc:])
+    wq = rng.standard_normal((noc, 4))
+    wg = rng.standard_normal((nbf, 5))
+    seed = 0.7
+    p = abi.make_params(ilimit=0, min_res=1e-30, **kw)
+    H = 1e-30
+
+    def cs_step(dq=None, dg=None, aoa_im=0.0):
+        o = OracleCCComplexStep(m, p, aoa_im)
+        o.set("phi", phi)
+        o.set("qc", qc)
+        o.set("qp", qp)
+        o.iteration(CFL)  # sets the face viscosity that the next time step reads
+        o.set("qc", qc, dq)
+        o.set("qp", qp, dg)
+        o.iteration(CFL)
+        return o.get("qc")[:noc], o.get("qp")[noc:], o.forces()
+
+    def coefficients(fx, fy, a):
+        return {"cl": 2 * (fy * np.cos(a) - fx * np.sin(a)), "cd": 2 * (fx * np.cos(a) + fy * np.sin(a))}
+
+    a = _frozen(m, kw)
+    _load(a, state)
+    a.adjoint_prepare(CFL)
+    alpha = np.deg2rad(kw["aoa_deg"])
+    dq = np.zeros_like(qc)
+    dq[:noc] = H * uq
+    dg = np.zeros_like(qp)
+    dg[noc:] = H * ug
+    cq, cg, (fx, fy) = cs_step(dq, dg)
+    J = coefficients(fx, fy, alpha)
+    for obj in ("cl", "cd"):
+        lhs = (np.sum(wq * cq.imag) + np.sum(wg * cg.imag) + seed * J[obj].imag) / H
+        oq, og, _ = a.adjoint_vjp(obj, seed, wq, wg)
+        rhs = np.sum(oq * uq) + np.sum(og * ug)
+        assert abs(lhs - rhs) <= 1e-8 * abs(lhs), (obj, lhs, rhs)
+    cq, cg, (fx, fy) = cs_step(aoa_im=H)
+    J = coefficients(fx, fy, alpha + 1j * H)
+    for obj in ("cl", "cd"):
+        lhs = (np.sum(wq * cq.imag) + np.sum(wg * cg.imag) + seed * J[obj].imag) / H
+        _, _, oa = a.adjoint_vjp(obj, seed, wq, wg)
+        assert abs(lhs - oa) <= 1e-8 * abs(lhs), (obj, lhs, oa)
