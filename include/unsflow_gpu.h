@@ -79,6 +79,17 @@ int uns_cc_residue(uns_cc_handle* h, double* fres_raw);
 /* Flux-based wall forces Fx1, Fy1 of the last fvresidual
  * (CCFVM/fvresidual.F90:99-100, CCFVM/viscous_flux.F90:530-533). */
 int uns_cc_forces(uns_cc_handle* h, double* fx1, double* fy1);
+/* find_cl_cd (CCFVM/main.F90:263-355) on the device, from the last residual:
+ * coef[0..4] = C_L, C_D of the pressure + viscous wall integral, C_m about
+ * (xref, yref) (flo.inp's reference point), and C_L, C_D of the flux-based
+ * Fx1, Fy1.  wall (may be NULL; room for nbf rows) receives per wall face, in
+ * face order, the row x, y, -C_p, C_f that the reference writes to
+ * XYCpCf.dat; *nwall (may be NULL) their count. */
+int uns_cc_find_cl_cd(uns_cc_handle* h, double xref, double yref, double* coef, double* wall, int* nwall);
+/* screen's min/max diagnostics (CCFVM/main.F90:187-221) over the interior
+ * cells from the current state: out[2k], out[2k+1] = min, max of density, u,
+ * v, pressure, temperature, Mach number, entropy log10(p / rho^gamma / ent_inf). */
+int uns_cc_screen_minmax(uns_cc_handle* h, double* out);
 /* Fast path: `niter` whole iterations of the main loop body
  * (CCFVM/main.F90:59-115) replayed from one captured CUDA graph.  cfl[k] is
  * the CFL of iteration k; fres_raw[k] receives that iteration's raw residual

@@ -46,6 +46,11 @@ int oracle_cc_iteration(oracle_cc* o, double cfl, double* fres_raw);
 int oracle_cc_get(oracle_cc* o, int field, double* out);
 /* Test hook: overwrite QC, QP (all cells incl. ghosts), GRAD or PHI. */
 int oracle_cc_set(oracle_cc* o, int field, const double* in);
+/* find_cl_cd (main.F90:263-355): coef[5] = C_L, C_D (wall integral), C_m,
+ * C_L, C_D (flux-based); wall [nwall][4] = x, y, -cp, cf (may be NULL). */
+int oracle_cc_find_cl_cd(oracle_cc* o, double xref, double yref, double* coef, double* wall, int* nwall);
+/* screen's min/max diagnostics (main.F90:187-221): out[14]. */
+int oracle_cc_screen_minmax(oracle_cc* o, double* out);
 
 /* Complex-step instance of the CCFVM oracle (oracle_cc_cs.cpp): the same
  * routines on a complex scalar whose branches follow the real part.  Inputs

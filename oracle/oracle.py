@@ -52,6 +52,8 @@ def lib() -> C.CDLL:
             "oracle_cc_cs_free": ([vp], None), "oracle_cc_cs_set": ([vp, i32, dp, dp], i32),
             "oracle_cc_cs_get": ([vp, i32, dp, dp], i32), "oracle_cc_cs_iteration": ([vp, C.c_double], i32),
             "oracle_cc_cs_forces": ([vp, dp, dp], i32),
+            "oracle_cc_find_cl_cd": ([vp, C.c_double, C.c_double, dp, dp, ip], i32),
+            "oracle_cc_screen_minmax": ([vp, dp], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(L, fn)
@@ -131,6 +133,16 @@ class OracleCC(_Oracle):
                 "grad": (self.noc, 4, 2), "phi": (self.noc, 4), "dt": (self.noc,), "la": (self.noc,),
                 "ptprim": (m["nop"], 5), "fqp": (nof, 5), "fla": (nof,), "fmu": (nof,),
                 "fgrad": (nof, 5, 2), "mul": (self.noc,)}[f]
+
+    def find_cl_cd(self, xref=0.25, yref=0.0):
+        coef, wall, n = np.zeros(5), np.zeros((self.nbf, 4)), C.c_int()
+        self._call("find_cl_cd", C.c_double(xref), C.c_double(yref), _dp(coef), _dp(wall), C.byref(n))
+        return coef, wall[:n.value]
+
+    def screen_minmax(self):
+        out = np.zeros(14)
+        self._call("screen_minmax", _dp(out))
+        return out.reshape(7, 2)
 
     def con2prim(self): self._call("con2prim")
     def avg_c2v(self): self._call("avg_c2v")

@@ -19,6 +19,7 @@ using R = double;
 using std::atan;
 using std::cos;
 using std::fabs;
+using std::log10;
 using std::max;
 using std::min;
 using std::pow;
@@ -151,6 +152,19 @@ int oracle_cc_set(oracle_cc* o, int field, const double* in) {
             break;
         default: return UNS_ERR_ARG;
     }
+    return UNS_OK;
+}
+
+int oracle_cc_find_cl_cd(oracle_cc* o, double xref, double yref, double* coef, double* wall, int* nwall) {
+    std::vector<double> w((size_t)o->s.nbf * 4);
+    int n = cc_find_cl_cd(o->s, xref, yref, coef, w.data());
+    if (wall) std::copy(w.begin(), w.begin() + (size_t)n * 4, wall);
+    if (nwall) *nwall = n;
+    return UNS_OK;
+}
+
+int oracle_cc_screen_minmax(oracle_cc* o, double* out) {
+    cc_screen_minmax(o->s, out);
     return UNS_OK;
 }
 

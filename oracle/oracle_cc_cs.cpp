@@ -38,6 +38,7 @@ inline bool operator!=(cs a, cs b) { return a.z.real() != b.z.real(); }
 using std::atan;
 using std::cos;
 using std::fabs;
+using std::log10;
 using std::max;
 using std::min;
 using std::pow;
@@ -51,6 +52,7 @@ inline cs min(cs a, cs b) { return (b < a) ? b : a; }
 inline cs cos(cs a) { return cs(std::cos(a.z)); }
 inline cs sin(cs a) { return cs(std::sin(a.z)); }
 inline cs atan(cs a) { return cs(std::atan(a.z)); }
+inline cs log10(cs a) { return cs(std::log10(a.z)); }
 inline cs add_imag(cs x, double im) { return cs(x.z + std::complex<double>(0.0, im)); }
 
 using R = cs;

@@ -35,7 +35,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
              "-I", str(INCLUDE), "-I", str(CSRC / "host")]
 
-GPU_SOURCES = ["uns_api.cu", "uns_cc.cu", "uns_cc_adj.cu", "uns_nc.cu", "uns_noalloc.cu"]
+GPU_SOURCES = ["uns_api.cu", "uns_cc.cu", "uns_cc_adj.cu", "uns_cc_post.cu", "uns_nc.cu", "uns_noalloc.cu"]
 HOST_SOURCES = ["host/host_mesh.cpp", "host/host_api.cpp"]
 
 

@@ -136,6 +136,7 @@ struct uns_cc_handle {
     int gen = 0;           // bumped whenever the captured iteration changes (precision, capacity)
     double cfl_cur = 0.0;  // CFL passed to the last time_step call
     uns::CCAdj* adj = nullptr;  // discrete-adjoint state, created by uns_cc_adjoint_prepare
+    double* d_post = nullptr;   // post-processing scratch (uns_cc_post.cu), created on first use
 
     template <class T>
     int alloc(T*& p, size_t n) {

@@ -141,6 +141,18 @@ class CCSolver(_Solver):
         assert a.shape == self._field_shape(field), (field, a.shape)
         self._call("set_field", self.fields[field], _dp(a))
 
+    def find_cl_cd(self, xref: float = 0.25, yref: float = 0.0):
+        """find_cl_cd on the device: (C_L, C_D, C_m, C_L1, C_D1) and the wall rows (x, y, -C_p, C_f)."""
+        coef, wall, n = np.zeros(5), np.zeros((self.nbf, 4)), C.c_int()
+        self._call("find_cl_cd", C.c_double(xref), C.c_double(yref), _dp(coef), _dp(wall), C.byref(n))
+        return coef, wall[:n.value]
+
+    def screen_minmax(self) -> np.ndarray:
+        """screen's [7][2] min/max of density, u, v, p, T, Mach, entropy."""
+        out = np.zeros(14)
+        self._call("screen_minmax", _dp(out))
+        return out.reshape(7, 2)
+
     def cl_cd(self) -> tuple[float, float]:
         """Flux-based C_L, C_D of the last residual (CCFVM/main.F90:348-353)."""
         fx, fy = self.forces()
