@@ -59,11 +59,17 @@ WORKLOADS = {
                      params=dict(m_inf=0.5, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0),
                      desc="CCFVM Euler, 128x64 O-mesh split to 16,384 triangles, M0.5 a2, Roe, GG + VKN, RK3 CFL 0.9, "
                           "FP64 (the reference's CPU-sized case; CFL 1.0 leaves RK3 undefined there)"),
-    "cc_batched": dict(kind="cc_batch", n=256, tri=(5000, 200000), seed=20261203, dwall=1e-3,
+    "cc_batched": dict(kind="cc_batch", n=256, tri=(5000, 200000), seed=20261203, dwall=1e-3, packed=True,
                        params=dict(flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0, precision="mixed"),
-                       desc="256 CCFVM Euler instances in one graph launch per iteration: airfoil O-meshes with "
-                            "log-uniform 5k-200k triangles, Mach U[0.3,0.85], alpha U[-2,6] deg, Roe or Rusanov, "
-                            "RK3 CFL 0.9, FP32 flux / FP64 accumulation (seeded)"),
+                       desc="256 CCFVM Euler instances packed into one index space, one launch of each kernel per "
+                            "iteration for all of them: airfoil O-meshes with log-uniform 5k-200k triangles, Mach "
+                            "U[0.3,0.85], alpha U[-2,6] deg, Roe or Rusanov, RK3 CFL 0.9, FP32 flux / FP64 "
+                            "accumulation (seeded)"),
+    "cc_batched_graphs": dict(kind="cc_batch", n=256, tri=(5000, 200000), seed=20261203, dwall=1e-3,
+                              params=dict(flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0,
+                                          precision="mixed"),
+                              desc="the cc_batched instances as separate handles, one CUDA graph whose parallel "
+                                   "branches are their own iterations (uns_cc_batch_*)"),
     "cc": dict(kind="cc", ni=2048, nj=1024, dwall=1e-3,
                params=dict(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0),
                desc="CCFVM Euler, 2048x1024 O-mesh split to 4,194,304 triangles, M0.75 a2, Roe, GG + VKN, RK3, FP64"),
@@ -369,8 +375,15 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     inst = batch_instances(w)
     meshes = [mesh.CCMesh.airfoil(ni, nj, 0.12, 20.0, w["dwall"]) for ni, nj, _ in inst]
     params = [abi.make_params(**kw) for _, _, kw in inst]
-    solvers = [CCSolver(m, p) for m, p in zip(meshes, params)]
-    batch = CCBatch(solvers)
+    packed = w.get("packed", False)
+    if packed:  # one index space: one launch of each kernel for all instances
+        from unsflow2d_gb300.solver import CCPacked
+        batch = CCPacked(meshes, params)
+        n_inst = batch.n
+    else:  # one graph whose parallel branches are the instances' own iterations
+        solvers = [CCSolver(m, p) for m, p in zip(meshes, params)]
+        batch = CCBatch(solvers)
+        n_inst = len(solvers)
     setup_s = time.time() - t0
     cells = int(sum(m.arrays["noc"] for m in meshes))
     it = 0
@@ -409,7 +422,10 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     clocks = clk.summary()
     if rank != 0:
         return None
-    n = len(solvers)
+    n = n_inst
+    launches = (LAUNCHES[("cc", "rk3")] if packed else LAUNCHES[("cc", "rk3")] * n) * args.steps
+    path = ("uns_cc_packed_iterate" if packed else "uns_cc_batch_iterate") + \
+        ": CFL schedules in, residual histories out, one call for all steps"
     return {
         "metric": METRIC, "value": round(tot / secs / 1e6, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
@@ -420,8 +436,8 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
                    "setup_s": round(setup_s, 2)},
         "e2e": {"value": round(tot_w / secs_w / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 8 * n,
                 "d2h_bytes_per_step": 8 * n + 4 * n // max(args.steps, 1),
-                "path": "uns_cc_batch_iterate: CFL schedules in, residual histories out, one call for all steps"},
-        "gpu_launches": LAUNCHES[("cc", "rk3")] * n * args.steps,
+                "path": path},
+        "gpu_launches": launches,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": "whole batch iteration (all kernels of all instances)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),

@@ -180,6 +180,29 @@ int uns_cc_adjoint_solve(uns_cc_handle* h, int objective, int max_iter, double t
 /* The adjoint vector of the last solve: [noc][4] and [nbf][5] (either may be NULL). */
 int uns_cc_adjoint_get(uns_cc_handle* h, double* lambda_q, double* lambda_g);
 
+/* ==================================================== packed cases ====*/
+/* Many independent CCFVM cases in ONE index space (no reference
+ * counterpart: the reference runs one case per process).  The n meshes are
+ * concatenated -- interior cells padded per case to a multiple of 256, ghosts
+ * in case order -- and every element records its case, so one launch of each
+ * kernel advances all cases by one iteration (about twelve launches per
+ * iteration for any number of cases).  Each case keeps its mesh, Mach number,
+ * angle of attack, flux scheme, CFL schedule, residual norm, normalisation
+ * and stop level (params[i].min_res) and evolves bit-identically to a handle
+ * of its own; the cases share RK3 without residual smoothing, the gradient,
+ * limiter, flow type and precision.  The result is a CCFVM handle: its state
+ * (uns_cc_get_state: ntot rows), precision switch and destroy are the usual
+ * calls; it iterates with uns_cc_packed_iterate. */
+int uns_cc_create_packed(const uns_cc_mesh* meshes, const uns_params* params, int n, uns_cc_handle** out);
+/* Where case i lives in the packed state: its interior cells are rows
+ * cell_off[i] .. cell_off[i] + noc_i, its ghosts rows cell_off[n] +
+ * ghost_off[i] .. cell_off[n] + ghost_off[i + 1]; both arrays [n + 1]. */
+int uns_cc_packed_layout(uns_cc_handle* h, int* cell_off, int* ghost_off);
+/* As uns_cc_iterate for every case i: cfl[i*niter + k], fres_raw[i*niter + k],
+ * done_iters[i]. */
+int uns_cc_packed_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
+                          int* done_iters);
+
 /* ========================================================= precision ====*/
 /* Switches the arithmetic form (UNS_PREC_*) between calls; waits for the
  * handle's stream, and the next uns_*_iterate captures a new graph.  No

@@ -39,9 +39,35 @@ using namespace uns;
 namespace {
 
 
-__device__ __forceinline__ bool stopped(const CCView& v) { return v.done != nullptr && *((volatile int*)v.done) != 0; }
-__device__ __forceinline__ double cur_cfl(const CCView& v, double cfl) {
-    return v.cfl_sched ? v.cfl_sched[*v.iter] : cfl;
+__device__ __forceinline__ bool stopped(const CCView& v, int inst) {
+    return v.done != nullptr && ((volatile int*)v.done)[inst] != 0;
+}
+__device__ __forceinline__ bool stopped(const CCView& v) { return stopped(v, 0); }
+__device__ __forceinline__ double cur_cfl(const CCView& v, int inst, double cfl) {
+    return v.cfl_sched ? v.cfl_sched[(size_t)inst * v.cfl_stride + v.iter[inst]] : cfl;
+}
+// Instance of a cell / face / vertex (0 for a single case; -1 for padding).
+__device__ __forceinline__ int cell_inst(const CCView& v, int i) { return v.ninst ? v.cinst[i] : 0; }
+__device__ __forceinline__ int face_inst(const CCView& v, int f) { return v.ninst ? v.finst[f] : 0; }
+__device__ __forceinline__ int vert_inst(const CCView& v, int k) { return v.ninst ? v.pinst[k] : 0; }
+// Instance of a block of interior cells: its first cell is a real one.
+__device__ __forceinline__ int block_inst(const CCView& v) { return v.ninst ? v.cinst[blockIdx.x * blockDim.x] : 0; }
+__device__ __forceinline__ const Gas& gas_of(const CCView& v, int inst) { return v.ninst ? v.gas[inst] : v.g; }
+
+// Minimum / maximum of a 64-bit key over a group of lanes (all of which call
+// it with the same mask): the extreme high word, then the extreme low word
+// among the lanes holding it.
+__device__ __forceinline__ unsigned long long grp_min_u64(unsigned grp, unsigned long long e) {
+    const unsigned hi = (unsigned)(e >> 32), lo = (unsigned)e;
+    const unsigned mh = __reduce_min_sync(grp, hi);
+    const unsigned ml = __reduce_min_sync(grp, hi == mh ? lo : 0xffffffffu);
+    return ((unsigned long long)mh << 32) | ml;
+}
+__device__ __forceinline__ unsigned long long grp_max_u64(unsigned grp, unsigned long long e) {
+    const unsigned hi = (unsigned)(e >> 32), lo = (unsigned)e;
+    const unsigned mh = __reduce_max_sync(grp, hi);
+    const unsigned ml = __reduce_max_sync(grp, hi == mh ? lo : 0u);
+    return ((unsigned long long)mh << 32) | ml;
 }
 
 // ---------------------------------------------------------------- kernels
@@ -51,22 +77,25 @@ __device__ __forceinline__ double cur_cfl(const CCView& v, double cfl) {
 enum { BEGIN_PRIM = 1, BEGIN_OLD = 2, BEGIN_MINMAX = 4, BEGIN_POS = 8 };
 
 __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
-    if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int inst = i < v.ntot ? cell_inst(v, i) : (v.ninst ? -1 : 0);
+    const bool live = inst >= 0 && !stopped(v, inst);
+    if (!v.ninst && !live) return;  // one case: the whole grid stops together
     unsigned long long emx[4] = {0ULL, 0ULL, 0ULL, 0ULL};
     unsigned long long emn[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
-    if (i < v.noc) {
+    if (live && i < v.noc) {
+        const Gas& gi = gas_of(v, inst);
         double4 q = v.qc[i];
         if ((flags & BEGIN_PRIM) && v.mixed) {  // con2prim in FP32 from the rounded state
             const float E = (float)q.x, r = (float)q.y, ru = (float)q.z, rv = (float)q.w;
             const float u = ru / r, w = rv / r;
-            const float p = (float)v.g.gamma1 * (E - 0.5f * r * (u * u + w * w));
+            const float p = (float)gi.gamma1 * (E - 0.5f * r * (u * u + w * w));
             v.qpf[i] = make_float4(r, u, w, p);
             v.qp[i] = make_double4(r, u, w, p);
-            if (v.laminar || v.grad_type == UNS_GRAD_GGFC) v.qT[i] = (double)(p / (r * (float)v.g.znd));
+            if (v.laminar || v.grad_type == UNS_GRAD_GGFC) v.qT[i] = (double)(p / (r * (float)gi.znd));
             if ((flags & BEGIN_POS) && (r <= 0.f || p <= 0.f)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
         } else if (flags & BEGIN_PRIM) {
-            Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
+            Prim P = con2prim(gi, q.x, q.y, q.z, q.w);
             v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
             v.qT[i] = P.t;
             if ((flags & BEGIN_POS) && (P.rho <= 0.0 || P.p <= 0.0)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
@@ -74,11 +103,23 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
         if (flags & BEGIN_OLD) v.qold[i] = q;
     }
     if (flags & BEGIN_MINMAX) {
-        if (i < v.ntot) {
+        if (live && i < v.ntot) {
             double4 p = v.qp[i];
             double a[4] = {p.x, p.y, p.z, p.w};
 #pragma unroll
             for (int j = 0; j < 4; ++j) { emx[j] = enc_ord(a[j]); emn[j] = emx[j]; }
+        }
+        if (v.ninst) {  // packed instances: reduce over the lanes of each instance
+            const unsigned grp = __match_any_sync(0xffffffffu, live ? inst : -1);
+            unsigned long long mx[4], mn[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) { mx[j] = grp_max_u64(grp, emx[j]); mn[j] = grp_min_u64(grp, emn[j]); }
+            if (live && (int)(threadIdx.x & 31) == __ffs(grp) - 1)
+                for (int j = 0; j < 4; ++j) {
+                    atomicMax(&v.minmax[8 * inst + j], mx[j]);
+                    atomicMin(&v.minmax[8 * inst + 4 + j], mn[j]);
+                }
+            return;
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -107,9 +148,8 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
 
 // avg_c2v vertex part (average.F90:263-281): pseudo-Laplacian weighted mean.
 __global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
-    if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.nop) return;
+    if (i >= v.nop || stopped(v, vert_inst(v, i))) return;
     if (v.mixed) {  // FP32 from the FP32 primitives; FP64 copies only where an FP64 kernel reads them
         const bool dbl = v.laminar || v.grad_type == UNS_GRAD_GGFC;
         float wt = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
@@ -150,18 +190,20 @@ __global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
 // avg_c2v face part (average.F90:284-288) + spectral02 face radius
 // (timestep.F90:399-423).
 __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
-    if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    const int inst = face_inst(v, f);
+    if (stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
     if (v.mixed) {  // FP32; the FP64 face radius stays (the LU-SGS prep reads it)
         const int2 p = v.fpt[f];
         const float4 a = v.ppf[p.x], b = v.ppf[p.y], na = v.fnaf[f];
         const float4 q = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z), 0.5f * (a.w + b.w));
         v.fqf[f] = q;
-        const float a0 = sqrtf((float)v.g.gamma * q.w / q.x);
+        const float a0 = sqrtf((float)g.gamma * q.w / q.x);
         float ll = na.z * (fabsf(q.y * na.x + q.z * na.y) + a0);
         if (v.laminar) {
-            ll = ll + (float)(v.g.vll * v.fmu[f]) / q.x;
+            ll = ll + (float)(g.vll * v.fmu[f]) / q.x;
             v.fq[f] = make_double4(q.x, q.y, q.z, q.w);
             v.fqT[f] = 0.5 * (v.ppT[p.x] + v.ppT[p.y]);
         }
@@ -175,10 +217,10 @@ __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     v.fq[f] = q;
     v.fqT[f] = 0.5 * (v.ppT[p.x] + v.ppT[p.y]);
     double2 n = v.fn[f];
-    double a0 = sqrt(v.g.gamma * q.w / q.x);
+    double a0 = sqrt(g.gamma * q.w / q.x);
     double un = q.y * n.x + q.z * n.y;
     double ll = v.farea[f] * (fabs(un) + a0);
-    ll = ll + v.g.vll * v.fmu[f] / q.x;
+    ll = ll + g.vll * v.fmu[f] / q.x;
     v.fla[f] = ll;
 }
 
@@ -216,9 +258,8 @@ __device__ __forceinline__ bool gradtri(const double* pr0, const double* pr1, co
 }
 
 __global__ void __launch_bounds__(kBlock) k_face_ggfc(CCView v) {
-    if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= v.nof) return;
+    if (f >= v.nof || stopped(v, face_inst(v, f))) return;
     int2 nb = v.fnb[f];
     int2 p = v.fpt[f];
     double2 X1 = v.pxy[p.x], X2 = v.pxy[p.y], Ci = v.cen[nb.x], Co = v.cen[nb.y];
@@ -254,33 +295,32 @@ __device__ __forceinline__ double4 d4(const double o[4]) { return make_double4(o
 // order (interior faces, then boundary faces).
 enum { CG_DT = 1, CG_GRAD = 2, CG_LIM = 4 };
 
-// atomicMin of an order-encoded double with one atomic per converged group of
-// lanes: the minimum 64-bit key is the minimum high word, then the minimum low
-// word among the lanes that hold it.  Same result as one atomic per lane
-// (min is exact and order-free), without 32 same-address atomics per warp.
-__device__ __forceinline__ void warp_atomic_min_u64(unsigned long long* dst, unsigned long long e) {
-    const unsigned mask = __activemask();
-    const unsigned hi = (unsigned)(e >> 32), lo = (unsigned)e;
-    const unsigned mh = __reduce_min_sync(mask, hi);
-    const unsigned ml = __reduce_min_sync(mask, hi == mh ? lo : 0xffffffffu);
-    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicMin(dst, ((unsigned long long)mh << 32) | ml);
+// atomicMin of an order-encoded dt into its instance's slot with one atomic
+// per converged group of lanes of one instance.  Same result as one atomic
+// per lane (min is exact and order-free), without 32 same-address atomics
+// per warp.
+__device__ __forceinline__ void warp_atomic_min_u64(const CCView& v, int inst, unsigned long long e) {
+    const unsigned mask = v.ninst ? __match_any_sync(__activemask(), inst) : __activemask();
+    const unsigned long long m = grp_min_u64(mask, e);
+    if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) atomicMin(&v.dtmin[inst], m);
 }
 
 __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, double cfl_in) {
-    if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
     const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
     if (flags & CG_DT) {
         double la = 0.0;
         for (int k = k0; k < k1; ++k) la = la + v.fla[v.cf[k] & FACE_MASK];
         v.la[i] = la;
-        double cfl = cur_cfl(v, cfl_in);
+        double cfl = cur_cfl(v, inst, cfl_in);
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
         v.dcv[i] = dt / v.cv[i];
         v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
-        warp_atomic_min_u64(v.dtmin, enc_ord(dt));
+        warp_atomic_min_u64(v, inst, enc_ord(dt));
     }
     double gx[4], gy[4];
     if (flags & CG_GRAD) {
@@ -362,8 +402,8 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         double qmax[4], qmin[4], tol[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            qmax[j] = dec_ord(v.minmax[j]);
-            qmin[j] = dec_ord(v.minmax[4 + j]);
+            qmax[j] = dec_ord(v.minmax[8 * inst + j]);
+            qmin[j] = dec_ord(v.minmax[8 * inst + 4 + j]);
             tol[j] = 0.05 * (qmax[j] - qmin[j]);
         }
         double qi[4], umax[4], umin[4], ph[4];
@@ -411,20 +451,21 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 // writes it back to the FP64 arrays when a caller reads them or the handle
 // leaves the form.
 __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags, double cfl_in) {
-    if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
     const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
     if (flags & CG_DT) {
         float la = 0.f;
         for (int k = k0; k < k1; ++k) la = la + v.flaf[v.cf[k] & FACE_MASK];
         const float cvf = (float)v.cv[i];
-        const float dt = (float)cur_cfl(v, cfl_in) * cvf / la;
+        const float dt = (float)cur_cfl(v, inst, cfl_in) * cvf / la;
         v.la[i] = (double)la;
         v.dt[i] = (double)dt;
         v.dcv[i] = (double)(dt / cvf);
         v.diag[i] = (double)(cvf / dt + 0.75f * la);
-        warp_atomic_min_u64(v.dtmin, enc_ord((double)dt));
+        warp_atomic_min_u64(v, inst, enc_ord((double)dt));
     }
     if (!(flags & (CG_GRAD | CG_LIM))) return;
     const float4 q4 = v.qpf[i];
@@ -485,7 +526,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
         float tol[4], umax[4], umin[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float hi = (float)dec_ord(v.minmax[j]), lo = (float)dec_ord(v.minmax[4 + j]);
+            const float hi = (float)dec_ord(v.minmax[8 * inst + j]), lo = (float)dec_ord(v.minmax[8 * inst + 4 + j]);
             tol[j] = 0.05f * (hi - lo);
             tol[j] = tol[j] * tol[j];
             umax[j] = qi[j];
@@ -533,15 +574,17 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags,
 // their ghost cell (farfield: Riemann state; wall: slip / no-slip mirror).
 // R = double for the FP64 form, float for FP32 face arithmetic.
 template <class R>
-__device__ __forceinline__ bool flux_dispatch(const CCView& v, R nx, R ny, R area, V4<R>& ql, V4<R>& qr, V4<R>& F) {
-    return face_flux<R>(v.g, nx, ny, area, ql, qr, F);
+__device__ __forceinline__ bool flux_dispatch(const Gas& g, R nx, R ny, R area, V4<R>& ql, V4<R>& qr, V4<R>& F) {
+    return face_flux<R>(g, nx, ny, area, ql, qr, F);
 }
 
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
-    if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    const int inst = face_inst(v, f);
+    if (stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
     if constexpr (std::is_same<R, float>::value) {
         if (f < v.nfi) {  // interior face of the mixed form: FP32 packs and geometry only
             const int2 nb = v.fnb[f];
@@ -562,7 +605,7 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
                 ql[j] = qi[j] + 0.5f * phi_i[j] * (zhi * beta + zlo * (gxi[j] * d.x + gyi[j] * d.y));
                 qr[j] = qo[j] + 0.5f * phi_o[j] * (zhi * -beta + zlo * (gxo[j] * d.z + gyo[j] * d.w));
             }
-            bool ok = flux_dispatch<float>(v, na.x, na.y, na.z, ql, qr, F);
+            bool ok = flux_dispatch<float>(g, na.x, na.y, na.z, ql, qr, F);
             if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
             v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
             return;
@@ -608,7 +651,7 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
             beta = qi[j] - qo[j];
             qr[j] = (R)(qo[j] + 0.5 * phi_o[j] * (zhi * beta + (1.0 - zhi) * alfa));
         }
-        bool ok = flux_dispatch<R>(v, (R)n.x, (R)n.y, (R)area, ql, qr, F);
+        bool ok = flux_dispatch<R>(g, (R)n.x, (R)n.y, (R)area, ql, qr, F);
         if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
         v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
         return;
@@ -619,7 +662,6 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
     V4<double> qcl;
 #pragma unroll
     for (int j = 0; j < 4; ++j) qcl[j] = qi[j] + phi_i[j] * (gxi[j] * d0 + gyi[j] * d1);
-    const Gas& g = v.g;
     double4 Fd = make_double4(0.0, 0.0, 0.0, 0.0);
     if (bc == 2001 || bc == 1001) {
         V4<double> cin = {0.0, 0.0, 0.0, 0.0};
@@ -638,21 +680,25 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
 
 // Sutherland viscosity of every interior cell (viscous_flux.F90:478-480,585-597).
 __global__ void __launch_bounds__(kBlock) k_cell_mul(CCView v) {
-    if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
     double4 c = v.qc[i];
-    Prim P = con2prim(v.g, c.x, c.y, c.z, c.w);
-    double num = 1.0 + v.g.T_infd / v.g.SCONST;
-    double den = P.t + v.g.T_infd / v.g.SCONST;
+    Prim P = con2prim(g, c.x, c.y, c.z, c.w);
+    double num = 1.0 + g.T_infd / g.SCONST;
+    double den = P.t + g.T_infd / g.SCONST;
     v.mul[i] = (num / den) * pow(P.t, 1.5);
 }
 
 // Laminar viscous face flux (viscous_flux.F90:488-534), stored as flux*area.
 __global__ void __launch_bounds__(kBlock) k_face_visc(CCView v) {
-    if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    const int inst = face_inst(v, f);
+    if (stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
     int2 nb = v.fnb[f];
     double2 n = v.fn[f];
     double area = v.farea[f];
@@ -667,9 +713,9 @@ __global__ void __launch_bounds__(kBlock) k_face_visc(CCView v) {
     double tauxx = two_third * (two * ux - vy);
     double tauxy = (uy + vx);
     double tauyy = two_third * (two * vy - ux);
-    double factor = (v.g.gamma - 1.0) * v.g.m_inf * v.g.m_inf * v.g.prandtl;
+    double factor = (g.gamma - 1.0) * g.m_inf * g.m_inf * g.prandtl;
     double qx = -(tx / factor), qy = -(ty / factor);
-    double mr = mu / v.g.rey;
+    double mr = mu / g.rey;
     double f1 = mr * ((uvel * tauxx + vvel * tauxy - qx) * n.x + (uvel * tauxy + vvel * tauyy - qy) * n.y);
     double f3 = mr * (tauxx * n.x + tauxy * n.y);
     double f4 = mr * (tauxy * n.x + tauyy * n.y);
@@ -683,10 +729,10 @@ __device__ __forceinline__ void add4(double r[4], const double4& a) { r[0] = r[0
 __device__ __forceinline__ void sub4(double r[4], const double4& a) { r[0] = r[0] - a.x; r[1] = r[1] - a.y; r[2] = r[2] - a.z; r[3] = r[3] - a.w; }
 
 __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int partial) {
-    if (stopped(v)) return;
+    if (stopped(v, block_inst(v))) return;  // blocks of cells are instance-pure
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0;
-    if (i < v.noc) {
+    if (i < v.noc && cell_inst(v, i) >= 0) {
         const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
         double r[4] = {0.0, 0.0, 0.0, 0.0};
         for (int k = k0; k < k1; ++k) {  // boundary faces first
@@ -740,10 +786,10 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
 // one FP64 add per cell before the warp stage (FP64 issue, not bytes, bounds
 // this kernel on GB300).
 __global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, int partial) {
-    if (stopped(v)) return;
+    if (stopped(v, block_inst(v))) return;  // blocks of cells are instance-pure
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0;
-    if (i < v.noc) {
+    if (i < v.noc && cell_inst(v, i) >= 0) {
         const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
         double r[4] = {0.0, 0.0, 0.0, 0.0};
         for (int k = k0; k < k1; ++k) {
@@ -857,10 +903,13 @@ __global__ void __launch_bounds__(kBlock) k_res_partial(CCView v) {
 // records the history, the first-iteration normalisation and the stop flag
 // (solution.F90:365-379, main.F90:57).
 __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, double* out) {
-    if (stopped(v)) return;
+    const int inst = blockIdx.x;  // one block per instance
+    if (stopped(v, inst)) return;
+    const int k0 = v.ninst ? v.boff[inst] : 0;
+    const int n = v.ninst ? v.boff[inst + 1] - k0 : nparts;
     __shared__ double s[kBlock];
     double t = 0.0;
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) t = t + v.partial[k];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) t = t + v.partial[k0 + k];
     s[threadIdx.x] = t;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -868,30 +917,35 @@ __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, doub
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double fres = sqrt(s[0] / (double)v.noc / 4.0);
-        if (out) *out = fres;
+        const int nc = v.ninst ? v.ncell[inst] : v.noc;
+        double fres = sqrt(s[0] / (double)nc / 4.0);
+        if (out) out[inst] = fres;
         if (v.iter) {
-            int it = *v.iter;
-            v.fres_hist[it] = fres;
-            if (it == 0 && v.first_iter) *v.fres1 = fres;
-            double f1 = *v.fres1;
+            int it = v.iter[inst];
+            v.fres_hist[(size_t)inst * v.cfl_stride + it] = fres;
+            if (it == 0 && v.first_iter) v.fres1[inst] = fres;
+            double f1 = v.fres1[inst];
             double nf = (f1 >= 2.220446049250313e-16) ? fres / f1 : fres;
-            if (!(nf > v.min_res) || v.err->code != 0) {
-                *v.done = 1;
+            const double mr = v.ninst ? v.minres[inst] : v.min_res;
+            if (!(nf > mr) || v.err->code != 0) {
+                v.done[inst] = 1;
                 if (v.err->code != 0) v.err->iter = it;
             }
-            *v.iter = it + 1;
+            v.iter[inst] = it + 1;
             // reset the encoded reductions for the next iteration
-            for (int j = 0; j < 4; ++j) { v.minmax[j] = 0ULL; v.minmax[4 + j] = ~0ULL; }
-            *v.dtmin = ~0ULL;
+            for (int j = 0; j < 4; ++j) { v.minmax[8 * inst + j] = 0ULL; v.minmax[8 * inst + 4 + j] = ~0ULL; }
+            v.dtmin[inst] = ~0ULL;
         }
     }
 }
 
 __global__ void k_reset_minmax(CCView v) {
-    if (stopped(v)) return;
-    if (threadIdx.x < 4) { v.minmax[threadIdx.x] = 0ULL; v.minmax[4 + threadIdx.x] = ~0ULL; }
-    if (threadIdx.x == 0) *v.dtmin = ~0ULL;
+    const int n = v.ninst ? v.ninst : 1;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        if (stopped(v, k)) continue;
+        for (int j = 0; j < 4; ++j) { v.minmax[8 * k + j] = 0ULL; v.minmax[8 * k + 4 + j] = ~0ULL; }
+        v.dtmin[k] = ~0ULL;
+    }
 }
 
 // Sequential wall-force sums in face order (fvresidual.F90:99-100 then
@@ -909,7 +963,7 @@ __global__ void k_forces(CCView v, double* out) {
 
 __global__ void k_check_pos(CCView v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= v.noc) return;
+    if (i >= v.noc || cell_inst(v, i) < 0) return;
     double4 p = v.qp[i];
     if (p.x <= 0.0 || p.w <= 0.0) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
 }
@@ -917,7 +971,9 @@ __global__ void k_check_pos(CCView v) {
 __global__ void k_initialize(CCView v, double4 qinf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < v.ntot) {
-        v.qc[i] = qinf; v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0;
+        const int inst = cell_inst(v, i);
+        v.qc[i] = (v.ninst && inst >= 0) ? v.qinfs[inst] : qinf;
+        v.qp[i] = make_double4(0.0, 0.0, 0.0, 0.0); v.qT[i] = 0.0;
         v.qpf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (i < v.noc) {
@@ -1485,7 +1541,7 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
         if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 0, 1, &fused))) return rc;
         if ((rc = enqueue_lusgs(h, v))) return rc;
     }
-    k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, nullptr);
+    k_res_final<<<std::max(1, v.ninst), kBlock, 0, h->stream>>>(v, h->nparts, nullptr);
     UNS_CUDA(cudaGetLastError());
     return UNS_OK;
 }
@@ -1536,10 +1592,51 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
 
 }  // namespace uns
 
+// Gas constants of one case: math + initialize (CCFVM/read_input.F90:217-262),
+// and its freestream conserved state.
+static Gas make_gas(const uns_params* p, double4* qinf) {
+    Gas g;
+    g.gamma = 1.4;
+    g.gamma1 = g.gamma - 1.0;
+    double pi = 4.0 * std::atan(1.0);
+    double aoa = p->aoa_deg * pi / 180.0;
+    double q1 = 1.0, q2 = std::cos(aoa) * 1.0, q3 = std::sin(aoa) * 1.0;
+    g.p_inf = 1.0 / (g.gamma * p->m_inf * p->m_inf);
+    double q0 = g.p_inf / (g.gamma - 1.0) + 0.5;
+    g.r_inf = q1;
+    g.a_inf = std::sqrt(g.gamma * g.p_inf / g.r_inf);
+    g.u_inf = q2 / q1;
+    g.v_inf = q3 / q1;
+    g.m_inf = p->m_inf;
+    g.znd = 1.0 / (g.gamma * p->m_inf * p->m_inf);
+    g.T_infd = 300.0;
+    g.SCONST = 110.4;
+    g.t_wall = p->t_wall / g.T_infd;
+    g.rey = p->rey;
+    g.prandtl = 0.72;
+    g.vll = (p->flow_type != UNS_FLOW_INVISCID) ? 2.0 * g.gamma / (g.prandtl * p->rey * 0.25) : 0.0;
+    g.mref = std::max((double)0.32f, 0.5 * p->m_inf);
+    g.flux = p->flux_type;
+    g.flow = p->flow_type;
+    g.iwall = p->iwall;
+    *qinf = make_double4(q0, q1, q2, q3);
+    return g;
+}
+
+static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_schedule, uns_cc_handle** out);
+static int grow_schedule(uns_cc_handle* h, int cap);
+static int iterate_graph(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters);
+
 // ====================================================================== C-ABI
 extern "C" {
 
 int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out) {
+    return create_impl(m, p, true, out);
+}
+
+}  // extern "C"
+
+static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_schedule, uns_cc_handle** out) {
     if (!m || !p || !out) { set_last_error("uns_cc_create: null argument"); return UNS_ERR_ARG; }
     *out = nullptr;
     if (m->nop <= 0 || m->noc <= 0 || m->nfi < 0 || m->nbf < 0) { set_last_error("uns_cc_create: bad sizes"); return UNS_ERR_ARG; }
@@ -1573,32 +1670,8 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
         delete h;
         return UNS_ERR_CUDA;
     }
-    // Gas constants: math + initialize (CCFVM/read_input.F90:217-262).
     Gas& g = h->g;
-    g.gamma = 1.4;
-    g.gamma1 = g.gamma - 1.0;
-    double pi = 4.0 * std::atan(1.0);
-    double aoa = p->aoa_deg * pi / 180.0;
-    double q1 = 1.0, q2 = std::cos(aoa) * 1.0, q3 = std::sin(aoa) * 1.0;
-    g.p_inf = 1.0 / (g.gamma * p->m_inf * p->m_inf);
-    double q0 = g.p_inf / (g.gamma - 1.0) + 0.5;
-    g.r_inf = q1;
-    g.a_inf = std::sqrt(g.gamma * g.p_inf / g.r_inf);
-    g.u_inf = q2 / q1;
-    g.v_inf = q3 / q1;
-    g.m_inf = p->m_inf;
-    g.znd = 1.0 / (g.gamma * p->m_inf * p->m_inf);
-    g.T_infd = 300.0;
-    g.SCONST = 110.4;
-    g.t_wall = p->t_wall / g.T_infd;
-    g.rey = p->rey;
-    g.prandtl = 0.72;
-    g.vll = (p->flow_type != UNS_FLOW_INVISCID) ? 2.0 * g.gamma / (g.prandtl * p->rey * 0.25) : 0.0;
-    g.mref = std::max((double)0.32f, 0.5 * p->m_inf);
-    g.flux = p->flux_type;
-    g.flow = p->flow_type;
-    g.iwall = p->iwall;
-    h->qinf = make_double4(q0, q1, q2, q3);
+    g = make_gas(p, &h->qinf);
 
     // Host-side derived connectivity.
     std::vector<double2> pxy(nop), cen(ntot), fn(nof), fcen(nof);
@@ -1692,7 +1765,7 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_fres1, 1))) return fail(rc);
     // LU-SGS warp schedule on the reference c2f lists.
-    {
+    if (lusgs_schedule) {
         int maxdeg = 0;
         for (int i = 0; i < noc; ++i) maxdeg = std::max(maxdeg, m->c2f_off[i + 1] - m->c2f_off[i]);
         if (maxdeg > 32) { set_last_error("uns_cc_create: a cell has more than 32 faces"); return fail(UNS_ERR_MESH); }
@@ -1743,6 +1816,8 @@ int uns_cc_create(const uns_cc_mesh* m, const uns_params* p, uns_cc_handle** out
 #undef UP
 #undef AL
 }
+
+extern "C" {
 
 int uns_cc_destroy(uns_cc_handle* h) {
     if (!h) return UNS_OK;
@@ -2005,6 +2080,7 @@ int uns_cc_forces(uns_cc_handle* h, double* fx, double* fy) {
 static int capture_iteration(uns_cc_handle* h, int first_iter, cudaGraph_t* out) {
     CCView v = h->v;
     v.cfl_sched = h->d_cfl;
+    v.cfl_stride = h->cfl_cap;
     v.iter = h->d_iter;
     v.done = h->d_done;
     v.fres_hist = h->d_hist;
@@ -2021,17 +2097,12 @@ static int capture_iteration(uns_cc_handle* h, int first_iter, cudaGraph_t* out)
 
 int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
     if (!h || niter < 0 || (niter > 0 && (!cfl || !fres_raw))) return UNS_ERR_ARG;
+    if (h->v.ninst) { set_last_error("uns_cc_iterate: a packed handle iterates with uns_cc_packed_iterate"); return UNS_ERR_ARG; }
     if (done_iters) *done_iters = 0;
     if (niter == 0) return UNS_OK;
     if (niter > h->cfl_cap) {
-        if (h->d_cfl) cudaFree(h->d_cfl);
-        if (h->d_hist) cudaFree(h->d_hist);
-        h->d_cfl = nullptr; h->d_hist = nullptr;
-        UNS_CUDA(cudaMalloc(&h->d_cfl, sizeof(double) * niter));
-        UNS_CUDA(cudaMalloc(&h->d_hist, sizeof(double) * niter));
-        h->cfl_cap = niter;
-        ++h->gen;
-        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+        int rc = grow_schedule(h, niter);
+        if (rc) return rc;
     }
     // The smoothing sweeps are launched only while their coefficient is
     // non-zero; the schedule must agree on that for the whole chunk.
@@ -2067,10 +2138,39 @@ int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_ite
         return UNS_OK;
     }
     (void)all_smooth;
-    UNS_CUDA(cudaMemcpyAsync(h->d_cfl, cfl, sizeof(double) * niter, cudaMemcpyHostToDevice, h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->d_iter, 0, sizeof(int), h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->d_done, 0, sizeof(int), h->stream));
-    UNS_CUDA(cudaMemsetAsync(h->d_hist, 0, sizeof(double) * niter, h->stream));
+    return iterate_graph(h, niter, cfl, first_iter, fres_raw, done_iters);
+}
+
+}  // extern "C"
+
+// Device CFL schedule and residual history with room for cap iterations per
+// instance; the captured iteration bakes in their addresses and stride.
+static int grow_schedule(uns_cc_handle* h, int cap) {
+    const size_t n = (size_t)std::max(1, h->v.ninst);
+    if (h->d_cfl) cudaFree(h->d_cfl);
+    if (h->d_hist) cudaFree(h->d_hist);
+    h->d_cfl = nullptr; h->d_hist = nullptr;
+    UNS_CUDA(cudaMalloc(&h->d_cfl, sizeof(double) * n * cap));
+    UNS_CUDA(cudaMalloc(&h->d_hist, sizeof(double) * n * cap));
+    h->cfl_cap = cap;
+    ++h->gen;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return UNS_OK;
+}
+
+// The graph-replayed iterations of every instance: cfl and fres_raw are
+// [instances][niter], done_iters [instances].
+static int iterate_graph(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
+    const int n = std::max(1, h->v.ninst);
+    if (niter > h->cfl_cap) {
+        int rc = grow_schedule(h, niter);
+        if (rc) return rc;
+    }
+    const size_t pitch = sizeof(double) * h->cfl_cap, row = sizeof(double) * niter;
+    UNS_CUDA(cudaMemcpy2DAsync(h->d_cfl, pitch, cfl, row, row, n, cudaMemcpyHostToDevice, h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_iter, 0, sizeof(int) * n, h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_done, 0, sizeof(int) * n, h->stream));
+    UNS_CUDA(cudaMemsetAsync(h->d_hist, 0, pitch * n, h->stream));
     if (!h->graph || h->graph_first != (first_iter ? 1 : 0)) {
         if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
         cudaGraph_t graph;
@@ -2082,13 +2182,15 @@ int uns_cc_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_ite
         h->graph_first = first_iter ? 1 : 0;
     }
     for (int k = 0; k < niter; ++k) UNS_CUDA(cudaGraphLaunch(h->graph, h->stream));
-    UNS_CUDA(cudaMemcpyAsync(fres_raw, h->d_hist, sizeof(double) * niter, cudaMemcpyDeviceToHost, h->stream));
-    int it = 0;
-    UNS_CUDA(cudaMemcpyAsync(&it, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpy2DAsync(fres_raw, row, h->d_hist, pitch, row, n, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<int> it(n, 0);
+    UNS_CUDA(cudaMemcpyAsync(it.data(), h->d_iter, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
     UNS_CUDA(cudaStreamSynchronize(h->stream));
-    if (done_iters) *done_iters = it;
+    if (done_iters) std::copy(it.begin(), it.end(), done_iters);
     return check_dev_err(h);
 }
+
+extern "C" {
 
 int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (!h || precision < UNS_PREC_FP64 || precision > UNS_PREC_MIXED_SWEEP) return UNS_ERR_ARG;
@@ -2313,6 +2415,163 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
         if (names) names[k] = k < NP ? kNames[k] : "";
     }
     return check_dev_err(h);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ packed cases
+// Many independent CCFVM cases in ONE index space: the meshes are
+// concatenated (points, then interior cells padded per case to a multiple of
+// the block size, interior faces, boundary faces and their ghosts in case
+// order), every element records its case, and the per-case constants and
+// loop control become arrays.  One launch of each kernel then advances every
+// case; each case's arithmetic, face orders and norm blocks are the ones it
+// has alone, so it evolves bit-identically to a handle of its own.
+extern "C" {
+
+int uns_cc_create_packed(const uns_cc_mesh* meshes, const uns_params* params, int n, uns_cc_handle** out) {
+    if (!meshes || !params || !out || n < 1) { set_last_error("uns_cc_create_packed: bad argument"); return UNS_ERR_ARG; }
+    *out = nullptr;
+    const uns_params& p0 = params[0];
+    for (int i = 0; i < n; ++i) {
+        const uns_params& p = params[i];
+        if (p.time_mode != UNS_TIME_RK3 || p.irs != 0 || p.grad_type != p0.grad_type || p.ilimit != p0.ilimit ||
+            p.flow_type != p0.flow_type || p.precision != p0.precision || p.limiter_type != p0.limiter_type) {
+            set_last_error("uns_cc_create_packed: cases must share RK3 without smoothing, gradient, limiter, flow "
+                           "type and precision (case " + std::to_string(i) + ")");
+            return UNS_ERR_ARG;
+        }
+        const uns_cc_mesh& m = meshes[i];
+        if (m.nop <= 0 || m.noc <= 0 || m.nfi < 0 || m.nbf < 0) { set_last_error("uns_cc_create_packed: bad sizes"); return UNS_ERR_ARG; }
+    }
+    std::vector<long long> C(n + 1, 0), F(n + 1, 0), B(n + 1, 0), P(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        const uns_cc_mesh& m = meshes[i];
+        C[i + 1] = C[i] + ((long long)m.noc + kBlock - 1) / kBlock * kBlock;
+        F[i + 1] = F[i] + m.nfi;
+        B[i + 1] = B[i] + m.nbf;
+        P[i + 1] = P[i] + m.nop;
+    }
+    if (C[n] + B[n] >= (1LL << 30) || F[n] + B[n] >= (1LL << 30)) { set_last_error("uns_cc_create_packed: too large"); return UNS_ERR_ARG; }
+    const int NOC = (int)C[n], NFI = (int)F[n], NBF = (int)B[n], NOP = (int)P[n], NOF = NFI + NBF, NTOT = NOC + NBF;
+    std::vector<double> px(NOP), py(NOP), cx(NTOT, 0.0), cy(NTOT, 0.0), cv(NOC, 1.0), cov(NOC, 1.0);
+    std::vector<double> r11(NOC, 1.0), r12(NOC, 0.0), r22(NOC, 1.0);
+    std::vector<int> nc2c(NOC, 0), fp1(NOF), fp2(NOF), fin(NOF), fout(NOF), fbc(NOF);
+    std::vector<double> fnx(NOF), fny(NOF), farea(NOF), fcx(NOF), fcy(NOF);
+    std::vector<int> c2f_off(NOC + 1, 0), c2f, v2c_off(NOP + 1, 0), v2c;
+    std::vector<double> v2c_wt;
+    std::vector<int> cinst(NTOT, -1), finst(NOF), pinst(NOP);
+    for (int i = 0; i < n; ++i) {
+        const uns_cc_mesh& m = meshes[i];
+        const int noc = m.noc, nfi = m.nfi, nof = m.nfi + m.nbf;
+        auto cell = [&](int c) { return c < noc ? (int)C[i] + c : NOC + (int)B[i] + (c - noc); };
+        auto face = [&](int f) { return f < nfi ? (int)F[i] + f : NFI + (int)B[i] + (f - nfi); };
+        for (int k = 0; k < m.nop; ++k) { px[P[i] + k] = m.px[k]; py[P[i] + k] = m.py[k]; pinst[P[i] + k] = i; }
+        for (int c = 0; c < noc + m.nbf; ++c) { cx[cell(c)] = m.cx[c]; cy[cell(c)] = m.cy[c]; cinst[cell(c)] = i; }
+        for (int c = 0; c < noc; ++c) {
+            const int g = (int)C[i] + c;
+            cv[g] = m.cv[c]; cov[g] = m.cov[c]; r11[g] = m.r11[c]; r12[g] = m.r12[c]; r22[g] = m.r22[c]; nc2c[g] = m.nc2c[c];
+        }
+        for (int f = 0; f < nof; ++f) {
+            const int g = face(f);
+            if (m.fin[f] < 0 || m.fin[f] >= noc || m.fp1[f] < 0 || m.fp1[f] >= m.nop || m.fp2[f] < 0 || m.fp2[f] >= m.nop ||
+                (f < nfi ? (m.fout[f] < 0 || m.fout[f] >= noc) : (m.fout[f] != noc + (f - nfi)))) {
+                set_last_error("uns_cc_create_packed: case " + std::to_string(i) + " face " + std::to_string(f) +
+                               " has an out-of-range index");
+                return UNS_ERR_MESH;
+            }
+            fp1[g] = (int)P[i] + m.fp1[f]; fp2[g] = (int)P[i] + m.fp2[f];
+            fin[g] = cell(m.fin[f]); fout[g] = cell(m.fout[f]); fbc[g] = m.fbc[f];
+            fnx[g] = m.fnx[f]; fny[g] = m.fny[f]; farea[g] = m.farea[f]; fcx[g] = m.fcx[f]; fcy[g] = m.fcy[f];
+            finst[g] = i;
+        }
+    }
+    // cell -> faces (reference c2f order) and vertex -> cells, in global order
+    for (int i = 0; i < n; ++i) {
+        const uns_cc_mesh& m = meshes[i];
+        const int noc = m.noc, nfi = m.nfi, ntot = noc + m.nbf;
+        auto face = [&](int f) { return f < nfi ? (int)F[i] + f : NFI + (int)B[i] + (f - nfi); };
+        auto cell = [&](int c) { return c < noc ? (int)C[i] + c : NOC + (int)B[i] + (c - noc); };
+        for (int c = 0; c < (int)(C[i + 1] - C[i]); ++c) {
+            const int g = (int)C[i] + c;
+            if (c < noc)
+                for (int k = m.c2f_off[c]; k < m.c2f_off[c + 1]; ++k) {
+                    if (m.c2f[k] < 0 || m.c2f[k] >= m.nfi + m.nbf) { set_last_error("uns_cc_create_packed: c2f index out of range"); return UNS_ERR_MESH; }
+                    c2f.push_back(face(m.c2f[k]));
+                }
+            c2f_off[g + 1] = (int)c2f.size();
+        }
+        for (int k = 0; k < m.nop; ++k) {
+            const int g = (int)P[i] + k;
+            for (int e = m.v2c_off[k]; e < m.v2c_off[k + 1]; ++e) {
+                if (m.v2c[e] < 0 || m.v2c[e] >= ntot) { set_last_error("uns_cc_create_packed: v2c index out of range"); return UNS_ERR_MESH; }
+                v2c.push_back(cell(m.v2c[e]));
+                v2c_wt.push_back(m.v2c_wt[e]);
+            }
+            v2c_off[g + 1] = (int)v2c.size();
+        }
+    }
+    uns_cc_mesh pm;
+    pm.nop = NOP; pm.noc = NOC; pm.nfi = NFI; pm.nbf = NBF;
+    pm.px = px.data(); pm.py = py.data(); pm.cx = cx.data(); pm.cy = cy.data(); pm.cv = cv.data(); pm.cov = cov.data();
+    pm.fp1 = fp1.data(); pm.fp2 = fp2.data(); pm.fin = fin.data(); pm.fout = fout.data(); pm.fbc = fbc.data();
+    pm.fnx = fnx.data(); pm.fny = fny.data(); pm.farea = farea.data(); pm.fcx = fcx.data(); pm.fcy = fcy.data();
+    pm.r11 = r11.data(); pm.r12 = r12.data(); pm.r22 = r22.data(); pm.nc2c = nc2c.data();
+    pm.c2f_off = c2f_off.data(); pm.c2f = c2f.data(); pm.v2c_off = v2c_off.data(); pm.v2c = v2c.data(); pm.v2c_wt = v2c_wt.data();
+    uns_cc_handle* h = nullptr;
+    int rc = create_impl(&pm, &p0, false, &h);
+    if (rc) return rc;
+    auto fail = [&](int code) { uns_cc_destroy(h); return code; };
+    // per-case constants and loop control
+    std::vector<Gas> gas(n);
+    std::vector<double4> qinfs(n);
+    std::vector<int> boff(n + 1), ncell(n);
+    std::vector<double> minres(n);
+    for (int i = 0; i < n; ++i) {
+        gas[i] = make_gas(&params[i], &qinfs[i]);
+        boff[i] = (int)(C[i] / kBlock);
+        ncell[i] = meshes[i].noc;
+        minres[i] = params[i].min_res;
+    }
+    boff[n] = (int)(C[n] / kBlock);
+    CCView& v = h->v;
+#define UPP(field, vec) if ((rc = h->upload(*(std::remove_const<std::remove_pointer<decltype(v.field)>::type>::type**)&v.field, vec.data(), vec.size()))) return fail(rc)
+    UPP(cinst, cinst); UPP(finst, finst); UPP(pinst, pinst); UPP(gas, gas); UPP(qinfs, qinfs);
+    UPP(boff, boff); UPP(ncell, ncell); UPP(minres, minres);
+#undef UPP
+    if ((rc = h->alloc(v.minmax, 8 * (size_t)n)) || (rc = h->alloc(v.dtmin, (size_t)n)) || (rc = h->alloc(h->d_iter, (size_t)n)) ||
+        (rc = h->alloc(h->d_done, (size_t)n)) || (rc = h->alloc(h->d_fres1, (size_t)n)))
+        return fail(rc);
+    v.ninst = n;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) { set_last_error("uns_cc_create_packed: upload failed"); return fail(UNS_ERR_CUDA); }
+    if ((rc = uns_cc_initialize(h))) return fail(rc);
+    *out = h;
+    return UNS_OK;
+}
+
+int uns_cc_packed_layout(uns_cc_handle* h, int* cell_off, int* ghost_off) {
+    if (!h || !h->v.ninst || !cell_off || !ghost_off) { set_last_error("uns_cc_packed_layout: not a packed handle"); return UNS_ERR_ARG; }
+    const int n = h->v.ninst;
+    std::vector<int> b(n + 1), nc(n);
+    UNS_CUDA(cudaMemcpyAsync(b.data(), h->v.boff, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(nc.data(), h->v.ncell, sizeof(int) * n, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<int> fi(h->v.nof);
+    UNS_CUDA(cudaMemcpyAsync(fi.data(), h->v.finst, sizeof(int) * h->v.nof, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i <= n; ++i) cell_off[i] = b[i] * kBlock;
+    // ghosts follow the boundary faces, which are in case order
+    int k = 0;
+    for (int i = 0; i < n; ++i) {
+        ghost_off[i] = k;
+        while (k < h->v.nbf && fi[h->v.nfi + k] == i) ++k;
+    }
+    ghost_off[n] = k;
+    return UNS_OK;
+}
+
+int uns_cc_packed_iterate(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
+    if (!h || !h->v.ninst || niter < 1 || !cfl || !fres_raw) { set_last_error("uns_cc_packed_iterate: bad argument"); return UNS_ERR_ARG; }
+    return iterate_graph(h, niter, cfl, first_iter, fres_raw, done_iters);
 }
 
 }  // extern "C"

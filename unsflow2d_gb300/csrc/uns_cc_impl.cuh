@@ -102,6 +102,21 @@ struct CCView {
     float4* ppf;          // [nop] vertex-averaged primitives
     const float* v2c_wtf; // pseudo-Laplacian weights
     double* dcv;          // [noc] dt / cv of the current time step (both forms)
+    // packed instances (uns_cc_create_packed; ninst = 0 for one case): every
+    // element knows its instance; per-instance constants and loop control
+    // are arrays indexed by it (iter, done, fres1, minmax [8 each], dtmin,
+    // cfl_sched / fres_hist [cfl_stride each]).  Interior cells of each
+    // instance are padded to a multiple of kBlock (padding: instance -1), so
+    // every block of cells belongs to one instance.
+    int ninst, cfl_stride;
+    const int* cinst;       // [ntot] instance of each cell, ghosts included
+    const int* finst;       // [nof]
+    const int* pinst;       // [nop]
+    const Gas* gas;         // [ninst]
+    const double4* qinfs;   // [ninst] freestream conserved state
+    const int* boff;        // [ninst + 1] norm blocks of each instance
+    const int* ncell;       // [ninst] real interior cells
+    const double* minres;   // [ninst]
     Gas g;
     int grad_type, ilimit, irs, laminar, first_iter;
     int mixed;            // UNS_PREC_MIXED: keep the FP32 copies, run the FP32 kernels

@@ -303,6 +303,73 @@ class CCBatch:
             pass
 
 
+class CCPacked:
+    """Many CCFVM cases in one index space (uns_cc_create_packed): one launch
+    of each kernel advances every case per iteration.  Cases share RK3, the
+    gradient, limiter, flow type and precision; mesh, Mach number, angle of
+    attack, flux scheme, CFL schedule and stop level are their own."""
+
+    def __init__(self, meshes, params_list):
+        self._lib = abi.gpu_lib()
+        n = len(meshes)
+        views, self._keep = [], []
+        self.noc, self.nbf = [], []
+        for m in meshes:
+            arr = m.arrays if hasattr(m, "arrays") else m
+            v, k = abi.cc_view_from_arrays(arr)
+            views.append(v)
+            self._keep.append((k, arr))
+            self.noc.append(int(arr["noc"]))
+            self.nbf.append(int(arr["nbf"]))
+        va = (abi.CCMeshView * n)(*views)
+        pa = (abi.Params * n)(*params_list)
+        h = C.c_void_p()
+        abi.check(self._lib.uns_cc_create_packed(va, pa, n, C.byref(h)), self._lib, "uns_cc_create_packed")
+        self._h = h
+        co, go = (C.c_int * (n + 1))(), (C.c_int * (n + 1))()
+        abi.check(self._lib.uns_cc_packed_layout(h, co, go), self._lib, "uns_cc_packed_layout")
+        self.cell_off, self.ghost_off = np.array(list(co)), np.array(list(go))
+        self.n = n
+        self.ntot = int(self.cell_off[-1]) + int(self.ghost_off[-1])
+
+    def iterate(self, cfl: np.ndarray, first_iter: bool) -> tuple[list[np.ndarray], np.ndarray]:
+        """cfl: [cases, niter].  Returns each case's raw residual norms of the
+        iterations it ran, and those counts."""
+        cfl = np.ascontiguousarray(cfl, dtype=np.float64)
+        n, niter = cfl.shape
+        assert n == self.n
+        out = np.zeros((n, niter))
+        done = (C.c_int * n)()
+        rc = self._lib.uns_cc_packed_iterate(self._h, niter, _dp(cfl), 1 if first_iter else 0, _dp(out), done)
+        abi.check(rc, self._lib, "uns_cc_packed_iterate")
+        d = np.array(list(done))
+        return [out[i, :d[i]] for i in range(n)], d
+
+    def get_state(self, i: int) -> np.ndarray:
+        """Conserved state of case i: its cells then its ghosts, [noc + nbf][4]."""
+        full = np.zeros((self.ntot, 4))
+        abi.check(self._lib.uns_cc_get_state(self._h, _dp(full)), self._lib, "uns_cc_get_state")
+        c0, g0 = int(self.cell_off[i]), int(self.cell_off[-1]) + int(self.ghost_off[i])
+        return np.concatenate([full[c0:c0 + self.noc[i]], full[g0:g0 + self.nbf[i]]])
+
+    def set_precision(self, precision: str) -> None:
+        abi.check(self._lib.uns_cc_set_precision(self._h, abi.PREC[precision]), self._lib, "uns_cc_set_precision")
+
+    def stream(self) -> int:
+        return int(self._lib.uns_cc_stream(self._h) or 0)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.uns_cc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def converge(solver, target: float, max_iter: int, switch_drop: float | None = None, chunk: int = 500,
              on_chunk=None) -> dict:
     """Run the main loop from iteration 1 until the density residual has dropped
