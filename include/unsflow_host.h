@@ -39,6 +39,15 @@ int uns_host_cc_airfoil_dy(int ni, int nj, double thickness, double rfar, double
  * 479-512) followed by geometric. */
 int uns_host_cc_read(const char* path, uns_host_cc** out);
 int uns_host_nc_read(const char* path, uns_host_nc** out);
+/* MeshGen's input (MeshGen/SolverInputMESH.f90:56-67): a single-block
+ * formatted plot3d O-grid (nbk; nx ny nz; x, y, z with i fastest; the last i
+ * column repeats the first; j = 1 on the wall, j = ny on the farfield), its
+ * quads split into triangles as the airfoil generator splits them, preprocessed
+ * for either solver (the reference's MeshGen writes NCFVM quads only). */
+int uns_host_cc_plot3d(const char* path, uns_host_cc** out);
+int uns_host_nc_plot3d(const char* path, uns_host_nc** out);
+/* The airfoil generator's O-grid written in that plot3d layout. */
+int uns_host_airfoil_plot3d(int ni, int nj, double thickness, double rfar, double dwall, const char* path);
 /* Write the raw (file) form in the reference's geometry.inp layout. */
 int uns_host_cc_write(const uns_host_cc* m, const char* path);
 int uns_host_nc_write(const uns_host_nc* m, const char* path);

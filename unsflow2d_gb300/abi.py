@@ -242,6 +242,8 @@ def host_lib() -> C.CDLL:
             "uns_host_last_error": ([], C.c_char_p),
             "uns_host_cc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),
             "uns_host_cc_airfoil_dy": ([i32, i32, dp, dp, dp, _D, pp], i32),
+            "uns_host_cc_plot3d": ([C.c_char_p, pp], i32), "uns_host_nc_plot3d": ([C.c_char_p, pp], i32),
+            "uns_host_airfoil_plot3d": ([i32, i32, dp, dp, dp, C.c_char_p], i32),
             "uns_host_nc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),
             "uns_host_cc_read": ([C.c_char_p, pp], i32), "uns_host_nc_read": ([C.c_char_p, pp], i32),
             "uns_host_cc_write": ([vp, C.c_char_p], i32), "uns_host_nc_write": ([vp, C.c_char_p], i32),

@@ -91,6 +91,36 @@ int uns_host_nc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns
     return UNS_OK;
 }
 
+int uns_host_cc_plot3d(const char* path, uns_host_cc** out) {
+    if (!path || !out) return fail(UNS_ERR_ARG, "null argument");
+    auto* m = new uns_host_cc();
+    std::string err;
+    int rc = read_plot3d_cc(path, m->raw, err);
+    if (!rc) rc = geometric_cc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_nc_plot3d(const char* path, uns_host_nc** out) {
+    if (!path || !out) return fail(UNS_ERR_ARG, "null argument");
+    auto* m = new uns_host_nc();
+    std::string err;
+    int rc = read_plot3d_nc(path, m->raw, err);
+    if (!rc) rc = geometric_nc(m->raw, m->mesh, err);
+    if (rc) { delete m; return fail(rc, err); }
+    *out = m;
+    return UNS_OK;
+}
+
+int uns_host_airfoil_plot3d(int ni, int nj, double t, double rfar, double dwall, const char* path) {
+    if (!path) return fail(UNS_ERR_ARG, "null path");
+    AirfoilSpec s{ni, nj, t, rfar, dwall};
+    std::string err;
+    int rc = write_plot3d_airfoil(s, path, err);
+    return rc ? fail(rc, err) : UNS_OK;
+}
+
 int uns_host_cc_read(const char* path, uns_host_cc** out) {
     if (!path || !out) return fail(UNS_ERR_ARG, "null argument");
     auto* m = new uns_host_cc();

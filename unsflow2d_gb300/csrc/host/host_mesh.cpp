@@ -158,12 +158,19 @@ int build_topology(const OGrid& g, TriTopo& t, std::string& err) {
 
 }  // namespace
 
+static int raw_cc_from_ogrid(const OGrid& g, RawCC& m, std::string& err);
+static int raw_nc_from_ogrid(const OGrid& g, RawNC& m, std::string& err);
+
 int gen_airfoil_cc(const AirfoilSpec& s, RawCC& m, std::string& err) {
     OGrid g;
     int rc = build_ogrid(s, g, err);
     if (rc) return rc;
+    return raw_cc_from_ogrid(g, m, err);
+}
+
+static int raw_cc_from_ogrid(const OGrid& g, RawCC& m, std::string& err) {
     TriTopo t;
-    rc = build_topology(g, t, err);
+    int rc = build_topology(g, t, err);
     if (rc) return rc;
     m = RawCC();
     m.nop = t.nop; m.noc = t.noc;
@@ -188,8 +195,12 @@ int gen_airfoil_nc(const AirfoilSpec& s, RawNC& m, std::string& err) {
     OGrid g;
     int rc = build_ogrid(s, g, err);
     if (rc) return rc;
+    return raw_nc_from_ogrid(g, m, err);
+}
+
+static int raw_nc_from_ogrid(const OGrid& g, RawNC& m, std::string& err) {
     TriTopo t;
-    rc = build_topology(g, t, err);
+    int rc = build_topology(g, t, err);
     if (rc) return rc;
     m = RawNC();
     m.nop = t.nop; m.noc = t.noc;
@@ -208,6 +219,84 @@ int gen_airfoil_nc(const AirfoilSpec& s, RawNC& m, std::string& err) {
     // The farfield cell is `out`, so it has to sit on the right of p1 -> p2.
     for (auto& e : t.farfield) push(e.p2, e.p1, -1, e.c1, 2001);
     m.nof = (int)m.fp1.size();
+    return UNS_OK;
+}
+
+// ---------------------------------------------------------------- plot3d
+// Single-block formatted plot3d grid as MeshGen reads it
+// (MeshGen/SolverInputMESH.f90:56-67): nbk; nx ny nz; then x, y, z each with i
+// fastest.  An O-grid: i runs around the body (its last column repeats the
+// first and is dropped), j from the wall (j = 1) to the farfield (j = ny).
+// Its quads are split into triangles exactly as the analytic generator's.
+static int read_plot3d_ogrid(const std::string& path, OGrid& g, std::string& err) {
+    std::ifstream f(path);
+    if (!f) { err = "cannot open " + path; return UNS_ERR_IO; }
+    long long nbk = 0, nx = 0, ny = 0, nz = 0;
+    if (!(f >> nbk)) { err = path + ": bad header"; return UNS_ERR_IO; }
+    if (nbk != 1) { err = "plot3d: only a single block is allowed"; return UNS_ERR_ARG; }
+    if (!(f >> nx >> ny >> nz) || nx < 5 || ny < 2 || nz != 1 || nx * ny > (1LL << 28)) {
+        err = path + ": bad block size (nx >= 5, ny >= 2, nz = 1)";
+        return UNS_ERR_IO;
+    }
+    const size_t n = (size_t)nx * ny;
+    std::vector<double> x(n), y(n);
+    for (size_t k = 0; k < n; ++k) if (!(f >> x[k])) { err = path + ": truncated x"; return UNS_ERR_IO; }
+    for (size_t k = 0; k < n; ++k) if (!(f >> y[k])) { err = path + ": truncated y"; return UNS_ERR_IO; }
+    double z;
+    for (size_t k = 0; k < n; ++k) if (!(f >> z)) { err = path + ": truncated z"; return UNS_ERR_IO; }
+    // the periodic column: i = nx repeats i = 1
+    double scale = 0.0;
+    for (size_t k = 0; k < n; ++k) scale = std::max(scale, std::max(std::fabs(x[k]), std::fabs(y[k])));
+    for (long long j = 0; j < ny; ++j) {
+        const size_t a = (size_t)j * nx, b = a + nx - 1;
+        if (std::fabs(x[a] - x[b]) > 1e-12 * scale || std::fabs(y[a] - y[b]) > 1e-12 * scale) {
+            err = "plot3d: not an O-grid (the last i column must repeat the first)";
+            return UNS_ERR_MESH;
+        }
+    }
+    g.I = (int)nx - 1;
+    g.J = (int)ny - 1;
+    g.x.assign((size_t)(g.J + 1) * g.I, 0.0);
+    g.y.assign((size_t)(g.J + 1) * g.I, 0.0);
+    for (int j = 0; j <= g.J; ++j)
+        for (int i = 0; i < g.I; ++i) {
+            g.x[(size_t)j * g.I + i] = x[(size_t)j * nx + i];
+            g.y[(size_t)j * g.I + i] = y[(size_t)j * nx + i];
+        }
+    return UNS_OK;
+}
+
+int read_plot3d_cc(const std::string& path, RawCC& m, std::string& err) {
+    OGrid g;
+    int rc = read_plot3d_ogrid(path, g, err);
+    if (rc) return rc;
+    return raw_cc_from_ogrid(g, m, err);
+}
+
+int read_plot3d_nc(const std::string& path, RawNC& m, std::string& err) {
+    OGrid g;
+    int rc = read_plot3d_ogrid(path, g, err);
+    if (rc) return rc;
+    return raw_nc_from_ogrid(g, m, err);
+}
+
+int write_plot3d_airfoil(const AirfoilSpec& s, const std::string& path, std::string& err) {
+    OGrid g;
+    int rc = build_ogrid(s, g, err);
+    if (rc) return rc;
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) { err = "cannot write " + path; return UNS_ERR_IO; }
+    const int nx = g.I + 1, ny = g.J + 1;
+    std::fprintf(f, "1\n%d %d 1\n", nx, ny);
+    for (int c = 0; c < 3; ++c) {
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const size_t k = (size_t)j * g.I + (i % g.I);
+                const double val = c == 0 ? g.x[k] : (c == 1 ? g.y[k] : 0.0);
+                std::fprintf(f, "%.17g\n", val);
+            }
+    }
+    if (std::fclose(f) != 0) { err = "write failed: " + path; return UNS_ERR_IO; }
     return UNS_OK;
 }
 

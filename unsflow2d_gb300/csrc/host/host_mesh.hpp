@@ -88,6 +88,11 @@ struct AirfoilSpec {
 int gen_airfoil_cc(const AirfoilSpec& s, RawCC& out, std::string& err);
 int gen_airfoil_nc(const AirfoilSpec& s, RawNC& out, std::string& err);
 
+// Single-block plot3d O-grid (MeshGen's input), triangulated as the generator does.
+int read_plot3d_cc(const std::string& path, RawCC& out, std::string& err);
+int read_plot3d_nc(const std::string& path, RawNC& out, std::string& err);
+int write_plot3d_airfoil(const AirfoilSpec& s, const std::string& path, std::string& err);
+
 int read_geometry_cc(const std::string& path, RawCC& out, std::string& err);
 int write_geometry_cc(const std::string& path, const RawCC& m, std::string& err);
 int read_geometry_nc(const std::string& path, RawNC& out, std::string& err);

@@ -37,6 +37,15 @@ class _HostMesh:
         abi.check(fn(str(path).encode(), C.byref(h)), lib, f"read {path}")
         return cls(h.value)
 
+    @classmethod
+    def plot3d(cls, path: str):
+        """A single-block plot3d O-grid (MeshGen's input), triangulated."""
+        lib = abi.host_lib()
+        h = C.c_void_p()
+        fn = getattr(lib, f"uns_host_{cls.kind}_plot3d")
+        abi.check(fn(str(path).encode(), C.byref(h)), lib, f"plot3d {path}")
+        return cls(h.value)
+
     def write(self, path: str) -> None:
         fn = getattr(self._lib, f"uns_host_{self.kind}_write")
         abi.check(fn(self._h, str(path).encode()), self._lib, f"write {path}")
@@ -90,6 +99,13 @@ class NCMesh(_HostMesh):
     @property
     def nnodes(self) -> int:
         return self.arrays["nop"]
+
+
+def write_airfoil_plot3d(path: str, ni: int, nj: int, thickness: float = 0.12, rfar: float = 20.0,
+                         dwall: float = 1e-3) -> None:
+    """The analytic airfoil O-grid as a single-block plot3d file."""
+    lib = abi.host_lib()
+    abi.check(lib.uns_host_airfoil_plot3d(ni, nj, thickness, rfar, dwall, str(path).encode()), lib, "plot3d write")
 
 
 def read_flo_inp(path: str, kind: str = "cc") -> tuple[abi.Params, str]:
