@@ -151,7 +151,7 @@ def peaks():
 # ---------------------------------------------------------------- bytes model
 def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
     """Unique bytes each kernel must move per launch: every array it touches
-    counted once at its full size, no credit for reuse (the design doc table).
+    counted once at its full size, no credit for reuse.
     mixed: the CCFVM mixed form's kernels, which read FP32 copies."""
     if kind == "nc":
         N, E = m["nop"], m["nof"]

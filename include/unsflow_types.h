@@ -5,8 +5,7 @@
  * module can mirror every struct field for field.
  *
  * Index convention: every index in these structs is 0-based.  A Fortran caller
- * subtracts 1 from cell/face/point numbers when it fills a view (see the
- * binding in INTEGRATION.md).
+ * subtracts 1 from cell/face/point numbers when it fills a view.
  */
 #ifndef UNSFLOW_TYPES_H
 #define UNSFLOW_TYPES_H

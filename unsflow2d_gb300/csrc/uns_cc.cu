@@ -1,6 +1,6 @@
 // uns_cc.cu -- cell-centred (CCFVM) residual-and-update hot path on GB300.
 //
-// Design (see the design doc for the roofline per kernel):
+// Design:
 //   * structure-of-arrays in HBM with small per-entity vectors: double4 for
 //     the four conserved / primitive / gradient / limiter values of a cell,
 //     so a gathered neighbour costs one 32-byte sector;
