@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 // this form (phi is a running minimum across iterations); k_unpack_f32
 // writes it back to the FP64 arrays when a caller reads them or the handle
 // leaves the form.
-__global__ void __launch_bounds__(kBlock) k_cell_grad_mixed(CCView v, int flags, double cfl_in) {
+__global__ void __launch_bounds__(kBlock, 5) k_cell_grad_mixed(CCView v, int flags, double cfl_in) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
     const int inst = cell_inst(v, i);
