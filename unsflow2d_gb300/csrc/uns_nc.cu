@@ -73,6 +73,7 @@ struct NCView {
     int nrec;
     double4* rec;    // per record, per LU-SGS call: 3 x double4 (k_nc_sweep_prep) or 4 x float4 (k_nc_sweep_prep_mixed)
     double* diag;    // LU-SGS diagonal cv/dt + 0.5*omega*la (lusgs.f90:36)
+    double* diaginv; // its FP64 reciprocal, read by the FP32 sweeps (a multiply on their critical path)
     double4* rec_a;  // sweep records [pass * nop + node]: (u, v, p, e*rho) of qc
     double4* rec_b;  //   and dqc; rho is rebuilt as qold.rho + dqc.rho
     double* partial;   // [2*nblk]: sum, max
@@ -296,6 +297,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_node_res(NCView v, double cfl_in,
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
         v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
+        v.diaginv[i] = 1.0 / v.diag[i];
         if (irk > 0) {
             double a = rk3_a(irk), b = rk3_b(irk);
             double dtbyarea = dt / v.cv[i];
@@ -518,7 +520,7 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
 struct SweepIn {
     double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
     int nb;
-    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
+    double D, o, r;  // lanes 0..3: the reciprocal of the node's diagonal, qold and res, variable k
 };
 
 __device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
@@ -697,7 +699,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
 struct SweepInM {
     float rho, ru, rv, E, u, v, p, un, nx, ny, ds, ol, sign;  // the slot's record
     int nb;
-    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
+    double D, o, r;  // lanes 0..3: the reciprocal of the node's diagonal, qold and res, variable k
 };
 
 __device__ __forceinline__ void sweep_load_edge_m(const NCView& v, int rec, SweepInM& x) {
@@ -712,6 +714,7 @@ __device__ __forceinline__ void sweep_load_edge_m(const NCView& v, int rec, Swee
 __device__ __forceinline__ void sweep_load_m(const NCView& v, const int4& S, int lane, SweepInM& x) {
     if ((lane >> 2) < S.w) sweep_load_edge_m(v, S.z + (lane >> 2), x);
     own_load(v, S, lane, x.D, x.o, x.r);
+    if (lane < 4) x.D = v.diaginv[S.x];  // the FP32 sweep multiplies by the FP64 reciprocal
 }
 
 // lusgs sweeps in the mixed form: the schedule, lanes, hand-offs and FP64
@@ -771,7 +774,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
             else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
         }
         if (__ballot_sync(full, !ok)) return;
-        const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
+        const double d = pass == 0 ? (-r - cres) * X.D : r - cres * X.D;
         const double q = X.o + d;
         spec = false;
         if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
@@ -1033,7 +1036,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
     ALN(qc, nop); ALN(qp, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
-    ALN(diag, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
+    ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
     ALN(err, 1);
     h->nparts = nblocks(nop);
     ALN(partial, 2 * h->nparts);
