@@ -520,7 +520,7 @@ __device__ __forceinline__ double pick4(int k, double a, double b, double c, dou
 struct SweepIn {
     double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
     int nb;
-    double D, o, r;  // lanes 0..3: the reciprocal of the node's diagonal, qold and res, variable k
+    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
 };
 
 __device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
