@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) { emx[j] = enc_ord(a[j]); emn[j] = emx[j]; }
         }
-        if (v.ninst) {  // packed instances: reduce over the lanes of each instance
+        if (v.ninst && blockIdx.x * blockDim.x >= v.noc) {  // ghost blocks of packed cases: per-case lane groups
             const unsigned grp = __match_any_sync(0xffffffffu, live ? inst : -1);
             unsigned long long mx[4], mn[4];
 #pragma unroll
@@ -136,12 +136,13 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
         if (l == 0)
             for (int j = 0; j < 4; ++j) { smx[w][j] = emx[j]; smn[w][j] = emn[j]; }
         __syncthreads();
-        if (threadIdx.x < 4) {
+        if (threadIdx.x < 4) {  // a block of one case (padded interior blocks of packed cases too)
+            const int bi = block_inst(v);
             int j = threadIdx.x;
             unsigned long long a = smx[0][j], b = smn[0][j];
             for (int k = 1; k < kBlock / 32; ++k) { a = smx[k][j] > a ? smx[k][j] : a; b = smn[k][j] < b ? smn[k][j] : b; }
-            atomicMax(&v.minmax[j], a);
-            atomicMin(&v.minmax[4 + j], b);
+            atomicMax(&v.minmax[8 * bi + j], a);
+            atomicMin(&v.minmax[8 * bi + 4 + j], b);
         }
     }
 }
