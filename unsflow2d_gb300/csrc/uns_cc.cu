@@ -321,6 +321,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         v.dt[i] = dt;
         v.dcv[i] = dt / v.cv[i];
         v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
+        v.diaginv[i] = 1.0 / v.diag[i];
         warp_atomic_min_u64(v, inst, enc_ord(dt));
     }
     double gx[4], gy[4];
@@ -466,6 +467,7 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell_grad_mixed(CCView v, int fla
         v.dt[i] = (double)dt;
         v.dcv[i] = (double)(dt / cvf);
         v.diag[i] = (double)(cvf / dt + 0.75f * la);
+        v.diaginv[i] = 1.0 / v.diag[i];
         warp_atomic_min_u64(v, inst, enc_ord((double)dt));
     }
     if (!(flags & (CG_GRAD | CG_LIM))) return;
@@ -1286,7 +1288,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
 struct SweepInM {
     float rho, ru, rv, E, u, v, p, un, nx, ny, area, ol;  // the slot's record
     int nb;
-    double D, o, r;  // lanes 0..3: the cell's diagonal, qold and res, variable k
+    double D, o, r;  // lanes 0..3: the reciprocal of the cell's diagonal, qold and res, variable k
 };
 
 __device__ __forceinline__ void sweep_load_face_m(const CCView& v, int rec, SweepInM& x) {
@@ -1301,10 +1303,12 @@ __device__ __forceinline__ void sweep_load_face_m(const CCView& v, int rec, Swee
 __device__ __forceinline__ void sweep_load_m(const CCView& v, const int4& S, int lane, SweepInM& x) {
     if ((lane >> 2) < S.w) sweep_load_face_m(v, S.z + (lane >> 2), x);
     own_load(v, S, lane, x.D, x.o, x.r);
+    if (lane < 4) x.D = v.diaginv[S.x];  // the FP32 sweep multiplies by the FP64 reciprocal
 }
 
 // lusgs2 sweeps in the mixed form: the schedule, lanes, hand-offs and FP64
-// sums / diagonal division of k_lusgs; FP32 delta-form face terms.
+// sums of k_lusgs, the diagonal as its FP64 reciprocal (formed with the
+// diagonal, off the sweep's critical path); FP32 delta-form face terms.
 __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1360,7 +1364,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
             else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
         }
         if (__ballot_sync(full, !ok)) return;
-        const double d = pass == 0 ? (-r - 0.5 * cres) / X.D : r - 0.5 * cres / X.D;
+        const double d = pass == 0 ? (-r - 0.5 * cres) * X.D : r - 0.5 * cres * X.D;
         const double q = X.o + d;
         spec = false;
         if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
@@ -1754,7 +1758,7 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     AL(pp, nop); AL(ppT, nop); AL(fq, nof); AL(fqT, nof); AL(fla, nof); AL(fmu, nof);
     AL(fF, nof); AL(fV, nof); AL(fgx, nof); AL(fgy, nof); AL(fgT, nof); AL(fasum, nof);
     AL(fwall, nbf); AL(fwallv, nbf);
-    AL(diag, noc); AL(rec_a, 2 * (size_t)noc); AL(rec_b, 2 * (size_t)noc);
+    AL(diag, noc); AL(diaginv, noc); AL(rec_a, 2 * (size_t)noc); AL(rec_b, 2 * (size_t)noc);
     UP(fgeof, fgeof); UP(fnaf, fnaf); UP(lswf, lswf);
     AL(qpf, ntot); AL(fqf, nof); AL(flaf, nof); AL(packf, 4 * (size_t)noc); AL(ppf, nop); AL(dcv, noc);
     { std::vector<float> t(m->v2c_wt, m->v2c_wt + m->v2c_off[nop]); UP(v2c_wtf, t); }

@@ -67,6 +67,7 @@ struct CCView {
     double2* fwall;   // per boundary face: wall convective (flux3, flux4)
     double2* fwallv;  // per boundary face: wall viscous (-flux3*A, -flux4*A)
     double* diag;     // lusgs2 diagonal cv/dt + 0.5*omega*la (lusgs.F90:236)
+    double* diaginv;  // its FP64 reciprocal (the FP32 sweep multiplies by it)
     // LU-SGS sweep schedule (host-built): per position of the warp lists
     // (it, pass, first record, records); per record, in the reference c2f
     // order of the taken faces: face, neighbour, 1 if the face normal points
