@@ -86,14 +86,16 @@ WORKLOADS = {
 }
 
 # Kernels launched per iteration (our own; memsets excluded).
-LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 12, ("cc", "lusgs"): 12}
+# CCFVM inviscid RK3: reset_minmax, begin, vertex_avg, face_prim_spec, cell_grad,
+# face_conv, cell_res (stage 1), cell_rk23_wall + cell_rk23 (stages 2-3), res_final.
+LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 10, ("cc", "lusgs"): 12}
 
 
 def cc_launches(p) -> int:
     """Kernels one CCFVM iteration launches (enqueue_iteration)."""
-    if p.time_mode != abi.TIME["rk3"] or p.flow_type != abi.FLOW["laminar"]:
-        return LAUNCHES[("cc", "rk3" if p.time_mode == abi.TIME["rk3"] else "lusgs")]
     ggfc = p.grad_type == abi.GRAD["ggfc"]
+    if p.time_mode != abi.TIME["rk3"] or p.flow_type != abi.FLOW["laminar"]:
+        return LAUNCHES[("cc", "rk3" if p.time_mode == abi.TIME["rk3"] else "lusgs")] + (1 if ggfc else 0)
     # reset_minmax, begin, vertex_avg, face_prim_spec, [face_ggfc], cell_grad,
     # 3 x (face_conv, cell_mul, [face_ggfc, (reset_minmax, begin), cell_grad], face_visc, cell_res), res_final
     per_stage = 4 + (0 if ggfc else 2 + (2 if p.ilimit else 0))
@@ -172,6 +174,7 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
         }
     N, F, P = m["noc"], m["nfi"] + m["nbf"], m["nop"]
     G = m["nbf"]
+    W = int((np.asarray(m["fbc"])[m["nfi"]:] == 1001).sum())  # wall faces
     if mixed:
         nnz = len(m["v2c"])
         return {
@@ -189,6 +192,10 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
             "face_conv": 8 * F + 32 * F + 64 * N + 32 * F + 72 * G,
             # face lists, FP64 fluxes, qc read+write, qold, res, dt/cv
             "cell_res": 16 * N + 32 * F + 32 * N * 4 + 8 * N,
+            # RK stages 2-3 in one pass: per cell the stored residual, qc read+write, qold, dt/cv and
+            # its wall bit; per wall face its neighbours, geometry, the 64-byte pack of its cell, ghost
+            # writes, wall force and flux, and its cell's face lists, stored fluxes and residual write
+            "cell_rk23": 136 * N + N // 8 + (300 + 148) * W,
             "residue": 8 * ((N + 255) // 256),
         }
     return {
@@ -199,6 +206,7 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
         "cell_grad": 4 * N + 12 * N + 8 * F + 40 * F + 24 * F + 16 * N + 64 * N + 32 * N + 40 * P + 16 * F + 32 * N * 2,
         "face_conv": 8 * F + 24 * F + 16 * F + 4 * G + 16 * (N + G) + 32 * (N + G) + 64 * N + 32 * N + 32 * F + 72 * G,
         "cell_res": 16 * N + 32 * F + 32 * N * 4 + 16 * N,
+        "cell_rk23": 136 * N + N // 8 + (364 + 148) * W,
         "residue": 8 * ((N + 255) // 256),
     }
 
@@ -215,12 +223,17 @@ TRAFFIC_PER_UNIT = {
 }
 
 
-def launches_per_iter(kind: str, rk3: bool, laminar: bool) -> dict:
-    """How many launches of each profiled phase one iteration makes."""
+def launches_per_iter(kind: str, rk3: bool, laminar: bool, irs: bool = False) -> dict:
+    """How many launches of each profiled phase one iteration makes.  An
+    inviscid CCFVM RK3 step without smoothing computes its face fluxes once
+    (stage 1) and runs stages 2 and 3 as one pass over the cells (cell_rk23),
+    recomputing only the wall faces' fluxes."""
     n = 3 if rk3 else 1
     if kind == "nc":
         return {"grad_lim": n, "edge": n, "node_res": n}
-    return {"face_conv": n, "cell_res": n, "viscous": n if laminar else 0, "cirs": n}
+    if rk3 and not laminar and not irs:
+        return {"face_conv": 1, "cell_res": 1, "cell_rk23": 1, "viscous": 0, "cirs": 0}
+    return {"face_conv": n, "cell_res": n, "viscous": n if laminar else 0, "cirs": n, "cell_rk23": 0}
 
 
 # ---------------------------------------------------------------- accuracy
@@ -548,7 +561,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     nbytes = algorithmic_bytes(kind, m.arrays, mixed_cc)
     peak, peak_src = peaks()
     dom = max(prof, key=prof.get)
-    nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"])
+    nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"], p.irs != 0)
     per_launch = {k: v / max(nl.get(k, 1), 1) for k, v in prof.items()}  # ms per launch
     rl_kernel = max((k for k in nbytes if k in prof and prof[k] > 0), key=lambda k: prof[k])
     achieved = nbytes[rl_kernel] / (per_launch[rl_kernel] * 1e-3) / 1e9

@@ -581,47 +581,18 @@ __device__ __forceinline__ bool flux_dispatch(const Gas& g, R nx, R ny, R area, 
     return face_flux<R>(g, nx, ny, area, ql, qr, F);
 }
 
+// Boundary face f of cell `in` (fvresidual.F90:27-101): the reconstructed
+// state of the cell (the FP32 pack of record in the mixed form), the farfield
+// or wall ghost from it and, for a wall, from the cell's conserved state cin;
+// writes the ghost cell, the wall force and the flux, and returns the flux.
 template <class R>
-__global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= v.nof) return;
-    const int inst = face_inst(v, f);
-    if (stopped(v, inst)) return;
-    const Gas& g = gas_of(v, inst);
-    if constexpr (std::is_same<R, float>::value) {
-        if (f < v.nfi) {  // interior face of the mixed form: FP32 packs and geometry only
-            const int2 nb = v.fnb[f];
-            const float4* A = v.packf + 4 * (size_t)nb.x;
-            const float4* B = v.packf + 4 * (size_t)nb.y;
-            const float4 qa = A[0], ga = A[1], ha = A[2], pa = A[3];
-            const float4 qb = B[0], gb = B[1], hb = B[2], pb = B[3];
-            const float4 d = v.fgeof[f], na = v.fnaf[f];
-            const float zhi = 1.f / 3.f, zlo = 1.f - 1.f / 3.f;
-            const float qi[4] = {qa.x, qa.y, qa.z, qa.w}, qo[4] = {qb.x, qb.y, qb.z, qb.w};
-            const float gxi[4] = {ga.x, ga.y, ga.z, ga.w}, gyi[4] = {ha.x, ha.y, ha.z, ha.w};
-            const float gxo[4] = {gb.x, gb.y, gb.z, gb.w}, gyo[4] = {hb.x, hb.y, hb.z, hb.w};
-            const float phi_i[4] = {pa.x, pa.y, pa.z, pa.w}, phi_o[4] = {pb.x, pb.y, pb.z, pb.w};
-            V4<float> ql, qr, F;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
-                const float beta = qo[j] - qi[j];
-                ql[j] = qi[j] + 0.5f * phi_i[j] * (zhi * beta + zlo * (gxi[j] * d.x + gyi[j] * d.y));
-                qr[j] = qo[j] + 0.5f * phi_o[j] * (zhi * -beta + zlo * (gxo[j] * d.z + gyo[j] * d.w));
-            }
-            bool ok = flux_dispatch<float>(g, na.x, na.y, na.z, ql, qr, F);
-            if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
-            v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
-            return;
-        }
-    }
-    int2 nb = v.fnb[f];
-    int in = nb.x, out = nb.y;
-    double2 n = v.fn[f];
-    double area = v.farea[f];
-    double2 fc = v.fcen[f];
-    double2 ci = v.cen[in];
+__device__ __forceinline__ double4 bnd_face_flux(const CCView& v, const Gas& g, int f, int in, const double cin4[4]) {
+    const double2 n = v.fn[f];
+    const double area = v.farea[f];
+    const double2 fc = v.fcen[f];
+    const double2 ci = v.cen[in];
     double qi[4], gxi[4], gyi[4], phi_i[4];
-    if constexpr (std::is_same<R, float>::value) {  // boundary face of the mixed form: the pack of record
+    if constexpr (std::is_same<R, float>::value) {
         const float4* A = v.packf + 4 * (size_t)in;
         const float4 a0 = A[0], a1 = A[1], a2 = A[2], a3 = A[3];
         qi[0] = a0.x; qi[1] = a0.y; qi[2] = a0.z; qi[3] = a0.w;
@@ -634,44 +605,18 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
         d4get(v.gy[in], gyi);
         d4get(v.phi[in], phi_i);
     }
-    V4<R> ql, qr, F;
-    if (f < v.nfi) {
-        double2 co = v.cen[out];
-        double qo[4], gxo[4], gyo[4], phi_o[4];
-        d4get(v.qp[out], qo);
-        d4get(v.gx[out], gxo);
-        d4get(v.gy[out], gyo);
-        d4get(v.phi[out], phi_o);
-        const double zhi = 1.0 / 3.0;
-        double dl0 = fc.x - ci.x, dl1 = fc.y - ci.y;
-        double dr0 = fc.x - co.x, dr1 = fc.y - co.y;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
-            double alfa = gxi[j] * dl0 + gyi[j] * dl1;
-            double beta = qo[j] - qi[j];
-            ql[j] = (R)(qi[j] + 0.5 * phi_i[j] * (zhi * beta + (1.0 - zhi) * alfa));
-            alfa = gxo[j] * dr0 + gyo[j] * dr1;
-            beta = qi[j] - qo[j];
-            qr[j] = (R)(qo[j] + 0.5 * phi_o[j] * (zhi * beta + (1.0 - zhi) * alfa));
-        }
-        bool ok = flux_dispatch<R>(g, (R)n.x, (R)n.y, (R)area, ql, qr, F);
-        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
-        v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
-        return;
-    }
-    // boundary face
-    int bc = v.fbc[f];
-    double d0 = fc.x - ci.x, d1 = fc.y - ci.y;
+    const int bc = v.fbc[f];
+    const double d0 = fc.x - ci.x, d1 = fc.y - ci.y;
     V4<double> qcl;
 #pragma unroll
     for (int j = 0; j < 4; ++j) qcl[j] = qi[j] + phi_i[j] * (gxi[j] * d0 + gyi[j] * d1);
     double4 Fd = make_double4(0.0, 0.0, 0.0, 0.0);
     if (bc == 2001 || bc == 1001) {
-        V4<double> cin = {0.0, 0.0, 0.0, 0.0};
-        if (bc == 1001) { double4 c = v.qc[in]; cin = V4<double>{c.x, c.y, c.z, c.w}; }
+        const V4<double> cin = {cin4[0], cin4[1], cin4[2], cin4[3]};
         CCBnd<double> b = cc_boundary<double, R>(g, bc, n.x, n.y, area, qcl, cin, g.u_inf, g.v_inf);
         if (!b.ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
         Fd = make_double4(b.F[0], b.F[1], b.F[2], b.F[3]);
+        const int out = v.fnb[f].y;
         v.qc[out] = make_double4(b.gq[0], b.gq[1], b.gq[2], b.gq[3]);
         v.qp[out] = make_double4(b.gp[0], b.gp[1], b.gp[2], b.gp[3]);
         v.qT[out] = b.gT;
@@ -679,6 +624,81 @@ __global__ void __launch_bounds__(kBlock) k_face_conv(CCView v) {
         if (bc == 1001) v.fwall[f - v.nfi] = make_double2(Fd.z, Fd.w);
     }
     v.fF[f] = Fd;
+    return Fd;
+}
+
+// One thread per face; the first blocks take the boundary faces, whose FP64
+// ghost arithmetic is the longest per thread, so that they run beside the
+// interior faces instead of after them.
+template <class R>
+__global__ void __launch_bounds__(kBlock, std::is_same<R, float>::value ? 4 : 1) k_face_conv(CCView v) {
+    const int nbb = (v.nbf + kBlock - 1) / kBlock;
+    const bool bnd = (int)blockIdx.x < nbb;
+    const int f = bnd ? v.nfi + blockIdx.x * kBlock + threadIdx.x : (blockIdx.x - nbb) * kBlock + threadIdx.x;
+    if (f >= (bnd ? v.nof : v.nfi)) return;
+    const int inst = face_inst(v, f);
+    if (stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
+    const int2 nb = v.fnb[f];
+    if (bnd) {
+        double cin[4] = {0.0, 0.0, 0.0, 0.0};
+        if (v.fbc[f] == 1001) d4get(v.qc[nb.x], cin);
+        bnd_face_flux<R>(v, g, f, nb.x, cin);
+        return;
+    }
+    if constexpr (std::is_same<R, float>::value) {  // interior face of the mixed form: FP32 packs and geometry only
+        const float4* A = v.packf + 4 * (size_t)nb.x;
+        const float4* B = v.packf + 4 * (size_t)nb.y;
+        const float4 qa = A[0], ga = A[1], ha = A[2], pa = A[3];
+        const float4 qb = B[0], gb = B[1], hb = B[2], pb = B[3];
+        const float4 d = v.fgeof[f], na = v.fnaf[f];
+        const float zhi = 1.f / 3.f, zlo = 1.f - 1.f / 3.f;
+        const float qi[4] = {qa.x, qa.y, qa.z, qa.w}, qo[4] = {qb.x, qb.y, qb.z, qb.w};
+        const float gxi[4] = {ga.x, ga.y, ga.z, ga.w}, gyi[4] = {ha.x, ha.y, ha.z, ha.w};
+        const float gxo[4] = {gb.x, gb.y, gb.z, gb.w}, gyo[4] = {hb.x, hb.y, hb.z, hb.w};
+        const float phi_i[4] = {pa.x, pa.y, pa.z, pa.w}, phi_o[4] = {pb.x, pb.y, pb.z, pb.w};
+        V4<float> ql, qr, F;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
+            const float beta = qo[j] - qi[j];
+            ql[j] = qi[j] + 0.5f * phi_i[j] * (zhi * beta + zlo * (gxi[j] * d.x + gyi[j] * d.y));
+            qr[j] = qo[j] + 0.5f * phi_o[j] * (zhi * -beta + zlo * (gxo[j] * d.z + gyo[j] * d.w));
+        }
+        bool ok = flux_dispatch<float>(g, na.x, na.y, na.z, ql, qr, F);
+        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        v.fF[f] = make_double4((double)F[0], (double)F[1], (double)F[2], (double)F[3]);
+    } else {
+        const int in = nb.x, out = nb.y;
+        const double2 n = v.fn[f];
+        const double area = v.farea[f];
+        const double2 fc = v.fcen[f];
+        const double2 ci = v.cen[in], co = v.cen[out];
+        double qi[4], gxi[4], gyi[4], phi_i[4], qo[4], gxo[4], gyo[4], phi_o[4];
+        d4get(v.qp[in], qi);
+        d4get(v.gx[in], gxi);
+        d4get(v.gy[in], gyi);
+        d4get(v.phi[in], phi_i);
+        d4get(v.qp[out], qo);
+        d4get(v.gx[out], gxo);
+        d4get(v.gy[out], gyo);
+        d4get(v.phi[out], phi_o);
+        const double zhi = 1.0 / 3.0;
+        double dl0 = fc.x - ci.x, dl1 = fc.y - ci.y;
+        double dr0 = fc.x - co.x, dr1 = fc.y - co.y;
+        V4<double> ql, qr, F;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {  // recon (fvresidual.F90:235-247)
+            double alfa = gxi[j] * dl0 + gyi[j] * dl1;
+            double beta = qo[j] - qi[j];
+            ql[j] = qi[j] + 0.5 * phi_i[j] * (zhi * beta + (1.0 - zhi) * alfa);
+            alfa = gxo[j] * dr0 + gyo[j] * dr1;
+            beta = qi[j] - qo[j];
+            qr[j] = qo[j] + 0.5 * phi_o[j] * (zhi * beta + (1.0 - zhi) * alfa);
+        }
+        bool ok = flux_dispatch<double>(g, n.x, n.y, area, ql, qr, F);
+        if (!ok) set_err(v.err, UNS_ERR_NEG_SOUND_SPEED, f);
+        v.fF[f] = make_double4(F[0], F[1], F[2], F[3]);
+    }
 }
 
 // Sutherland viscosity of every interior cell (viscous_flux.F90:478-480,585-597).
@@ -845,6 +865,133 @@ __global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, in
             for (int k = threadIdx.x + 32; k < kBlock; k += 32) t = t + sh[k];
             t = warp_sum(t);
             if (threadIdx.x == 0) v.partial[blockIdx.x] = t;
+        }
+    }
+}
+
+// RK stages 2 and 3 of an inviscid step in one pass over the cells.  Those
+// stages' interior and farfield face fluxes equal the first stage's: their
+// inputs -- the cells' primitives, gradient and limiter -- are formed once
+// per time step (main.F90:62-84) and the farfield ghost is built from them
+// alone; only a wall ghost reads the stage's conserved state (slip_wall /
+// NoSlip_wall, boundCond.F90:19-81).  So a cell without a wall face keeps the
+// first stage's residual in both stages, and a wall cell's residual changes
+// only through its own wall faces, whose fluxes its thread recomputes from
+// the cell's stage state.  Each stage update and the last stage's norm
+// partial are evaluated as in the stage-by-stage sequence (k_cell_res for the
+// FP64 form, k_cell_res_mixed for the mixed form), so states, residuals,
+// ghosts and norms are the same bit for bit.
+template <bool kMixed>
+__device__ __forceinline__ void rk_update(int irk, double D, const double o[4], const double r[4], double q[4]) {
+    const double a = rk3_a(irk), b = rk3_b(irk);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (kMixed) q[j] = __fma_rn(a, o[j], b * __fma_rn(-D, r[j], q[j]));
+        else q[j] = a * o[j] + b * (q[j] - D * r[j]);
+    }
+}
+
+// The residual of wall cell i at stage state q: its wall faces' fluxes
+// recomputed (ghosts, wall force and fF written), the other faces' stored.
+template <class R>
+__device__ __forceinline__ void wall_cell_res(const CCView& v, const Gas& g, int i, const double q[4], double r[4]) {
+    const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+    auto flux = [&](int f) -> double4 {
+        return (f >= v.nfi && v.fbc[f] == 1001) ? bnd_face_flux<R>(v, g, f, i, q) : v.fF[f];
+    };
+    if constexpr (std::is_same<R, float>::value) {  // k_cell_res_mixed's order
+        for (int k = k0; k < k1; ++k) {
+            const int e = v.cf[k], f = e & FACE_MASK;
+            const double4 F = flux(f);
+            const double s = (f < v.nfi && (e & SIDE_BIT)) ? -1.0 : 1.0;
+            if (k == k0) { r[0] = s * F.x; r[1] = s * F.y; r[2] = s * F.z; r[3] = s * F.w; }
+            else { r[0] = __fma_rn(s, F.x, r[0]); r[1] = __fma_rn(s, F.y, r[1]); r[2] = __fma_rn(s, F.z, r[2]); r[3] = __fma_rn(s, F.w, r[3]); }
+        }
+    } else {  // k_cell_res's order: boundary faces first
+        r[0] = r[1] = r[2] = r[3] = 0.0;
+        for (int k = k0; k < k1; ++k) {
+            const int f = v.cf[k] & FACE_MASK;
+            if (f >= v.nfi) add4(r, flux(f));
+        }
+        for (int k = k0; k < k1; ++k) {
+            const int e = v.cf[k], f = e & FACE_MASK;
+            if (f < v.nfi) { if (e & SIDE_BIT) sub4(r, v.fF[f]); else add4(r, v.fF[f]); }
+        }
+    }
+}
+
+// Stages 2 and 3 of cell i (instance inst): the stage updates and, for a
+// wall cell, its residual in each stage; returns the squared residual that
+// the last stage's norm takes.
+template <class R, bool kWall>
+__device__ __forceinline__ double rk23_cell(const CCView& v, int i, int inst) {
+    constexpr bool kMixed = std::is_same<R, float>::value;
+    double r[4], q[4], o[4];
+    d4get(v.res[i], r);
+    d4get(v.qc[i], q);
+    d4get(v.qold[i], o);
+    const double D = v.dcv[i];
+    for (int irk = 2; irk <= 3; ++irk) {
+        if (kWall) wall_cell_res<R>(v, gas_of(v, inst), i, q, r);
+        rk_update<kMixed>(irk, D, o, r, q);
+    }
+    if (kWall) v.res[i] = d4(r);
+    v.qc[i] = d4(q);
+    if (kMixed) return __fma_rn(r[3], r[3], __fma_rn(r[2], r[2], __fma_rn(r[1], r[1], r[0] * r[0])));
+    return r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+}
+
+// The wall cells (v.wcell), one per thread in one-warp blocks so that their
+// long FP64 chains spread over the SMs; they run before k_cell_rk23.
+template <class R>
+__global__ void __launch_bounds__(32) k_cell_rk23_wall(CCView v) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= v.nwcell) return;
+    const int i = v.wcell[t];
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
+    rk23_cell<R, true>(v, i, inst);
+}
+
+// Every other cell: a stream over the stored residual and states; the wall
+// cells contribute the last-stage residual k_cell_rk23_wall stored.  The norm
+// partial is reduced as the stage-by-stage kernels reduce it.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_cell_rk23(CCView v) {
+    constexpr bool kMixed = std::is_same<R, float>::value;
+    if (stopped(v, block_inst(v))) return;  // blocks of cells are instance-pure
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int inst = i < v.noc ? cell_inst(v, i) : -1;
+    double rr = 0.0;
+    if (inst >= 0) {
+        if ((__ldg(v.bcell + (i >> 5)) >> (i & 31)) & 1u) {
+            double r[4];
+            d4get(v.res[i], r);
+            if (kMixed) rr = __fma_rn(r[3], r[3], __fma_rn(r[2], r[2], __fma_rn(r[1], r[1], r[0] * r[0])));
+            else rr = r[0] * r[0] + r[1] * r[1] + r[2] * r[2] + r[3] * r[3];
+        } else {
+            rr = rk23_cell<R, false>(v, i, inst);
+        }
+    }
+    if (kMixed) {  // k_cell_res_mixed's block reduction
+        __shared__ double sh[kBlock];
+        sh[threadIdx.x] = rr;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = sh[threadIdx.x];
+            for (int k = threadIdx.x + 32; k < kBlock; k += 32) t = t + sh[k];
+            t = warp_sum(t);
+            if (threadIdx.x == 0) v.partial[blockIdx.x] = t;
+        }
+    } else {  // k_cell_res's
+        __shared__ double s[kBlock / 32];
+        rr = warp_sum(rr);
+        if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = rr;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int k = 0; k < kBlock / 32; ++k) t = t + s[k];
+            v.partial[blockIdx.x] = t;
         }
     }
 }
@@ -1446,6 +1593,14 @@ int enqueue_minmax(uns_cc_handle* h, CCView& v) {
 }
 
 // k_cell_grad, or its FP32 form for a handle in the mixed form.
+// k_face_conv's grid: the boundary faces' blocks, then the interior faces'.
+#define LAUNCH_FACE_CONV(R, v)                                                                     \
+    do {                                                                                           \
+        const int nb_ = std::max(1, (int)(((v).nbf + kBlock - 1) / kBlock) + nblocks((v).nfi));    \
+        k_face_conv<R><<<nb_, kBlock, 0, h->stream>>>(v);                                          \
+        UNS_CUDA(cudaGetLastError());                                                              \
+    } while (0)
+
 #define LAUNCH_CELL_GRAD(v, flags, cfl)                                                 \
     do {                                                                               \
         if ((v).mixed) LAUNCH(k_cell_grad_mixed, (v).noc, (v), (int)(flags), (cfl));   \
@@ -1465,11 +1620,33 @@ double epsirs_of(const uns_cc_handle* h, double cfl) {
     return std::max(0.25 * (r * r - 1.0), 0.0);
 }
 
+// Whether the main loop's RK3 step runs stages 2 and 3 as one pass over the
+// cells (k_cell_rk23): an inviscid flow without a smoothing sweep (a viscous
+// stage recomputes the cell gradient and viscosity from the stage's state; a
+// smoothing sweep replaces the residual that the pass reuses).
+bool rk23_in_one_pass(const uns_cc_handle* h, const CCView& v, double cfl) {
+    const double eps = v.irs ? epsirs_of(h, cfl) : 0.0;
+    return h->P.time_mode == UNS_TIME_RK3 && !v.laminar && !(v.irs && eps > 0.0);
+}
+
+// RK stages 2 and 3 in one pass over the cells: the wall cells first.
+int enqueue_rk23(uns_cc_handle* h, CCView& v) {
+    if (v.nwcell > 0) {
+        const int nb = (v.nwcell + 31) / 32;
+        if (v.mixed) k_cell_rk23_wall<float><<<nb, 32, 0, h->stream>>>(v);
+        else k_cell_rk23_wall<double><<<nb, 32, 0, h->stream>>>(v);
+        UNS_CUDA(cudaGetLastError());
+    }
+    if (v.mixed) LAUNCH(k_cell_rk23<float>, v.noc, v);
+    else LAUNCH(k_cell_rk23<double>, v.noc, v);
+    return UNS_OK;
+}
+
 // fvresidual as a kernel sequence; irk > 0 fuses that RK stage into the
 // residual gather (only when no smoothing sweep sits in between).
 int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int partial, bool* fused) {
-    if (h->P.precision == UNS_PREC_MIXED) LAUNCH(k_face_conv<float>, v.nof, v);
-    else LAUNCH(k_face_conv<double>, v.nof, v);
+    if (h->P.precision == UNS_PREC_MIXED) LAUNCH_FACE_CONV(float, v);
+    else LAUNCH_FACE_CONV(double, v);
     if (v.laminar) {
         LAUNCH(k_cell_mul, v.noc, v);
         if (v.grad_type != UNS_GRAD_GGFC) {
@@ -1535,7 +1712,11 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
     LAUNCH(k_face_prim_spec, v.nof, v);
     if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
     LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.0);
-    if (h->P.time_mode == UNS_TIME_RK3) {
+    if (rk23_in_one_pass(h, v, cfl_for_eps)) {
+        bool fused = false;
+        if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 1, 0, &fused))) return rc;
+        if ((rc = enqueue_rk23(h, v))) return rc;
+    } else if (h->P.time_mode == UNS_TIME_RK3) {
         for (int irk = 1; irk <= 3; ++irk) {
             bool fused = false;
             if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, irk, irk == 3, &fused))) return rc;
@@ -1577,7 +1758,7 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
     if ((rc = hook(h, REC_AFTER_START, 0, ctx))) return rc;
     for (int irk = 1; irk <= 3; ++irk) {
         if ((rc = hook(h, REC_BEFORE_FACE_CONV, irk, ctx))) return rc;
-        LAUNCH(k_face_conv<double>, v.nof, v);
+        LAUNCH_FACE_CONV(double, v);
         if (v.laminar) {
             if ((rc = hook(h, REC_BEFORE_CELL_MUL, irk, ctx))) return rc;
             LAUNCH(k_cell_mul, v.noc, v);
@@ -1749,6 +1930,18 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     UP(lsw, lsw);
     { std::vector<int> t(m->nc2c, m->nc2c + noc); UP(nc2c, t); }
     UP(cf_off, cnt); UP(cf, cf);
+    {  // wall cells: a bit per cell and their list
+        std::vector<unsigned> t((noc + 31) / 32, 0u);
+        std::vector<int> wc;
+        for (int f = nfi; f < nof; ++f) {
+            const int c = m->fin[f];
+            if (m->fbc[f] == 1001 && c >= 0 && c < noc) t[c >> 5] |= 1u << (c & 31);
+        }
+        for (int c = 0; c < noc; ++c)
+            if ((t[c >> 5] >> (c & 31)) & 1u) wc.push_back(c);
+        UP(bcell, t); UP(wcell, wc);
+        v.nwcell = (int)wc.size();
+    }
     UP(rc2f_off, rc2f_off); UP(rc2f, rc2f);
     { std::vector<int> t(m->v2c_off, m->v2c_off + nop + 1); UP(v2c_off, t); }
     { std::vector<int> t(m->v2c, m->v2c + m->v2c_off[nop]); UP(v2c, t); }
@@ -2339,8 +2532,8 @@ void* uns_cc_stream(uns_cc_handle* h) { return h ? (void*)h->stream : nullptr; }
 
 int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
     static const char* kNames[] = {"begin", "vertex_avg", "face_prim_spec", "face_ggfc", "cell_grad", "face_conv",
-                                   "viscous", "cell_res", "cirs", "lusgs_sweeps", "residue"};
-    const int NP = 11;
+                                   "viscous", "cell_res", "cirs", "lusgs_sweeps", "residue", "cell_rk23"};
+    const int NP = 12;
     if (!h || reps < 1 || !ms) return UNS_ERR_ARG;
     std::vector<double> acc(NP, 0.0);
     cudaEvent_t e0, e1;
@@ -2373,10 +2566,11 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
         if (!rc) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
         if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
         if (!rc) rc = timed(4, [&]() -> int { LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), cfl); return UNS_OK; });
-        for (int irk = 1; irk <= (rk3 ? 3 : 1) && !rc; ++irk) {
+        const bool one_pass = rk23_in_one_pass(h, v, cfl);
+        for (int irk = 1; irk <= (rk3 && !one_pass ? 3 : 1) && !rc; ++irk) {
             rc = timed(5, [&]() -> int {
-                if (h->P.precision == UNS_PREC_MIXED) LAUNCH(k_face_conv<float>, v.nof, v);
-                else LAUNCH(k_face_conv<double>, v.nof, v);
+                if (h->P.precision == UNS_PREC_MIXED) LAUNCH_FACE_CONV(float, v);
+                else LAUNCH_FACE_CONV(double, v);
                 return UNS_OK;
             });
             if (!rc && v.laminar) rc = timed(6, [&]() -> int {
@@ -2392,8 +2586,8 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
             });
             int fuse = (rk3 && !smooth) ? irk : 0;
             if (!rc) rc = timed(7, [&]() -> int {
-                if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, smooth ? 0 : 1);
-                else LAUNCH(k_cell_res, v.noc, v, fuse, smooth ? 0 : 1);
+                if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
+                else LAUNCH(k_cell_res, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
                 return UNS_OK;
             });
             if (!rc && smooth) rc = timed(8, [&]() -> int {
@@ -2405,6 +2599,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
                 return UNS_OK;
             });
         }
+        if (!rc && one_pass) rc = timed(11, [&]() -> int { return enqueue_rk23(h, v); });
         if (!rc && !rk3) rc = timed(9, [&]() -> int { return enqueue_lusgs(h, v); });
         if (!rc) rc = timed(10, [&]() -> int {
             k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);

@@ -33,6 +33,9 @@ struct CCView {
     const int* nc2c;
     const int* cf_off;    // index-sorted faces per cell, SIDE_BIT for `out`
     const int* cf;
+    const unsigned* bcell;  // bit i: interior cell i has a wall face
+    const int* wcell;       // those cells in increasing order
+    int nwcell;
     const int* rc2f_off;  // reference c2f order (LU-SGS)
     const int* rc2f;
     const int* v2c_off;
