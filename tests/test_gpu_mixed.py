@@ -41,6 +41,25 @@ def test_cc_mixed_tracks_fp64(case):
     assert np.max(np.abs(qb - qa)) <= 1e-4 * np.max(np.abs(qa))
 
 
+def test_cc_mixed_cell_side_gradient_equals_face_pass():
+    """The graph step of the mixed Green-Gauss form forms face averages and
+    radii inside the cell gradient pass from cell-side records; the
+    per-routine calls run the face pass (k_face_prim_spec) and then the cell
+    pass.  From the same state both give the same dt, gradient, limiter and
+    face radii bit for bit."""
+    m = mesh.CCMesh.airfoil(32, 16)
+    p = abi.make_params(flux="roe", grad="gg", m_inf=0.7, aoa_deg=2.0, precision="mixed")
+    cfl = mesh.cfl_schedule(p, 1, 21, "cc")
+    a, b = CCSolver(m, p), CCSolver(m, p)
+    a.iterate(cfl[:20], first_iter=True)
+    b.iterate(cfl[:20], first_iter=True)
+    assert np.array_equal(a.get_state(), b.get_state())
+    a.iterate(cfl[20:], first_iter=False)
+    b.iteration(cfl[20])
+    for name in ("dt", "la", "grad", "phi", "fla"):
+        assert np.array_equal(a.get(name), b.get(name)), name
+
+
 @pytest.mark.parametrize("case", [
     dict(flux="vanleer", limiter="vkn", time="rk3", cfl_max=0.9, m_inf=0.6, aoa_deg=2.89),
     dict(flux="ausm", limiter="barth_corrected", time="lusgs", cfl_max=50.0, m_inf=0.8, aoa_deg=1.25),

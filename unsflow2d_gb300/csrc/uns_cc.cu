@@ -294,7 +294,9 @@ __device__ __forceinline__ double4 d4(const double o[4]) { return make_double4(o
 // gradient.F90:399-443, Gradient_GG_FC :511-564, Gradient_LSQR :308-377) and
 // limiter_VKN1 (limiter.F90:146-279).  Face order is the reference's loop
 // order (interior faces, then boundary faces).
-enum { CG_DT = 1, CG_GRAD = 2, CG_LIM = 4 };
+// CG_DIAG: also the LU-SGS diagonal and its reciprocal (with CG_DT; only an
+// LU-SGS step reads them).
+enum { CG_DT = 1, CG_GRAD = 2, CG_LIM = 4, CG_DIAG = 8 };
 
 // atomicMin of an order-encoded dt into its instance's slot with one atomic
 // per converged group of lanes of one instance.  Same result as one atomic
@@ -320,8 +322,10 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
         double dt = cfl * v.cv[i] / la;
         v.dt[i] = dt;
         v.dcv[i] = dt / v.cv[i];
-        v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
-        v.diaginv[i] = 1.0 / v.diag[i];
+        if (flags & CG_DIAG) {
+            v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
+            v.diaginv[i] = 1.0 / v.diag[i];
+        }
         warp_atomic_min_u64(v, inst, enc_ord(dt));
     }
     double gx[4], gy[4];
@@ -466,8 +470,10 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell_grad_mixed(CCView v, int fla
         v.la[i] = (double)la;
         v.dt[i] = (double)dt;
         v.dcv[i] = (double)(dt / cvf);
-        v.diag[i] = (double)(cvf / dt + 0.75f * la);
-        v.diaginv[i] = 1.0 / v.diag[i];
+        if (flags & CG_DIAG) {
+            v.diag[i] = (double)(cvf / dt + 0.75f * la);
+            v.diaginv[i] = 1.0 / v.diag[i];
+        }
         warp_atomic_min_u64(v, inst, enc_ord((double)dt));
     }
     if (!(flags & (CG_GRAD | CG_LIM))) return;
@@ -556,6 +562,97 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell_grad_mixed(CCView v, int fla
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 const float D_L = gx[j] * d0 + gy[j] * d1;
+                float phi0 = 1.f;
+                if (D_L != 0.f) {  // limiter.F90:286-294 with a = (umax or umin) - qi, b = D_L
+                    const float a = (D_L > 0.f ? umax[j] : umin[j]) - qi[j];
+                    const float nr = a * a + 2.f * a * D_L + tol[j];
+                    const float dr = a * a + 2.f * D_L * D_L + a * D_L + tol[j];
+                    phi0 = __fdividef(nr, dr);
+                }
+                ph[j] = rmin(ph[j], phi0);
+            }
+        }
+    }
+    v.packf[4 * (size_t)i] = q4;
+    v.packf[4 * (size_t)i + 1] = make_float4(gx[0], gx[1], gx[2], gx[3]);
+    v.packf[4 * (size_t)i + 2] = make_float4(gy[0], gy[1], gy[2], gy[3]);
+    v.packf[4 * (size_t)i + 3] = make_float4(ph[0], ph[1], ph[2], ph[3]);
+}
+
+// k_face_prim_spec + k_cell_grad_mixed for the Green-Gauss gradient of an
+// inviscid flow in the mixed form, as one gather per cell.  Each of the
+// cell's faces is described by a cell-side record (v.sideg / v.sidei, in the
+// cell's face order): the unit normal signed outward as Gradient_GG counts it,
+// the centre-to-midpoint offset of this side, the cell across the face (-1 on
+// a boundary) and the face's end points.  The face average and spectral
+// radius are formed from the end points' vertex values with the operations of
+// k_face_prim_spec (the sign of the normal drops out of |u.n|), so the
+// records stream in order and the only gathers are the vertex values and the
+// neighbours' primitives.  dt, the gradient, the limiter and the pack are
+// those of k_cell_grad_mixed, bit for bit.
+__global__ void __launch_bounds__(kBlock, 4) k_cell_grad_side(CCView v, int flags, double cfl_in) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.noc) return;
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
+    const Gas& g = gas_of(v, inst);
+    const float gam = (float)g.gamma;
+    const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+    const float4 q4 = v.qpf[i];
+    const float qi[4] = {q4.x, q4.y, q4.z, q4.w};
+    float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+    float umax[4] = {qi[0], qi[1], qi[2], qi[3]}, umin[4] = {qi[0], qi[1], qi[2], qi[3]};
+    float la = 0.f;
+    for (int k = k0; k < k1; ++k) {
+        const float4 sg = v.sideg[k];
+        const int4 si = v.sidei[k];
+        const float area = __int_as_float(si.w);
+        const float4 a = v.ppf[si.y], b = v.ppf[si.z];
+        const float4 u = si.x >= 0 ? v.qpf[si.x] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 q = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z), 0.5f * (a.w + b.w));
+        const float a0 = sqrtf(gam * q.w / q.x);
+        la = la + area * (fabsf(q.y * sg.x + q.z * sg.y) + a0);
+        const float dx = sg.x * area, dy = sg.y * area;
+        gx[0] += q.x * dx; gx[1] += q.y * dx; gx[2] += q.z * dx; gx[3] += q.w * dx;
+        gy[0] += q.x * dy; gy[1] += q.y * dy; gy[2] += q.z * dy; gy[3] += q.w * dy;
+        const float4 w = si.x >= 0 ? u : q;  // the face average on a boundary face, as limiter.F90 uses
+        umax[0] = rmax(umax[0], w.x); umin[0] = rmin(umin[0], w.x);
+        umax[1] = rmax(umax[1], w.y); umin[1] = rmin(umin[1], w.y);
+        umax[2] = rmax(umax[2], w.z); umin[2] = rmin(umin[2], w.z);
+        umax[3] = rmax(umax[3], w.w); umin[3] = rmin(umin[3], w.w);
+    }
+    const float cvf = (float)v.cv[i];
+    if (flags & CG_DT) {
+        const float dt = (float)cur_cfl(v, inst, cfl_in) * cvf / la;
+        v.la[i] = (double)la;
+        v.dt[i] = (double)dt;
+        v.dcv[i] = (double)(dt / cvf);
+        if (flags & CG_DIAG) {
+            v.diag[i] = (double)(cvf / dt + 0.75f * la);
+            v.diaginv[i] = 1.0 / v.diag[i];
+        }
+        warp_atomic_min_u64(v, inst, enc_ord((double)dt));
+    }
+    {
+        const float r = 1.f / cvf;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) { gx[j] *= r; gy[j] *= r; }
+    }
+    const float4 p0 = v.packf[4 * (size_t)i + 3];
+    float ph[4] = {p0.x, p0.y, p0.z, p0.w};
+    if (flags & CG_LIM) {
+        float tol[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float hi = (float)dec_ord(v.minmax[8 * inst + j]), lo = (float)dec_ord(v.minmax[8 * inst + 4 + j]);
+            tol[j] = 0.05f * (hi - lo);
+            tol[j] = tol[j] * tol[j];
+        }
+        for (int k = k0; k < k1; ++k) {
+            const float4 sg = v.sideg[k];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float D_L = gx[j] * sg.z + gy[j] * sg.w;
                 float phi0 = 1.f;
                 if (D_L != 0.f) {  // limiter.F90:286-294 with a = (umax or umin) - qi, b = D_L
                     const float a = (D_L > 0.f ? umax[j] : umin[j]) - qi[j];
@@ -1629,6 +1726,14 @@ bool rk23_in_one_pass(const uns_cc_handle* h, const CCView& v, double cfl) {
     return h->P.time_mode == UNS_TIME_RK3 && !v.laminar && !(v.irs && eps > 0.0);
 }
 
+// Whether the step forms the face averages and radii inside the cell
+// gradient pass (k_cell_grad_side): the mixed form with the Green-Gauss
+// gradient of an inviscid flow under RK3 (the LU-SGS prep reads the FP64 face
+// radii that k_face_prim_spec writes).
+bool grad_by_sides(const uns_cc_handle* h, const CCView& v) {
+    return v.mixed && v.sideg != nullptr && h->P.time_mode == UNS_TIME_RK3;
+}
+
 // RK stages 2 and 3 in one pass over the cells: the wall cells first.
 int enqueue_rk23(uns_cc_handle* h, CCView& v) {
     if (v.nwcell > 0) {
@@ -1709,9 +1814,14 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
     int bflags = BEGIN_PRIM | BEGIN_OLD | BEGIN_POS | (v.ilimit ? BEGIN_MINMAX : 0);
     LAUNCH(k_begin, v.ntot, v, bflags);
     LAUNCH(k_vertex_avg, v.nop, v);
-    LAUNCH(k_face_prim_spec, v.nof, v);
-    if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
-    LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.0);
+    const int gflags = CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0) | (h->P.time_mode == UNS_TIME_RK3 ? 0 : CG_DIAG);
+    if (grad_by_sides(h, v)) {
+        LAUNCH(k_cell_grad_side, v.noc, v, gflags, 0.0);
+    } else {
+        LAUNCH(k_face_prim_spec, v.nof, v);
+        if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
+        LAUNCH_CELL_GRAD(v, gflags, 0.0);
+    }
     if (rk23_in_one_pass(h, v, cfl_for_eps)) {
         bool fused = false;
         if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 1, 0, &fused))) return rc;
@@ -1930,6 +2040,22 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     UP(lsw, lsw);
     { std::vector<int> t(m->nc2c, m->nc2c + noc); UP(nc2c, t); }
     UP(cf_off, cnt); UP(cf, cf);
+    if (p->grad_type == UNS_GRAD_GG && p->flow_type != UNS_FLOW_LAMINAR) {  // cell-side records (k_cell_grad_side)
+        std::vector<float4> sg(cf.size());
+        std::vector<int4> si(cf.size());
+        for (size_t k = 0; k < cf.size(); ++k) {
+            const int e = cf[k], f = e & FACE_MASK;
+            const bool out_side = f < nfi && (e & SIDE_BIT);
+            const float s = (f < nfi && !(e & SIDE_BIT)) ? 1.f : -1.f;  // Gradient_GG's sign (boundary: -1)
+            const float4 na = fnaf[f], gd = fgeof[f];
+            sg[k] = make_float4(s * na.x, s * na.y, out_side ? gd.z : gd.x, out_side ? gd.w : gd.y);
+            const int nbr = f < nfi ? (out_side ? m->fin[f] : m->fout[f]) : -1;
+            int area_bits;
+            std::memcpy(&area_bits, &na.z, sizeof(int));
+            si[k] = make_int4(nbr, m->fp1[f], m->fp2[f], area_bits);
+        }
+        UP(sideg, sg); UP(sidei, si);
+    }
     {  // wall cells: a bit per cell and their list
         std::vector<unsigned> t((noc + 31) / 32, 0u);
         std::vector<int> wc;
@@ -2059,6 +2185,8 @@ int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
     if (!h || !out) return UNS_ERR_ARG;
     const CCView& v = h->v;
     if (v.mixed && (field == UNS_CC_GRAD || field == UNS_CC_PHI)) LAUNCH(k_unpack_f32, v.noc, v);
+    // the graph step of this form forms the face radii inside k_cell_grad_side
+    if (v.mixed && v.sideg && field == UNS_CC_FLA) LAUNCH(k_face_prim_spec, v.nof, v);
     auto d2h = [&](void* dst, const void* src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
     };
@@ -2183,7 +2311,7 @@ int uns_cc_time_step(uns_cc_handle* h, double cfl, double* dtglobal) {
     h->cfl_cur = cfl;  // cirs of this iteration uses the same CFL
     k_reset_minmax<<<1, 32, 0, h->stream>>>(v);
     UNS_CUDA(cudaGetLastError());
-    LAUNCH_CELL_GRAD(v, CG_DT, cfl);
+    LAUNCH_CELL_GRAD(v, CG_DT | CG_DIAG, cfl);
     if (dtglobal) {
         unsigned long long e = 0;
         UNS_CUDA(cudaMemcpyAsync(&e, v.dtmin, 8, cudaMemcpyDeviceToHost, h->stream));
@@ -2563,9 +2691,15 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
             return UNS_OK;
         });
         if (!rc) rc = timed(1, [&]() -> int { LAUNCH(k_vertex_avg, v.nop, v); return UNS_OK; });
-        if (!rc) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
+        const bool sides = grad_by_sides(h, v);
+        if (!rc && !sides) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
         if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
-        if (!rc) rc = timed(4, [&]() -> int { LAUNCH_CELL_GRAD(v, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), cfl); return UNS_OK; });
+        if (!rc) rc = timed(4, [&]() -> int {
+            const int gflags = CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0) | (rk3 ? 0 : CG_DIAG);
+            if (sides) LAUNCH(k_cell_grad_side, v.noc, v, gflags, cfl);
+            else LAUNCH_CELL_GRAD(v, gflags, cfl);
+            return UNS_OK;
+        });
         const bool one_pass = rk23_in_one_pass(h, v, cfl);
         for (int irk = 1; irk <= (rk3 && !one_pass ? 3 : 1) && !rc; ++irk) {
             rc = timed(5, [&]() -> int {

@@ -33,6 +33,8 @@ struct CCView {
     const int* nc2c;
     const int* cf_off;    // index-sorted faces per cell, SIDE_BIT for `out`
     const int* cf;
+    const float4* sideg;  // per cf entry (GG, inviscid): outward-signed unit normal x, y; this side's offset x, y
+    const int4* sidei;    // per cf entry: cell across (-1 on a boundary), end points p1, p2, length (float bits)
     const unsigned* bcell;  // bit i: interior cell i has a wall face
     const int* wcell;       // those cells in increasing order
     int nwcell;
