@@ -86,16 +86,24 @@ WORKLOADS = {
 }
 
 # Kernels launched per iteration (our own; memsets excluded).
-# CCFVM inviscid RK3: reset_minmax, begin, vertex_avg, face_prim_spec, cell_grad,
+# CCFVM inviscid RK3 in FP64: reset_minmax, begin, vertex_avg, face_prim_spec, cell_grad,
 # face_conv, cell_res (stage 1), cell_rk23_wall + cell_rk23 (stages 2-3), res_final.
-LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 10, ("cc", "lusgs"): 12}
+# Mixed GG form: reset_minmax, begin, vertex_avg, cell_grad_side, face_conv,
+# cell_rk23_wall (wall cells, stages 1-3), cell_res_mixed, res_final.
+LAUNCHES = {("nc", "lusgs"): 9, ("nc", "rk3"): 11, ("cc", "rk3"): 10, ("cc", "lusgs"): 12, ("cc", "rk3_mixed_gg"): 8}
 
 
 def cc_launches(p) -> int:
     """Kernels one CCFVM iteration launches (enqueue_iteration)."""
     ggfc = p.grad_type == abi.GRAD["ggfc"]
-    if p.time_mode != abi.TIME["rk3"] or p.flow_type != abi.FLOW["laminar"]:
-        return LAUNCHES[("cc", "rk3" if p.time_mode == abi.TIME["rk3"] else "lusgs")] + (1 if ggfc else 0)
+    rk3 = p.time_mode == abi.TIME["rk3"]
+    mixed = p.precision == abi.PREC["mixed"]
+    if not rk3:
+        return LAUNCHES[("cc", "lusgs")] + (1 if ggfc else 0)
+    if p.flow_type != abi.FLOW["laminar"]:
+        if mixed and p.grad_type == abi.GRAD["gg"]:
+            return LAUNCHES[("cc", "rk3_mixed_gg")]
+        return LAUNCHES[("cc", "rk3")] + (1 if ggfc else 0) - (1 if mixed else 0)
     # reset_minmax, begin, vertex_avg, face_prim_spec, [face_ggfc], cell_grad,
     # 3 x (face_conv, cell_mul, [face_ggfc, (reset_minmax, begin), cell_grad], face_visc, cell_res), res_final
     per_stage = 4 + (0 if ggfc else 2 + (2 if p.ilimit else 0))
@@ -151,10 +159,12 @@ def peaks():
 
 
 # ---------------------------------------------------------------- bytes model
-def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
+def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = False) -> dict:
     """Unique bytes each kernel must move per launch: every array it touches
     counted once at its full size, no credit for reuse.
-    mixed: the CCFVM mixed form's kernels, which read FP32 copies."""
+    mixed: the CCFVM mixed form's kernels, which read FP32 copies; sides: its
+    inviscid Green-Gauss RK3 step (k_cell_grad_side, wall cells through all
+    three stages, one residual pass with the stages in closed form)."""
     if kind == "nc":
         N, E = m["nop"], m["nof"]
         B = int((m["fbc"] != 0).sum())
@@ -175,6 +185,23 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False) -> dict:
     N, F, P = m["noc"], m["nfi"] + m["nbf"], m["nop"]
     G = m["nbf"]
     W = int((np.asarray(m["fbc"])[m["nfi"]:] == 1001).sum())  # wall faces
+    if mixed and sides:
+        nnz = len(m["v2c"])
+        nside = 2 * m["nfi"] + m["nbf"]
+        return {
+            "begin": 32 * N + 32 * N + 16 * N + 32 * N + 32 * G,
+            "vertex_avg": 4 * P + 8 * nnz + 16 * (N + G) + 16 * P,
+            # offsets, 32-byte cell-side records, vertex values, FP32 primitives (own and across), cv;
+            # la, dt, dt/cv written; pack (phi read, 64 B written)
+            "cell_grad": 4 * N + 32 * nside + 16 * P + 16 * N + 8 * N + 24 * N + 16 * N + 64 * N,
+            "face_conv": 8 * F + 32 * F + 64 * N + 32 * F + 72 * G,
+            # face lists, FP64 fluxes, qc read+write, res written, dt/cv, wall bits
+            "cell_res": 16 * N + 32 * F + 64 * N + 32 * N + 8 * N + N // 8,
+            # wall cells, stages 1-3: per wall face its neighbours, geometry, the pack of its cell, ghost
+            # writes, wall force and flux; its cell's face lists, stored fluxes, state and residual
+            "cell_rk23": (300 + 148 + 80) * W,
+            "residue": 8 * ((N + 255) // 256),
+        }
     if mixed:
         nnz = len(m["v2c"])
         return {
@@ -223,16 +250,18 @@ TRAFFIC_PER_UNIT = {
 }
 
 
-def launches_per_iter(kind: str, rk3: bool, laminar: bool, irs: bool = False) -> dict:
+def launches_per_iter(kind: str, rk3: bool, laminar: bool, irs: bool = False, sides: bool = False) -> dict:
     """How many launches of each profiled phase one iteration makes.  An
     inviscid CCFVM RK3 step without smoothing computes its face fluxes once
     (stage 1) and runs stages 2 and 3 as one pass over the cells (cell_rk23),
-    recomputing only the wall faces' fluxes."""
+    recomputing only the wall faces' fluxes; the mixed Green-Gauss step
+    (sides) has no face pass and runs its wall cells as the cell_rk23 phase."""
     n = 3 if rk3 else 1
     if kind == "nc":
         return {"grad_lim": n, "edge": n, "node_res": n}
     if rk3 and not laminar and not irs:
-        return {"face_conv": 1, "cell_res": 1, "cell_rk23": 1, "viscous": 0, "cirs": 0}
+        return {"face_conv": 1, "cell_res": 1, "cell_rk23": 1, "viscous": 0, "cirs": 0,
+                "face_prim_spec": 0 if sides else 1}
     return {"face_conv": n, "cell_res": n, "viscous": n if laminar else 0, "cirs": n, "cell_rk23": 0}
 
 
@@ -427,8 +456,8 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     tot_w, secs_w = replicas.reduce_timing(dist, cells * args.steps, wall, device=str(dev))
     nbytes = 0
     for m in meshes:
-        b = algorithmic_bytes("cc", m.arrays, True)
-        nl = launches_per_iter("cc", True, False)
+        b = algorithmic_bytes("cc", m.arrays, True, sides=True)
+        nl = launches_per_iter("cc", True, False, sides=True)
         nbytes += sum(v * max(nl.get(k, 1), 1) for k, v in b.items() if k not in ("face_ggfc", "residue"))
     achieved = nbytes / (ms / 1e3 / args.steps) / 1e9
     peak, peak_src = peaks()
@@ -436,7 +465,7 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     if rank != 0:
         return None
     n = n_inst
-    launches = (LAUNCHES[("cc", "rk3")] if packed else LAUNCHES[("cc", "rk3")] * n) * args.steps
+    launches = (LAUNCHES[("cc", "rk3_mixed_gg")] if packed else LAUNCHES[("cc", "rk3_mixed_gg")] * n) * args.steps
     path = ("uns_cc_packed_iterate" if packed else "uns_cc_batch_iterate") + \
         ": CFL schedules in, residual histories out, one call for all steps"
     return {
@@ -558,10 +587,13 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     # Per-kernel device times (CUDA events on the library stream) -> roofline.
     prof = solver.profile(float(cfl_list(p, kind, it + 1, 1)[0]), reps=3)
     mixed_cc = kind == "cc" and p.precision == abi.PREC["mixed"]
-    nbytes = algorithmic_bytes(kind, m.arrays, mixed_cc)
+    sides = (mixed_cc and p.grad_type == abi.GRAD["gg"] and p.flow_type != abi.FLOW["laminar"]
+             and p.time_mode == abi.TIME["rk3"] and p.irs == 0)
+    nbytes = algorithmic_bytes(kind, m.arrays, mixed_cc, sides)
     peak, peak_src = peaks()
     dom = max(prof, key=prof.get)
-    nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"], p.irs != 0)
+    nl = launches_per_iter(kind, p.time_mode == abi.TIME["rk3"], p.flow_type == abi.FLOW["laminar"], p.irs != 0,
+                           sides)
     per_launch = {k: v / max(nl.get(k, 1), 1) for k, v in prof.items()}  # ms per launch
     rl_kernel = max((k for k in nbytes if k in prof and prof[k] > 0), key=lambda k: prof[k])
     achieved = nbytes[rl_kernel] / (per_launch[rl_kernel] * 1e-3) / 1e9

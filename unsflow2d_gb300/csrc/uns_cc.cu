@@ -904,52 +904,58 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
 // fluxes in the cell's face order (the first face initialises the sum), the
 // RK stage with fused multiply-adds, and the FP64 norm partial reduced with
 // one FP64 add per cell before the warp stage (FP64 issue, not bytes, bounds
-// this kernel on GB300).
-__global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, int partial) {
+// this kernel on GB300).  walls_done: the mixed form's one-pass step, where
+// k_cell_rk23_wall has already advanced the wall cells through all three
+// stages; they only contribute their residual to the norm here.
+__global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, int partial, int walls_done) {
     if (stopped(v, block_inst(v))) return;  // blocks of cells are instance-pure
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0;
     if (i < v.noc && cell_inst(v, i) >= 0) {
-        const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
         double r[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int k = k0; k < k1; ++k) {
-            const int e = v.cf[k], f = e & FACE_MASK;
-            const double4 F = v.fF[f];
-            const bool neg = f < v.nfi && (e & SIDE_BIT);
-            if (k == k0) {  // sign flip on the bits: no FP64 instruction
-                const long long m = neg ? (long long)0x8000000000000000ULL : 0LL;
-                r[0] = __longlong_as_double(__double_as_longlong(F.x) ^ m);
-                r[1] = __longlong_as_double(__double_as_longlong(F.y) ^ m);
-                r[2] = __longlong_as_double(__double_as_longlong(F.z) ^ m);
-                r[3] = __longlong_as_double(__double_as_longlong(F.w) ^ m);
-            } else {
-                const double s = neg ? -1.0 : 1.0;
-                r[0] = __fma_rn(s, F.x, r[0]); r[1] = __fma_rn(s, F.y, r[1]); r[2] = __fma_rn(s, F.z, r[2]); r[3] = __fma_rn(s, F.w, r[3]);
-            }
-        }
-        if (v.laminar) {
+        if (walls_done && ((__ldg(v.bcell + (i >> 5)) >> (i & 31)) & 1u)) {
+            d4get(v.res[i], r);  // a wall cell: its last-stage residual (k_cell_rk23_wall)
+        } else {
+            const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
             for (int k = k0; k < k1; ++k) {
                 const int e = v.cf[k], f = e & FACE_MASK;
-                const double4 V = v.fV[f];
-                const double s = (f < v.nfi && (e & SIDE_BIT)) ? 1.0 : -1.0;
-                r[0] = __fma_rn(s, V.x, r[0]); r[1] = __fma_rn(s, V.y, r[1]); r[2] = __fma_rn(s, V.z, r[2]); r[3] = __fma_rn(s, V.w, r[3]);
+                const double4 F = v.fF[f];
+                const bool neg = f < v.nfi && (e & SIDE_BIT);
+                if (k == k0) {  // sign flip on the bits: no FP64 instruction
+                    const long long m = neg ? (long long)0x8000000000000000ULL : 0LL;
+                    r[0] = __longlong_as_double(__double_as_longlong(F.x) ^ m);
+                    r[1] = __longlong_as_double(__double_as_longlong(F.y) ^ m);
+                    r[2] = __longlong_as_double(__double_as_longlong(F.z) ^ m);
+                    r[3] = __longlong_as_double(__double_as_longlong(F.w) ^ m);
+                } else {
+                    const double s = neg ? -1.0 : 1.0;
+                    r[0] = __fma_rn(s, F.x, r[0]); r[1] = __fma_rn(s, F.y, r[1]); r[2] = __fma_rn(s, F.z, r[2]); r[3] = __fma_rn(s, F.w, r[3]);
+                }
             }
-        }
-        v.res[i] = d4(r);
-        if (irk > 0) {
-            const double D = v.dcv[i];
-            double c[4], q[4];
-            d4get(v.qc[i], c);
-#pragma unroll
-            for (int j = 0; j < 4; ++j) q[j] = __fma_rn(-D, r[j], c[j]);
-            if (irk > 1) {
-                const double a = rk3_a(irk), b = rk3_b(irk);
-                double o[4];
-                d4get(v.qold[i], o);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) q[j] = __fma_rn(a, o[j], b * q[j]);
+            if (v.laminar) {
+                for (int k = k0; k < k1; ++k) {
+                    const int e = v.cf[k], f = e & FACE_MASK;
+                    const double4 V = v.fV[f];
+                    const double s = (f < v.nfi && (e & SIDE_BIT)) ? 1.0 : -1.0;
+                    r[0] = __fma_rn(s, V.x, r[0]); r[1] = __fma_rn(s, V.y, r[1]); r[2] = __fma_rn(s, V.z, r[2]); r[3] = __fma_rn(s, V.w, r[3]);
+                }
             }
-            v.qc[i] = d4(q);
+            v.res[i] = d4(r);
+            if (irk > 0) {
+                const double D = v.dcv[i];
+                double c[4], q[4];
+                d4get(v.qc[i], c);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) q[j] = __fma_rn(-D, r[j], c[j]);
+                if (irk > 1) {
+                    const double a = rk3_a(irk), b = rk3_b(irk);
+                    double o[4];
+                    d4get(v.qold[i], o);
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) q[j] = __fma_rn(a, o[j], b * q[j]);
+                }
+                v.qc[i] = d4(q);
+            }
         }
         if (partial) rr = __fma_rn(r[3], r[3], __fma_rn(r[2], r[2], __fma_rn(r[1], r[1], r[0] * r[0])));
     }
@@ -989,12 +995,14 @@ __device__ __forceinline__ void rk_update(int irk, double D, const double o[4], 
 }
 
 // The residual of wall cell i at stage state q: its wall faces' fluxes
-// recomputed (ghosts, wall force and fF written), the other faces' stored.
+// recomputed (ghosts, wall force and fF written), the other faces' stored;
+// with recompute false every face's stored flux (the first stage's sum).
 template <class R>
-__device__ __forceinline__ void wall_cell_res(const CCView& v, const Gas& g, int i, const double q[4], double r[4]) {
+__device__ __forceinline__ void wall_cell_res(const CCView& v, const Gas& g, int i, const double q[4], double r[4],
+                                              bool recompute = true) {
     const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
     auto flux = [&](int f) -> double4 {
-        return (f >= v.nfi && v.fbc[f] == 1001) ? bnd_face_flux<R>(v, g, f, i, q) : v.fF[f];
+        return (recompute && f >= v.nfi && v.fbc[f] == 1001) ? bnd_face_flux<R>(v, g, f, i, q) : v.fF[f];
     };
     if constexpr (std::is_same<R, float>::value) {  // k_cell_res_mixed's order
         for (int k = k0; k < k1; ++k) {
@@ -1019,15 +1027,24 @@ __device__ __forceinline__ void wall_cell_res(const CCView& v, const Gas& g, int
 
 // Stages 2 and 3 of cell i (instance inst): the stage updates and, for a
 // wall cell, its residual in each stage; returns the squared residual that
-// the last stage's norm takes.
-template <class R, bool kWall>
+// the last stage's norm takes.  kFrom1 (a wall cell of the mixed form): the
+// first stage too, from the stored face fluxes (k_cell_res_mixed's sum and
+// update).
+template <class R, bool kWall, bool kFrom1 = false>
 __device__ __forceinline__ double rk23_cell(const CCView& v, int i, int inst) {
     constexpr bool kMixed = std::is_same<R, float>::value;
     double r[4], q[4], o[4];
-    d4get(v.res[i], r);
     d4get(v.qc[i], q);
     d4get(v.qold[i], o);
     const double D = v.dcv[i];
+    if constexpr (kFrom1) {
+        static_assert(kMixed && kWall, "the first stage here is the mixed form's");
+        wall_cell_res<R>(v, gas_of(v, inst), i, q, r, false);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) q[j] = __fma_rn(-D, r[j], q[j]);
+    } else {
+        d4get(v.res[i], r);
+    }
     for (int irk = 2; irk <= 3; ++irk) {
         if (kWall) wall_cell_res<R>(v, gas_of(v, inst), i, q, r);
         rk_update<kMixed>(irk, D, o, r, q);
@@ -1039,15 +1056,16 @@ __device__ __forceinline__ double rk23_cell(const CCView& v, int i, int inst) {
 }
 
 // The wall cells (v.wcell), one per thread in one-warp blocks so that their
-// long FP64 chains spread over the SMs; they run before k_cell_rk23.
-template <class R>
+// long FP64 chains spread over the SMs; they run before k_cell_rk23 (FP64
+// form, stages 2-3) or k_cell_res_mixed (mixed form, all three stages).
+template <class R, bool kFrom1>
 __global__ void __launch_bounds__(32) k_cell_rk23_wall(CCView v) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= v.nwcell) return;
     const int i = v.wcell[t];
     const int inst = cell_inst(v, i);
     if (inst < 0 || stopped(v, inst)) return;
-    rk23_cell<R, true>(v, i, inst);
+    rk23_cell<R, true, kFrom1>(v, i, inst);
 }
 
 // Every other cell: a stream over the stored residual and states; the wall
@@ -1734,16 +1752,22 @@ bool grad_by_sides(const uns_cc_handle* h, const CCView& v) {
     return v.mixed && v.sideg != nullptr && h->P.time_mode == UNS_TIME_RK3;
 }
 
-// RK stages 2 and 3 in one pass over the cells: the wall cells first.
+// The wall cells' stages: 2-3 in the FP64 form, 1-3 in the mixed form.
+int enqueue_wall_rk(uns_cc_handle* h, CCView& v) {
+    if (v.nwcell == 0) return UNS_OK;
+    const int nb = (v.nwcell + 31) / 32;
+    if (v.mixed) k_cell_rk23_wall<float, true><<<nb, 32, 0, h->stream>>>(v);
+    else k_cell_rk23_wall<double, false><<<nb, 32, 0, h->stream>>>(v);
+    UNS_CUDA(cudaGetLastError());
+    return UNS_OK;
+}
+
+// RK stages 2 and 3 of the FP64 form in one pass over the cells: the wall
+// cells first.
 int enqueue_rk23(uns_cc_handle* h, CCView& v) {
-    if (v.nwcell > 0) {
-        const int nb = (v.nwcell + 31) / 32;
-        if (v.mixed) k_cell_rk23_wall<float><<<nb, 32, 0, h->stream>>>(v);
-        else k_cell_rk23_wall<double><<<nb, 32, 0, h->stream>>>(v);
-        UNS_CUDA(cudaGetLastError());
-    }
-    if (v.mixed) LAUNCH(k_cell_rk23<float>, v.noc, v);
-    else LAUNCH(k_cell_rk23<double>, v.noc, v);
+    int rc = enqueue_wall_rk(h, v);
+    if (rc) return rc;
+    LAUNCH(k_cell_rk23<double>, v.noc, v);
     return UNS_OK;
 }
 
@@ -1767,7 +1791,7 @@ int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int par
     // ((0*x + r) * 1 == r for finite x), so they are launched only for eps > 0.
     bool smooth = v.irs && eps > 0.0;
     *fused = !smooth && irk > 0;
-    if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0, 0);
     else LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
     if (smooth) {
         UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
@@ -1822,7 +1846,21 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
         if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
         LAUNCH_CELL_GRAD(v, gflags, 0.0);
     }
-    if (rk23_in_one_pass(h, v, cfl_for_eps)) {
+    if (rk23_in_one_pass(h, v, cfl_for_eps) && v.mixed) {
+        // Mixed form: the wall cells through all three stages, then every other
+        // cell's update and the norm.  A cell without a wall face has the same
+        // residual r in all three stages, and then the RK3 stages (main.F90:
+        // 92-101, a = 0, 3/4, 1/3; b = 1, 1/4, 2/3) give, with D = dt/cv,
+        //   q1 = qold - D r,  q2 = 3/4 qold + 1/4 (q1 - D r) = qold - D r / 2,
+        //   q3 = 1/3 qold + 2/3 (q2 - D r) = qold - D r = q1
+        // in exact arithmetic; this form keeps the FP64 q1 (it differs from the
+        // three rounded stage updates in the last bits, far below the FP32 face
+        // arithmetic).  The FP64 form evaluates both stage updates in the
+        // reference's operation order (k_cell_rk23).
+        LAUNCH_FACE_CONV(float, v);
+        if ((rc = enqueue_wall_rk(h, v))) return rc;
+        LAUNCH(k_cell_res_mixed, v.noc, v, 1, 1, 1);
+    } else if (rk23_in_one_pass(h, v, cfl_for_eps)) {
         bool fused = false;
         if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 1, 0, &fused))) return rc;
         if ((rc = enqueue_rk23(h, v))) return rc;
@@ -2719,8 +2757,9 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
                 return UNS_OK;
             });
             int fuse = (rk3 && !smooth) ? irk : 0;
+            if (!rc && one_pass && v.mixed) rc = timed(11, [&]() -> int { return enqueue_wall_rk(h, v); });
             if (!rc) rc = timed(7, [&]() -> int {
-                if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
+                if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, smooth ? 0 : 1, one_pass ? 1 : 0);
                 else LAUNCH(k_cell_res, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
                 return UNS_OK;
             });
@@ -2733,7 +2772,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
                 return UNS_OK;
             });
         }
-        if (!rc && one_pass) rc = timed(11, [&]() -> int { return enqueue_rk23(h, v); });
+        if (!rc && one_pass && !v.mixed) rc = timed(11, [&]() -> int { return enqueue_rk23(h, v); });
         if (!rc && !rk3) rc = timed(9, [&]() -> int { return enqueue_lusgs(h, v); });
         if (!rc) rc = timed(10, [&]() -> int {
             k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);
