@@ -155,13 +155,27 @@ __global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
         const bool dbl = v.laminar || v.grad_type == UNS_GRAD_GGFC;
         float wt = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
         double c4 = 0.0;
-        for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
-            const int c = __ldg(&v.v2c[k]);
-            const float w = __ldg(&v.v2c_wtf[k]);
-            const float4 q = v.qpf[c];
+        auto add = [&](int c, float w, const float4& q) {
             wt = wt + w;
             c0 = c0 + q.x * w; c1 = c1 + q.y * w; c2 = c2 + q.z * w; c3 = c3 + q.w * w;
             if (dbl) c4 = c4 + v.qT[c] * (double)w;
+        };
+        int k = v.v2c_off[i];
+        const int k1 = v.v2c_off[i + 1];
+        for (; k + 3 < k1; k += 4) {  // four cells' gathers in flight together, sums in order
+            int c[4];
+            float w[4];
+            float4 q[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) { c[u] = __ldg(&v.v2c[k + u]); w[u] = __ldg(&v.v2c_wtf[k + u]); }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) q[u] = v.qpf[c[u]];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) add(c[u], w[u], q[u]);
+        }
+        for (; k < k1; ++k) {
+            const int c = __ldg(&v.v2c[k]);
+            add(c, __ldg(&v.v2c_wtf[k]), v.qpf[c]);
         }
         const float r = 1.f / wt;
         const float4 pp = make_float4(c0 * r, c1 * r, c2 * r, c3 * r);
@@ -173,6 +187,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
         return;
     }
     double wt = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0;
+#pragma unroll 4
     for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
         int c = __ldg(&v.v2c[k]);
         double w = __ldg(&v.v2c_wt[k]);
@@ -591,6 +606,16 @@ __global__ void __launch_bounds__(kBlock, 5) k_cell_grad_mixed(CCView v, int fla
 // neighbours' primitives.  dt, the gradient, the limiter and the pack are
 // those of k_cell_grad_mixed, bit for bit.
 __global__ void __launch_bounds__(kBlock, 4) k_cell_grad_side(CCView v, int flags, double cfl_in) {
+    // the limiter tolerances of the block's instance (blocks of cells are
+    // instance-pure), decoded once per block
+    __shared__ float stol[4];
+    if ((flags & CG_LIM) && threadIdx.x < 4) {
+        const int b = block_inst(v), j = threadIdx.x;
+        const float hi = (float)dec_ord(v.minmax[8 * b + j]), lo = (float)dec_ord(v.minmax[8 * b + 4 + j]);
+        const float t = 0.05f * (hi - lo);
+        stol[j] = t * t;
+    }
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
     const int inst = cell_inst(v, i);
@@ -641,13 +666,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_cell_grad_side(CCView v, int flag
     const float4 p0 = v.packf[4 * (size_t)i + 3];
     float ph[4] = {p0.x, p0.y, p0.z, p0.w};
     if (flags & CG_LIM) {
-        float tol[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float hi = (float)dec_ord(v.minmax[8 * inst + j]), lo = (float)dec_ord(v.minmax[8 * inst + 4 + j]);
-            tol[j] = 0.05f * (hi - lo);
-            tol[j] = tol[j] * tol[j];
-        }
+        const float tol[4] = {stol[0], stol[1], stol[2], stol[3]};
         for (int k = k0; k < k1; ++k) {
             const float4 sg = v.sideg[k];
 #pragma unroll
@@ -917,9 +936,8 @@ __global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, in
             d4get(v.res[i], r);  // a wall cell: its last-stage residual (k_cell_rk23_wall)
         } else {
             const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
-            for (int k = k0; k < k1; ++k) {
-                const int e = v.cf[k], f = e & FACE_MASK;
-                const double4 F = v.fF[f];
+            auto add = [&](int k, int e, const double4& F) {
+                const int f = e & FACE_MASK;
                 const bool neg = f < v.nfi && (e & SIDE_BIT);
                 if (k == k0) {  // sign flip on the bits: no FP64 instruction
                     const long long m = neg ? (long long)0x8000000000000000ULL : 0LL;
@@ -930,6 +948,18 @@ __global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, in
                 } else {
                     const double s = neg ? -1.0 : 1.0;
                     r[0] = __fma_rn(s, F.x, r[0]); r[1] = __fma_rn(s, F.y, r[1]); r[2] = __fma_rn(s, F.z, r[2]); r[3] = __fma_rn(s, F.w, r[3]);
+                }
+            };
+            if (k1 - k0 == 3) {  // a triangle: the three fluxes' gathers in flight together, summed in order
+                const int e0 = v.cf[k0], e1 = v.cf[k0 + 1], e2 = v.cf[k0 + 2];
+                const double4 F0 = v.fF[e0 & FACE_MASK], F1 = v.fF[e1 & FACE_MASK], F2 = v.fF[e2 & FACE_MASK];
+                add(k0, e0, F0);
+                add(k0 + 1, e1, F1);
+                add(k0 + 2, e2, F2);
+            } else {
+                for (int k = k0; k < k1; ++k) {
+                    const int e = v.cf[k];
+                    add(k, e, v.fF[e & FACE_MASK]);
                 }
             }
             if (v.laminar) {
@@ -1174,7 +1204,16 @@ __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, doub
     const int n = v.ninst ? v.boff[inst + 1] - k0 : nparts;
     __shared__ double s[kBlock];
     double t = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) t = t + v.partial[k0 + k];
+    // eight partials loaded together, then added in the loop's order
+    int k = threadIdx.x;
+    for (; k + 7 * kBlock < n; k += 8 * kBlock) {
+        double p[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) p[u] = v.partial[k0 + k + u * kBlock];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t = t + p[u];
+    }
+    for (; k < n; k += kBlock) t = t + v.partial[k0 + k];
     s[threadIdx.x] = t;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -1217,9 +1256,11 @@ __global__ void k_reset_minmax(CCView v) {
 // viscous_flux.F90:530-533).
 __global__ void k_forces(CCView v, double* out) {
     double fx = 0.0, fy = 0.0;
-    for (int k = 0; k < v.nbf; ++k)
+#pragma unroll 8
+    for (int k = 0; k < v.nbf; ++k)  // unrolled: loads in flight together, sums in order
         if (v.fbc[v.nfi + k] == 1001) { fx = fx + v.fwall[k].x; fy = fy + v.fwall[k].y; }
     if (v.laminar)
+#pragma unroll 8
         for (int k = 0; k < v.nbf; ++k)
             if (v.fbc[v.nfi + k] == 1001) { fx = fx - v.fwallv[k].x; fy = fy - v.fwallv[k].y; }
     out[0] = fx;

@@ -61,7 +61,8 @@ __global__ void k_wall_terms(CCView v, double xref, double yref, double dyna, do
 __global__ void k_wall_sum(CCView v, const double* t, double* out) {
     double fx = 0.0, fy = 0.0, cm = 0.0;
     int i = 0;
-    for (int b = 0; b < v.nbf; ++b) {
+#pragma unroll 4
+    for (int b = 0; b < v.nbf; ++b) {  // unrolled: loads in flight together, sums in order
         if (v.fbc[v.nfi + b] != 1001) continue;
         const double* o = t + (size_t)b * kRow;
         fx = fx + o[4];

@@ -397,7 +397,8 @@ __global__ void __launch_bounds__(kBlock) k_nc_res_final(NCView v, int nparts, d
     __shared__ int si[kBlock];
     double t = 0.0, m = -1.0;
     int mi = 0x7fffffff;
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+#pragma unroll 4
+    for (int k = threadIdx.x; k < nparts; k += kBlock) {  // unrolled: loads in flight together, sums in order
         t = t + v.partial[2 * k];
         double pm = v.partial[2 * k + 1];
         int pi = v.partial_i[k];
