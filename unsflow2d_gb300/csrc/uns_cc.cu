@@ -83,6 +83,8 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
     if (!v.ninst && !live) return;  // one case: the whole grid stops together
     unsigned long long emx[4] = {0ULL, 0ULL, 0ULL, 0ULL};
     unsigned long long emn[4] = {~0ULL, ~0ULL, ~0ULL, ~0ULL};
+    bool have = false;  // the primitives below are this thread's qp (no read-back for the limiter range)
+    double pr[4];
     if (live && i < v.noc) {
         const Gas& gi = gas_of(v, inst);
         double4 q = v.qc[i];
@@ -92,22 +94,28 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
             const float p = (float)gi.gamma1 * (E - 0.5f * r * (u * u + w * w));
             v.qpf[i] = make_float4(r, u, w, p);
             v.qp[i] = make_double4(r, u, w, p);
+            pr[0] = r; pr[1] = u; pr[2] = w; pr[3] = p;
+            have = true;
             if (v.laminar || v.grad_type == UNS_GRAD_GGFC) v.qT[i] = (double)(p / (r * (float)gi.znd));
             if ((flags & BEGIN_POS) && (r <= 0.f || p <= 0.f)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
         } else if (flags & BEGIN_PRIM) {
             Prim P = con2prim(gi, q.x, q.y, q.z, q.w);
             v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
             v.qT[i] = P.t;
+            pr[0] = P.rho; pr[1] = P.u; pr[2] = P.v; pr[3] = P.p;
+            have = true;
             if ((flags & BEGIN_POS) && (P.rho <= 0.0 || P.p <= 0.0)) set_err(v.err, UNS_ERR_NONPOSITIVE, i);
         }
         if (flags & BEGIN_OLD) v.qold[i] = q;
     }
     if (flags & BEGIN_MINMAX) {
         if (live && i < v.ntot) {
-            double4 p = v.qp[i];
-            double a[4] = {p.x, p.y, p.z, p.w};
+            if (!have) {
+                const double4 p = v.qp[i];
+                pr[0] = p.x; pr[1] = p.y; pr[2] = p.z; pr[3] = p.w;
+            }
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { emx[j] = enc_ord(a[j]); emn[j] = emx[j]; }
+            for (int j = 0; j < 4; ++j) { emx[j] = enc_ord(pr[j]); emn[j] = emx[j]; }
         }
         if (v.ninst && blockIdx.x * blockDim.x >= v.noc) {  // ghost blocks of packed cases: per-case lane groups
             const unsigned grp = __match_any_sync(0xffffffffu, live ? inst : -1);
