@@ -532,7 +532,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
 
     # Mixed forms: the same iterations in FP64 from the same start, compared.
     accuracy = None
-    if p.precision != abi.PREC["fp64"] and rank == 0:
+    if p.precision != abi.PREC["fp64"] and rank == 0 and not args.no_accuracy:
         accuracy = accuracy_vs_fp64(w, m, solver, np.array(hist))
 
     # End to end through the per-routine C-ABI (the calls a Fortran driver
@@ -715,6 +715,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--mesh", default=None, help="override the O-mesh size, e.g. 512x256 (profiling runs)")
     ap.add_argument("--no-converge", action="store_true", help="skip the time-to-1e-8 leg")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the mixed forms' FP64 comparison run (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
