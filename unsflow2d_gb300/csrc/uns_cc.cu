@@ -934,7 +934,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_res(CCView v, int irk, int part
 // this kernel on GB300).  walls_done: the mixed form's one-pass step, where
 // k_cell_rk23_wall has already advanced the wall cells through all three
 // stages; they only contribute their residual to the norm here.
-__global__ void __launch_bounds__(kBlock) k_cell_res_mixed(CCView v, int irk, int partial, int walls_done) {
+__global__ void __launch_bounds__(kBlock, 8) k_cell_res_mixed(CCView v, int irk, int partial, int walls_done) {
     if (stopped(v, block_inst(v))) return;  // blocks of cells are instance-pure
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0;
