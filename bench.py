@@ -540,9 +540,9 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     # makes), with the state in pinned host memory copied in and out each step.
     lib = abi.gpu_lib()
     n_e2e = 0 if args.no_e2e else max(3, min(args.steps, 20))
-    host_in = torch.empty((solver.nstate, 4), dtype=torch.float64, pin_memory=True)
-    host_out = torch.empty((solver.nstate, 4), dtype=torch.float64, pin_memory=True)
-    host_in.copy_(torch.from_numpy(solver.get_state()))
+    # two pinned host states used in turn: step k reads one and writes the other
+    host = [torch.empty((solver.nstate, 4), dtype=torch.float64, pin_memory=True) for _ in range(2)]
+    host[0].copy_(torch.from_numpy(solver.get_state()))
     h = solver._h
     dp = lambda t: C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_double))
     fres = C.c_double()
@@ -554,6 +554,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     lusgs = p.time_mode == abi.TIME["lusgs"]
     for k in range(n_e2e):
         c = float(cfls[k])
+        host_in, host_out = host[k % 2], host[(k + 1) % 2]
         if kind == "nc":
             calls = [lambda: lib.uns_nc_set_state(h, dp(host_in)), lambda: lib.uns_nc_save_old(h)]
             if lusgs:
@@ -577,7 +578,6 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
             rc = call()
             if rc:
                 raise abi.UnsError(rc, lib.uns_last_error().decode())
-        host_in.copy_(host_out)
     e2e_s = max(time.perf_counter() - t_e0, 1e-9)
     tot_e2e, e2e_s = replicas.reduce_timing(dist, units * n_e2e, e2e_s, device=str(dev))
     state_bytes = solver.nstate * 32

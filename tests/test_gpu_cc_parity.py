@@ -125,3 +125,25 @@ def test_cc_graph_step_equals_routine_calls(cc_mesh, case):
     else:
         assert np.array_equal(qg, qr)
         assert np.array_equal(fg, fr)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cc_fvresidual_flux_cache_equals_full_call(cc_mesh, precision):
+    """uns_cc_fvresidual recomputes only the wall faces and their cells when
+    nothing but the conserved state has changed since its last full call
+    (the reference loop's RK stages 2 and 3); a call after any input change
+    (here a same-precision set_precision) computes every face.  Both give
+    the same residual bit for bit."""
+    p = abi.make_params(flux="roe", grad="gg", m_inf=0.7, aoa_deg=2.0, precision=precision)
+    cfl = mesh.cfl_schedule(p, 1, 15, "cc")
+    a, b = CCSolver(cc_mesh, p), CCSolver(cc_mesh, p)
+    for s in (a, b):
+        s.iterate(cfl[:14], first_iter=True)
+        s.con2prim(); s.avg_c2v(); s.time_step(float(cfl[14])); s.save_old(); s.gradient()
+        s.fvresidual(); s.rk_stage(1)
+    assert np.array_equal(a.get("res"), b.get("res"))
+    a.fvresidual()                 # cached: wall faces only
+    b.set_precision(precision)     # invalidates the cache
+    b.fvresidual()                 # every face
+    assert np.array_equal(a.get("res"), b.get("res"))
+    assert np.array_equal(a.get_state(), b.get_state())

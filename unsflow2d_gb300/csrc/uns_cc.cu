@@ -1106,6 +1106,21 @@ __global__ void __launch_bounds__(32) k_cell_rk23_wall(CCView v) {
     rk23_cell<R, true, kFrom1>(v, i, inst);
 }
 
+// The residual of every wall cell (v.wcell) from the stored face fluxes, in
+// the residual gather's order (uns_cc_fvresidual's cached form).
+template <class R>
+__global__ void __launch_bounds__(32) k_wall_res(CCView v) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= v.nwcell) return;
+    const int i = v.wcell[t];
+    const int inst = cell_inst(v, i);
+    if (inst < 0 || stopped(v, inst)) return;
+    const double q[4] = {0.0, 0.0, 0.0, 0.0};
+    double r[4];
+    wall_cell_res<R>(v, gas_of(v, inst), i, q, r, false);
+    v.res[i] = d4(r);
+}
+
 // Every other cell: a stream over the stored residual and states; the wall
 // cells contribute the last-stage residual k_cell_rk23_wall stored.  The norm
 // partial is reduced as the stage-by-stage kernels reduce it.
@@ -1801,6 +1816,25 @@ bool grad_by_sides(const uns_cc_handle* h, const CCView& v) {
     return v.mixed && v.sideg != nullptr && h->P.time_mode == UNS_TIME_RK3;
 }
 
+// uns_cc_fvresidual when only the wall ghosts can have changed since the last
+// call that computed every face (same primitives, gradient and limiter; the
+// reference main loop's RK stages 2 and 3): the boundary faces' fluxes and
+// the wall cells' residuals; every other cell keeps the residual it has.
+int enqueue_wall_res(uns_cc_handle* h, CCView& v) {
+    const int nbb = (v.nbf + kBlock - 1) / kBlock;  // k_face_conv's boundary blocks come first
+    if (nbb == 0) return UNS_OK;
+    if (v.mixed) k_face_conv<float><<<nbb, kBlock, 0, h->stream>>>(v);
+    else k_face_conv<double><<<nbb, kBlock, 0, h->stream>>>(v);
+    UNS_CUDA(cudaGetLastError());
+    if (v.nwcell > 0) {
+        const int nb = (v.nwcell + 31) / 32;
+        if (v.mixed) k_wall_res<float><<<nb, 32, 0, h->stream>>>(v);
+        else k_wall_res<double><<<nb, 32, 0, h->stream>>>(v);
+        UNS_CUDA(cudaGetLastError());
+    }
+    return UNS_OK;
+}
+
 // The wall cells' stages: 2-3 in the FP64 form, 1-3 in the mixed form.
 int enqueue_wall_rk(uns_cc_handle* h, CCView& v) {
     if (v.nwcell == 0) return UNS_OK;
@@ -2245,6 +2279,7 @@ int uns_cc_destroy(uns_cc_handle* h) {
 
 int uns_cc_initialize(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView v = h->v;
     k_initialize<<<nblocks(v.ntot), kBlock, 0, h->stream>>>(v, h->qinf);
     UNS_CUDA(cudaGetLastError());
@@ -2345,6 +2380,7 @@ int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
 
 int uns_cc_set_field(uns_cc_handle* h, int field, const double* in) {
     if (!h || !in) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView& v = h->v;
     switch (field) {
         case UNS_CC_QC:
@@ -2379,6 +2415,7 @@ int uns_cc_set_field(uns_cc_handle* h, int field, const double* in) {
 
 int uns_cc_con2prim(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView v = h->v;
     LAUNCH(k_begin, v.noc, v, (int)BEGIN_PRIM);
     return UNS_OK;
@@ -2386,6 +2423,7 @@ int uns_cc_con2prim(uns_cc_handle* h) {
 
 int uns_cc_avg_c2v(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView v = h->v;
     LAUNCH(k_vertex_avg, v.nop, v);
     LAUNCH(k_face_prim_spec, v.nof, v);
@@ -2417,12 +2455,14 @@ int uns_cc_save_old(uns_cc_handle* h) {
 
 int uns_cc_gradient(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView v = h->v;
     return enqueue_gradient(h, v, 0, 0.0, true);
 }
 
 int uns_cc_limit(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
+    ++h->flux_gen;
     CCView v = h->v;
     int rc = enqueue_minmax(h, v);
     if (rc) return rc;
@@ -2434,7 +2474,17 @@ int uns_cc_fvresidual(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
     CCView v = h->v;
     bool fused = false;
-    return enqueue_fvresidual(h, v, h->cfl_cur, 0, 0, &fused);
+    // Since the last call that computed every face, only the conserved state
+    // has changed (rk_stage, set_state): the interior and farfield fluxes read
+    // the primitives, gradient and limiter alone, so only the wall faces and
+    // their cells' residuals are recomputed (bit-identical to a full call).
+    // Viscous fluxes read the state, and a smoothing sweep replaces the stored
+    // residual: those calls compute everything.
+    const bool smooth = v.irs && epsirs_of(h, h->cfl_cur) > 0.0;
+    if (!v.laminar && !smooth && h->res_gen == h->flux_gen) return enqueue_wall_res(h, v);
+    const int rc = enqueue_fvresidual(h, v, h->cfl_cur, 0, 0, &fused);
+    if (!rc) h->res_gen = h->flux_gen;
+    return rc;
 }
 
 int uns_cc_rk_stage(uns_cc_handle* h, int irk) {
@@ -2574,6 +2624,7 @@ static int grow_schedule(uns_cc_handle* h, int cap) {
 // The graph-replayed iterations of every instance: cfl and fres_raw are
 // [instances][niter], done_iters [instances].
 static int iterate_graph(uns_cc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw, int* done_iters) {
+    ++h->flux_gen;
     const int n = std::max(1, h->v.ninst);
     if (niter > h->cfl_cap) {
         int rc = grow_schedule(h, niter);
@@ -2607,6 +2658,7 @@ extern "C" {
 
 int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (!h || precision < UNS_PREC_FP64 || precision > UNS_PREC_MIXED_SWEEP) return UNS_ERR_ARG;
+    ++h->flux_gen;
     if (h->P.precision != precision) {
         UNS_CUDA(cudaStreamSynchronize(h->stream));
         h->P.precision = precision;
@@ -2678,6 +2730,7 @@ int uns_cc_batch_iterate(uns_cc_batch* b, int niter, const double* cfl, int firs
     }
     for (int i = 0; i < n; ++i) {
         uns_cc_handle* h = b->hs[i];
+        ++h->flux_gen;
         for (int k = 0; k < niter; ++k)
             if (h->P.irs && epsirs_of(h, cfl[(size_t)i * niter + k]) > 0.0) {
                 set_last_error("uns_cc_batch_iterate: residual smoothing above CFLmax is not batched");
@@ -2750,6 +2803,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
                                    "viscous", "cell_res", "cirs", "lusgs_sweeps", "residue", "cell_rk23"};
     const int NP = 12;
     if (!h || reps < 1 || !ms) return UNS_ERR_ARG;
+    ++h->flux_gen;
     std::vector<double> acc(NP, 0.0);
     cudaEvent_t e0, e1;
     UNS_CUDA(cudaEventCreate(&e0));

@@ -746,6 +746,7 @@ extern "C" {
 
 int uns_cc_adjoint_prepare(uns_cc_handle* h, double cfl, double* cl, double* cd) {
     if (!h || !(cfl > 0.0)) return fail_adj("uns_cc_adjoint_prepare: bad argument", UNS_ERR_ARG);
+    ++h->flux_gen;  // the recorded iterations overwrite the step's arrays
     if (h->P.time_mode != UNS_TIME_RK3)
         return fail_adj("uns_cc_adjoint_prepare: the adjoint follows the RK3 iteration (time_mode = RK3)", UNS_ERR_ARG);
     if (h->P.precision != UNS_PREC_FP64)
@@ -782,6 +783,7 @@ int uns_cc_adjoint_vjp(uns_cc_handle* h, int objective, double seed, const doubl
                        double* og, double* oalpha) {
     if (!h || !wq || !wg || !oq || !og || (objective != UNS_OBJ_CL && objective != UNS_OBJ_CD))
         return fail_adj("uns_cc_adjoint_vjp: bad argument", UNS_ERR_ARG);
+    ++h->flux_gen;  // the recorded iterations overwrite the step's arrays
     if (!h->adj || !h->adj->recorded) return fail_adj("uns_cc_adjoint_vjp: call uns_cc_adjoint_prepare first", UNS_ERR_ARG);
     const CCView& v = h->v;
     AdjView& a = h->adj->a;
@@ -814,6 +816,7 @@ int uns_cc_adjoint_solve(uns_cc_handle* h, int objective, int max_iter, double t
                          int* iters) {
     if (!h || max_iter < 1 || !(tol >= 0.0) || (objective != UNS_OBJ_CL && objective != UNS_OBJ_CD))
         return fail_adj("uns_cc_adjoint_solve: bad argument", UNS_ERR_ARG);
+    ++h->flux_gen;  // the recorded iterations overwrite the step's arrays
     if (!h->adj || !h->adj->recorded) return fail_adj("uns_cc_adjoint_solve: call uns_cc_adjoint_prepare first", UNS_ERR_ARG);
     CCAdj& A = *h->adj;
     const CCView& v = h->v;

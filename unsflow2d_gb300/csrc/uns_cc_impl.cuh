@@ -156,6 +156,12 @@ struct uns_cc_handle {
     int graph_first = -1;
     int gen = 0;           // bumped whenever the captured iteration changes (precision, capacity)
     double cfl_cur = 0.0;  // CFL passed to the last time_step call
+    // uns_cc_fvresidual's flux cache: flux_gen is bumped by every call that may
+    // change the inputs of the interior and farfield face fluxes (primitives,
+    // gradient, limiter, precision, the whole step); res_gen is the flux_gen
+    // of the last fvresidual that computed every face.
+    long long flux_gen = 0;
+    long long res_gen = -1;
     uns::CCAdj* adj = nullptr;  // discrete-adjoint state, created by uns_cc_adjoint_prepare
     double* d_post = nullptr;   // post-processing scratch (uns_cc_post.cu), created on first use
 
