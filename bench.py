@@ -248,6 +248,20 @@ TRAFFIC_PER_UNIT = {
     ("cc", "face_conv", True): (157.10e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (139.32e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_grad", True): (261.26e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
+    ("cc", "cell_grad", False): (68.55e6 / 262144, "cells", "profiles/cc_fp64_512x256_full.md"),
+}
+
+# FP64-pipe utilisation (sm__pipe_fp64_cycles_active, fraction of peak while
+# active) of the same kernels from the same captures: the second roofline
+# fraction, the one that bounds the FP64 kernels.
+FP64_PIPE = {
+    ("nc", "lusgs_sweeps", False): (0.122, "profiles/nc_lusgs_512x256_full.md"),
+    ("cc", "cell_grad", False): (0.864, "profiles/cc_fp64_512x256_full.md"),
+    ("cc", "face_conv", False): (0.850, "profiles/cc_fp64_512x256_full.md"),
+    ("cc", "cell_res", False): (0.800, "profiles/cc_fp64_512x256_full.md"),
+    ("cc", "cell_grad", True): (0.190, "profiles/cc_mixed_1024x512_full.md"),
+    ("cc", "face_conv", True): (0.330, "profiles/cc_mixed_1024x512_full.md"),
+    ("cc", "cell_res", True): (0.716, "profiles/cc_mixed_1024x512_full.md"),
 }
 
 
@@ -632,7 +646,9 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
                      "duration_ms": round(per_launch[rl_kernel], 4),
                      "timing": "CUDA events on the library stream around each phase, 3 iterations after the timed region",
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured" else "fallback",
-                     "dominant_phase": dom},
+                     "dominant_phase": dom,
+                     "fp64_pipe_frac": FP64_PIPE.get((kind, rl_kernel, mixed_cc), (None, None))[0],
+                     "fp64_pipe_source": FP64_PIPE.get((kind, rl_kernel, mixed_cc), (None, None))[1]},
         "kernels": kernels,
     }
     if not args.no_cpu_baseline and args.gpus == 1:
