@@ -244,7 +244,7 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = Fal
 # summaries under profiles/): scaled here to the benchmark's size.
 TRAFFIC_PER_UNIT = {
     ("nc", "lusgs_sweeps", False): (103.81e6 / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
-    ("cc", "face_conv", False): (57.09e6 / 393728, "faces", "profiles/cc_face_conv_512x256_full.md"),
+    ("cc", "face_conv", False): (58.57e6 / 393728, "faces", "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", True): (157.10e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (139.32e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_grad", True): (261.26e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
