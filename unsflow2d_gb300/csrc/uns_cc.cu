@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
 }
 
 // avg_c2v vertex part (average.F90:263-281): pseudo-Laplacian weighted mean.
-__global__ void __launch_bounds__(kBlock) k_vertex_avg(CCView v) {
+__global__ void __launch_bounds__(512) k_vertex_avg(CCView v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nop || stopped(v, vert_inst(v, i))) return;
     if (v.mixed) {  // FP32 from the FP32 primitives; FP64 copies only where an FP64 kernel reads them
@@ -755,10 +756,11 @@ __device__ __forceinline__ double4 bnd_face_flux(const CCView& v, const Gas& g, 
 // ghost arithmetic is the longest per thread, so that they run beside the
 // interior faces instead of after them.
 template <class R>
-__global__ void __launch_bounds__(kBlock, std::is_same<R, float>::value ? 4 : 1) k_face_conv(CCView v) {
-    const int nbb = (v.nbf + kBlock - 1) / kBlock;
+__global__ void __launch_bounds__(512, std::is_same<R, float>::value ? 2 : 1) k_face_conv(CCView v) {
+    const int bs = blockDim.x;
+    const int nbb = (v.nbf + bs - 1) / bs;
     const bool bnd = (int)blockIdx.x < nbb;
-    const int f = bnd ? v.nfi + blockIdx.x * kBlock + threadIdx.x : (blockIdx.x - nbb) * kBlock + threadIdx.x;
+    const int f = bnd ? v.nfi + blockIdx.x * bs + threadIdx.x : (blockIdx.x - nbb) * bs + threadIdx.x;
     if (f >= (bnd ? v.nof : v.nfi)) return;
     const int inst = face_inst(v, f);
     if (stopped(v, inst)) return;
@@ -1775,8 +1777,17 @@ int enqueue_minmax(uns_cc_handle* h, CCView& v) {
 // k_face_conv's grid: the boundary faces' blocks, then the interior faces'.
 #define LAUNCH_FACE_CONV(R, v)                                                                     \
     do {                                                                                           \
-        const int nb_ = std::max(1, (int)(((v).nbf + kBlock - 1) / kBlock) + nblocks((v).nfi));    \
-        k_face_conv<R><<<nb_, kBlock, 0, h->stream>>>(v);                                          \
+        const int bs_ = (v).blk_face;                                                              \
+        const int nb_ = std::max(1, ((v).nbf + bs_ - 1) / bs_ + ((v).nfi + bs_ - 1) / bs_);        \
+        k_face_conv<R><<<nb_, bs_, 0, h->stream>>>(v);                                             \
+        UNS_CUDA(cudaGetLastError());                                                              \
+    } while (0)
+
+// A launch over n items with block size bs.
+#define LAUNCH_BS(kern, n, bs, ...)                                                                \
+    do {                                                                                           \
+        const int bs_ = (bs);                                                                      \
+        kern<<<std::max(1, (int)(((n) + bs_ - 1) / bs_)), bs_, 0, h->stream>>>(__VA_ARGS__);       \
         UNS_CUDA(cudaGetLastError());                                                              \
     } while (0)
 
@@ -1821,10 +1832,10 @@ bool grad_by_sides(const uns_cc_handle* h, const CCView& v) {
 // reference main loop's RK stages 2 and 3): the boundary faces' fluxes and
 // the wall cells' residuals; every other cell keeps the residual it has.
 int enqueue_wall_res(uns_cc_handle* h, CCView& v) {
-    const int nbb = (v.nbf + kBlock - 1) / kBlock;  // k_face_conv's boundary blocks come first
+    const int nbb = (v.nbf + v.blk_face - 1) / v.blk_face;  // k_face_conv's boundary blocks come first
     if (nbb == 0) return UNS_OK;
-    if (v.mixed) k_face_conv<float><<<nbb, kBlock, 0, h->stream>>>(v);
-    else k_face_conv<double><<<nbb, kBlock, 0, h->stream>>>(v);
+    if (v.mixed) k_face_conv<float><<<nbb, v.blk_face, 0, h->stream>>>(v);
+    else k_face_conv<double><<<nbb, v.blk_face, 0, h->stream>>>(v);
     UNS_CUDA(cudaGetLastError());
     if (v.nwcell > 0) {
         const int nb = (v.nwcell + 31) / 32;
@@ -1920,10 +1931,10 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
     UNS_CUDA(cudaGetLastError());
     int bflags = BEGIN_PRIM | BEGIN_OLD | BEGIN_POS | (v.ilimit ? BEGIN_MINMAX : 0);
     LAUNCH(k_begin, v.ntot, v, bflags);
-    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v);
     const int gflags = CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0) | (h->P.time_mode == UNS_TIME_RK3 ? 0 : CG_DIAG);
     if (grad_by_sides(h, v)) {
-        LAUNCH(k_cell_grad_side, v.noc, v, gflags, 0.0);
+        LAUNCH_BS(k_cell_grad_side, v.noc, v.blk_grad, v, gflags, 0.0);
     } else {
         LAUNCH(k_face_prim_spec, v.nof, v);
         if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
@@ -1982,7 +1993,7 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
     v.done = nullptr;
     int rc;
     LAUNCH(k_begin, v.ntot, v, (int)(BEGIN_PRIM | BEGIN_OLD | BEGIN_POS));
-    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v);
     LAUNCH(k_face_prim_spec, v.nof, v);
     if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
     LAUNCH(k_cell_grad, v.noc, v, (int)(CG_DT | CG_GRAD), cfl);
@@ -2150,6 +2161,19 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     v.laminar = p->flow_type == UNS_FLOW_LAMINAR;
     v.cfl_max = p->cfl_max; v.min_res = p->min_res;
     v.mixed = p->precision == UNS_PREC_MIXED;
+    // Block sizes of the kernels without block-level reductions, from a
+    // measured sweep of 64-512 on the 4.2 M-cell mixed step and the 256-case
+    // batch (faces 64, vertices 256, cell gradient 128); UNS_CC_BLOCK_FACE /
+    // _VERTEX (64..512) and UNS_CC_BLOCK_GRAD (64..256: a divisor of the
+    // 256-cell instance-pure blocks) override them for tuning runs.
+    auto block_env = [](const char* name, int def, int hi) {
+        const char* e = std::getenv(name);
+        const int b = e ? std::atoi(e) : def;
+        return (b == 64 || b == 128 || b == 256 || b == 512) && b <= hi ? b : def;
+    };
+    v.blk_face = block_env("UNS_CC_BLOCK_FACE", 64, 512);
+    v.blk_vert = block_env("UNS_CC_BLOCK_VERTEX", kBlock, 512);
+    v.blk_grad = block_env("UNS_CC_BLOCK_GRAD", 128, kBlock);
 #define UP(field, vec) if ((rc = h->upload(*(std::remove_const<std::remove_pointer<decltype(v.field)>::type>::type**)&v.field, vec.data(), vec.size()))) return fail(rc)
 #define AL(field, n) if ((rc = h->alloc(v.field, (n)))) return fail(rc)
     UP(pxy, pxy); UP(cen, cen);
@@ -2425,7 +2449,7 @@ int uns_cc_avg_c2v(uns_cc_handle* h) {
     if (!h) return UNS_ERR_ARG;
     ++h->flux_gen;
     CCView v = h->v;
-    LAUNCH(k_vertex_avg, v.nop, v);
+    LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v);
     LAUNCH(k_face_prim_spec, v.nof, v);
     return UNS_OK;
 }
@@ -2831,13 +2855,13 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
             LAUNCH(k_begin, v.ntot, v, BEGIN_PRIM | BEGIN_OLD | BEGIN_POS | (v.ilimit ? BEGIN_MINMAX : 0));
             return UNS_OK;
         });
-        if (!rc) rc = timed(1, [&]() -> int { LAUNCH(k_vertex_avg, v.nop, v); return UNS_OK; });
+        if (!rc) rc = timed(1, [&]() -> int { LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v); return UNS_OK; });
         const bool sides = grad_by_sides(h, v);
         if (!rc && !sides) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
         if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
         if (!rc) rc = timed(4, [&]() -> int {
             const int gflags = CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0) | (rk3 ? 0 : CG_DIAG);
-            if (sides) LAUNCH(k_cell_grad_side, v.noc, v, gflags, cfl);
+            if (sides) LAUNCH_BS(k_cell_grad_side, v.noc, v.blk_grad, v, gflags, cfl);
             else LAUNCH_CELL_GRAD(v, gflags, cfl);
             return UNS_OK;
         });

@@ -35,6 +35,7 @@ struct CCView {
     const int* cf;
     const float4* sideg;  // per cf entry (GG, inviscid): outward-signed unit normal x, y; this side's offset x, y
     const int4* sidei;    // per cf entry: cell across (-1 on a boundary), end points p1, p2, length (float bits)
+    int blk_face, blk_vert, blk_grad;  // block sizes of k_face_conv, k_vertex_avg, k_cell_grad_side
     const unsigned* bcell;  // bit i: interior cell i has a wall face
     const int* wcell;       // those cells in increasing order
     int nwcell;
