@@ -222,6 +222,12 @@ void* uns_nc_stream(uns_nc_handle* h);
  * NULL) receives a static phase name.  The state advances by reps
  * iterations, exactly as uns_*_iterate would advance it. */
 int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
+/* Launch-geometry autotuner (no reference counterpart): times the face,
+ * vertex and cell-gradient kernels at each candidate block size on the
+ * handle's mesh and state (writing scratch copies only), keeps the fastest
+ * and re-captures the step.  blocks (may be NULL) receives the chosen
+ * sizes: faces, vertices, cell gradient. */
+int uns_cc_autotune(uns_cc_handle* h, int reps, int* blocks);
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
 
 /* ===================================================== no-allocation ====*/

@@ -147,3 +147,23 @@ def test_cc_fvresidual_flux_cache_equals_full_call(cc_mesh, precision):
     b.fvresidual()                 # every face
     assert np.array_equal(a.get("res"), b.get("res"))
     assert np.array_equal(a.get_state(), b.get_state())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cc_autotune_keeps_results(cc_mesh, precision):
+    """uns_cc_autotune times the kernels on scratch outputs and only changes
+    launch geometry: the tuned handle's state is untouched by the tuning and
+    its later steps equal an untuned handle's bit for bit."""
+    p = abi.make_params(flux="roe", grad="gg", m_inf=0.7, aoa_deg=2.0, precision=precision)
+    cfl = mesh.cfl_schedule(p, 1, 40, "cc")
+    a, b = CCSolver(cc_mesh, p), CCSolver(cc_mesh, p)
+    a.iterate(cfl[:20], first_iter=True)
+    b.iterate(cfl[:20], first_iter=True)
+    q0 = a.get_state()
+    blocks = a.autotune(reps=2)
+    assert set(blocks) == {"face", "vertex", "cell_grad"} and blocks["face"] in (64, 128, 256, 512)
+    assert np.array_equal(a.get_state(), q0)
+    fa = a.iterate(cfl[20:], first_iter=False)
+    fb = b.iterate(cfl[20:], first_iter=False)
+    assert np.array_equal(a.get_state(), b.get_state())
+    assert np.array_equal(fa, fb)

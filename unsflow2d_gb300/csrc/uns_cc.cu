@@ -2822,6 +2822,107 @@ int uns_cc_batch_iterate(uns_cc_batch* b, int niter, const double* cfl, int firs
 
 void* uns_cc_stream(uns_cc_handle* h) { return h ? (void*)h->stream : nullptr; }
 
+// Launch-geometry autotuner: times k_face_conv, k_vertex_avg and (in the
+// mixed Green-Gauss step) k_cell_grad_side at each candidate block size on
+// the handle's own mesh and state, keeps the fastest, and re-captures the
+// step with them.  The timed launches read the handle's arrays and write
+// scratch copies only, so the solution, the running limiter and the device
+// counters are untouched.
+int uns_cc_autotune(uns_cc_handle* h, int reps, int* blocks) {
+    if (!h || reps < 1) return UNS_ERR_ARG;
+    ++h->flux_gen;
+    const CCView& v = h->v;
+    std::vector<void*> bufs;
+    auto scratch = [&](size_t bytes) -> void* {
+        void* q = nullptr;
+        if (cudaMalloc(&q, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+        bufs.push_back(q);
+        return q;
+    };
+    auto release = [&]() { for (void* q : bufs) cudaFree(q); bufs.clear(); };
+    CCView t = v;  // inputs as the handle has them, outputs redirected
+    t.cfl_sched = nullptr; t.iter = nullptr; t.done = nullptr;
+    bool ok = (t.fF = (double4*)scratch(sizeof(double4) * v.nof)) && (t.qc = (double4*)scratch(sizeof(double4) * v.ntot)) &&
+              (t.qp = (double4*)scratch(sizeof(double4) * v.ntot)) && (t.qT = (double*)scratch(sizeof(double) * v.ntot)) &&
+              (t.qpf = (float4*)scratch(sizeof(float4) * v.ntot)) && (t.fwall = (double2*)scratch(sizeof(double2) * v.nbf)) &&
+              (t.err = (DevErr*)scratch(sizeof(DevErr))) && (t.ppf = (float4*)scratch(sizeof(float4) * v.nop)) &&
+              (t.pp = (double4*)scratch(sizeof(double4) * v.nop)) && (t.ppT = (double*)scratch(sizeof(double) * v.nop)) &&
+              (t.la = (double*)scratch(sizeof(double) * v.noc)) && (t.dt = (double*)scratch(sizeof(double) * v.noc)) &&
+              (t.dcv = (double*)scratch(sizeof(double) * v.noc)) && (t.packf = (float4*)scratch(sizeof(float4) * 4 * (size_t)v.noc)) &&
+              (t.dtmin = (unsigned long long*)scratch(sizeof(unsigned long long) * std::max(1, v.ninst))) &&
+              (t.minmax = (unsigned long long*)scratch(sizeof(unsigned long long) * 8 * std::max(1, v.ninst)));
+    if (!ok) { release(); set_last_error("uns_cc_autotune: no device memory for the scratch outputs"); return UNS_ERR_CUDA; }
+    int rc = UNS_OK;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto cuda = [&](cudaError_t e) { if (e != cudaSuccess && rc == UNS_OK) { rc = UNS_ERR_CUDA; set_last_error(std::string("uns_cc_autotune: ") + cudaGetErrorString(e)); } };
+    cuda(cudaMemcpyAsync(t.qc, v.qc, sizeof(double4) * v.ntot, cudaMemcpyDeviceToDevice, h->stream));
+    cuda(cudaMemcpyAsync(t.qp, v.qp, sizeof(double4) * v.ntot, cudaMemcpyDeviceToDevice, h->stream));
+    cuda(cudaMemcpyAsync(t.qT, v.qT, sizeof(double) * v.ntot, cudaMemcpyDeviceToDevice, h->stream));
+    cuda(cudaMemcpyAsync(t.qpf, v.qpf, sizeof(float4) * v.ntot, cudaMemcpyDeviceToDevice, h->stream));
+    cuda(cudaMemcpyAsync(t.packf, v.packf, sizeof(float4) * 4 * (size_t)v.noc, cudaMemcpyDeviceToDevice, h->stream));
+    cuda(cudaMemsetAsync(t.err, 0, sizeof(DevErr), h->stream));
+    {  // a limiter range of [0, 1] for every case
+        auto enc = [](double x) {  // enc_ord on the host
+            unsigned long long b;
+            std::memcpy(&b, &x, sizeof(b));
+            return (b & 0x8000000000000000ULL) ? ~b : (b | 0x8000000000000000ULL);
+        };
+        std::vector<unsigned long long> mm(8 * (size_t)std::max(1, v.ninst));
+        for (size_t k = 0; k < mm.size(); ++k) mm[k] = enc((k % 8) < 4 ? 1.0 : 0.0);
+        cuda(cudaMemcpyAsync(t.minmax, mm.data(), sizeof(unsigned long long) * mm.size(), cudaMemcpyHostToDevice, h->stream));
+        cuda(cudaStreamSynchronize(h->stream));
+    }
+    cuda(cudaEventCreate(&e0));
+    cuda(cudaEventCreate(&e1));
+    const bool sides = grad_by_sides(h, v);
+    auto time_it = [&](auto&& launch) -> float {
+        launch();  // warm-up
+        cuda(cudaEventRecord(e0, h->stream));
+        for (int r = 0; r < reps; ++r) launch();
+        cuda(cudaEventRecord(e1, h->stream));
+        cuda(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cuda(cudaEventElapsedTime(&ms, e0, e1));
+        cuda(cudaGetLastError());
+        return ms;
+    };
+    auto pick = [&](std::initializer_list<int> cand, auto&& launch_with) -> int {
+        int best = 0;
+        float tbest = 0.f;
+        for (int bs : cand) {
+            const float ms = time_it([&]() { launch_with(bs); });
+            if (rc) return 0;
+            if (!best || ms < tbest) { best = bs; tbest = ms; }
+        }
+        return best;
+    };
+    int bf = 0, bv = 0, bg = 0;
+    if (rc == UNS_OK && v.nof > 0)
+        bf = pick({64, 128, 256, 512}, [&](int bs) {
+            const int nb = std::max(1, (v.nbf + bs - 1) / bs + (v.nfi + bs - 1) / bs);
+            if (v.mixed) k_face_conv<float><<<nb, bs, 0, h->stream>>>(t);
+            else k_face_conv<double><<<nb, bs, 0, h->stream>>>(t);
+        });
+    if (rc == UNS_OK && v.nop > 0)
+        bv = pick({64, 128, 256, 512}, [&](int bs) { k_vertex_avg<<<(v.nop + bs - 1) / bs, bs, 0, h->stream>>>(t); });
+    if (rc == UNS_OK && sides && v.noc > 0)
+        bg = pick({64, 128, 256}, [&](int bs) {
+            k_cell_grad_side<<<(v.noc + bs - 1) / bs, bs, 0, h->stream>>>(t, CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0), 0.5);
+        });
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaStreamSynchronize(h->stream);
+    release();
+    if (rc) return rc;
+    if (bf) h->v.blk_face = bf;
+    if (bv) h->v.blk_vert = bv;
+    if (bg) h->v.blk_grad = bg;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    ++h->gen;  // the captured step changes
+    if (blocks) { blocks[0] = h->v.blk_face; blocks[1] = h->v.blk_vert; blocks[2] = h->v.blk_grad; }
+    return check_dev_err(h);
+}
+
 int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase) {
     static const char* kNames[] = {"begin", "vertex_avg", "face_prim_spec", "face_ggfc", "cell_grad", "face_conv",
                                    "viscous", "cell_res", "cirs", "lusgs_sweeps", "residue", "cell_rk23"};

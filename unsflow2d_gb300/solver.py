@@ -73,6 +73,15 @@ class _Solver:
         self._call("profile", C.c_double(cfl), reps, _dp(ms), names, n)
         return {names[k].decode(): float(ms[k]) for k in range(n) if names[k] and names[k].decode()}
 
+    def autotune(self, reps: int = 3) -> dict:
+        """Pick the block sizes of the face, vertex and cell-gradient kernels by
+        timing them on this handle (uns_cc_autotune; CCFVM only)."""
+        if self.kind != "cc":
+            raise NotImplementedError("the launch-geometry autotuner covers the CCFVM kernels")
+        b = (C.c_int * 3)()
+        self._call("autotune", reps, b)
+        return {"face": b[0], "vertex": b[1], "cell_grad": b[2]}
+
     def get(self, field: str) -> np.ndarray:
         shape = self._field_shape(field)
         out = np.zeros(shape)
@@ -354,6 +363,13 @@ class CCPacked:
 
     def set_precision(self, precision: str) -> None:
         abi.check(self._lib.uns_cc_set_precision(self._h, abi.PREC[precision]), self._lib, "uns_cc_set_precision")
+
+    def autotune(self, reps: int = 3) -> dict:
+        """Block sizes of the face, vertex and cell-gradient kernels picked by
+        timing them on the packed mesh (uns_cc_autotune)."""
+        b = (C.c_int * 3)()
+        abi.check(self._lib.uns_cc_autotune(self._h, reps, b), self._lib, "uns_cc_autotune")
+        return {"face": b[0], "vertex": b[1], "cell_grad": b[2]}
 
     def stream(self) -> int:
         return int(self._lib.uns_cc_stream(self._h) or 0)
