@@ -378,9 +378,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
                     for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + q[j] * dx; gy[j] = gy[j] + q[j] * dy; }
                 }
             }
-            double var = v.cv[i];
+            const double var = v.cv[i], rv = 1.0 / var;  // eight quotients by cv: one division (Markstein)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { gx[j] = gx[j] / var; gy[j] = gy[j] / var; }
+            for (int j = 0; j < 4; ++j) { gx[j] = div_rn_recip(gx[j], var, rv); gy[j] = div_rn_recip(gy[j], var, rv); }
         } else if (v.grad_type == UNS_GRAD_GGFC) {
             for (int k = k0; k < k1; ++k) {
                 int f = v.cf[k] & FACE_MASK;
@@ -391,9 +391,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 #pragma unroll
                 for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + a[j] * s; gy[j] = gy[j] + b[j] * s; }
             }
-            double var = v.cov[i];
+            const double var = v.cov[i], rv = 1.0 / var;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { gx[j] = gx[j] / var; gy[j] = gy[j] / var; }
+            for (int j = 0; j < 4; ++j) { gx[j] = div_rn_recip(gx[j], var, rv); gy[j] = div_rn_recip(gy[j], var, rv); }
         } else {  // LSQR
             double qi[4];
             d4get(v.qp[i], qi);
@@ -455,6 +455,12 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 #pragma unroll
             for (int j = 0; j < 4; ++j) { umax[j] = rmax(umax[j], u[j]); umin[j] = rmin(umin[j], u[j]); }
         }
+        // phi = min(phi, phi0 of every face): the faces' ratios nr/dr are
+        // compared exactly and only the smallest is divided (the minimum of
+        // correctly rounded quotients is the rounded minimum), so one IEEE
+        // division per variable instead of one per face and variable.
+        double bn[4], bd[4];
+        bool have[4] = {false, false, false, false};
         double2 c = v.cen[i];
         for (int k = k0; k < k1; ++k) {
             int f = v.cf[k] & FACE_MASK;
@@ -463,12 +469,22 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 double D_L = gx[j] * d0 + gy[j] * d1;
-                double phi0 = 1.0;
-                if (D_L > 0.0) phi0 = vk_limit(umax[j] - qi[j], D_L, tol[j]);
-                else if (D_L < 0.0) phi0 = vk_limit(umin[j] - qi[j], D_L, tol[j]);
-                ph[j] = rmin(ph[j], phi0);
+                if (D_L > 0.0 || D_L < 0.0) {
+                    double nr, dr;
+                    vk_terms((D_L > 0.0 ? umax[j] : umin[j]) - qi[j], D_L, tol[j], nr, dr);
+                    if (!ratio_ok(nr, dr)) {
+                        ph[j] = rmin(ph[j], nr / dr);
+                    } else if (!have[j] || ratio_less(nr, dr, bn[j], bd[j])) {
+                        bn[j] = nr; bd[j] = dr; have[j] = true;
+                    }
+                } else {
+                    ph[j] = rmin(ph[j], 1.0);
+                }
             }
         }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (have[j]) ph[j] = rmin(ph[j], bn[j] / bd[j]);
         v.phi[i] = d4(ph);
     }
 }

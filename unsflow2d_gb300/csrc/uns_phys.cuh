@@ -408,11 +408,61 @@ __device__ __forceinline__ CCBnd<S> cc_boundary(const Gas& g, int bc, double nx,
     return o;
 }
 
-// Venkatakrishnan limiter function (CCFVM/limiter.F90:286-294)
+// Venkatakrishnan limiter function (CCFVM/limiter.F90:286-294): its
+// numerator and denominator, and their quotient.
+__device__ __forceinline__ void vk_terms(double a, double b, double tol, double& nr, double& dr) {
+    nr = a * a + 2.0 * a * b + tol * tol;
+    dr = a * a + 2.0 * b * b + a * b + tol * tol;
+}
 __device__ __forceinline__ double vk_limit(double a, double b, double tol) {
-    double nr = a * a + 2.0 * a * b + tol * tol;
-    double dr = a * a + 2.0 * b * b + a * b + tol * tol;
+    double nr, dr;
+    vk_terms(a, b, tol, nr, dr);
     return nr / dr;
+}
+
+// Exponent field of a double (integer pipe).
+__device__ __forceinline__ int dexp_field(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+// RN(a / b) given y = RN(1 / b), by Markstein's correction (P. Markstein,
+// "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Develop. 34(1), 1990): with q0 = RN(a y) (within
+// one ulp of a/b) the remainder r = a - b q0 is exact in one FMA, and
+// RN(q0 + r y) is the correctly rounded quotient.  The theorem assumes no
+// overflow or underflow, so operands and results outside a margin of the
+// normal range (and subnormals) take the IEEE division instead; for a zero
+// numerator the quotient is q0 itself (the corrected sum would turn -0 into
+// +0).  One IEEE division per distinct divisor, then three FP64 operations
+// per quotient.
+__device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
+    const double q0 = a * y;
+    const bool zero = (__double_as_longlong(a) & 0x7fffffffffffffffLL) == 0;
+    if (zero) return q0;
+    const double r = __fma_rn(-q0, b, a);
+    const double q1 = __fma_rn(r, y, q0);
+    const int ea = dexp_field(a), eq = dexp_field(q1);
+    if (ea < 128 || ea > 1920 || eq < 128 || eq > 1920) return a / b;
+    return q1;
+}
+
+// Whether n1/d1 < n2/d2 exactly (d1, d2 > 0, all finite and normal, the
+// cross products inside the normal range): n1 d2 and n2 d1 as exact
+// double-double values (product and its FMA error term) compared.  The
+// minimum of correctly rounded quotients is the correctly rounded quotient
+// of the exact minimum (rounding is monotonic), so one division of the
+// selected pair gives min_k RN(n_k / d_k).
+__device__ __forceinline__ bool ratio_less(double n1, double d1, double n2, double d2) {
+    const double p1 = n1 * d2, p2 = n2 * d1;
+    if (p1 != p2) return p1 < p2;
+    return __fma_rn(n1, d2, -p1) < __fma_rn(n2, d1, -p2);
+}
+
+// Whether the ratio test above is exact for these operands: d positive,
+// both with binary exponents within [-463, 457] (n may be zero), so that
+// every cross product and its error term stay normal.
+__device__ __forceinline__ bool ratio_ok(double n, double d) {
+    const int en = dexp_field(n), ed = dexp_field(d);
+    const bool nz = (__double_as_longlong(n) & 0x7fffffffffffffffLL) == 0;
+    return (nz || (en >= 560 && en <= 1480)) && ed >= 560 && ed <= 1480 && d > 0.0;
 }
 
 // Order-preserving 64-bit encoding of a double for atomicMax/atomicMin.
