@@ -144,39 +144,58 @@ __global__ void __launch_bounds__(kBlock) k_nc_grad_lim(NCView v) {
         }
     }
     g4(v.phi[i], ph);
-    double2 xi = v.pxy[i];
     double sq = sqrt(v.cv[i]);
+    // phi = min(phi, phj of every edge).  Each phj is min(1, n/d) (Barth:
+    // clamped to [0, 1] in the corrected form) and the clamps are monotonic,
+    // so only the smallest ratio needs a division: the edges' ratios are
+    // compared exactly (double-double cross products, denominators made
+    // positive) and the minimum of correctly rounded quotients is the
+    // rounded minimum.  One IEEE division per variable instead of one per
+    // edge and variable; the values are those of the per-edge form.
+    const bool vkn = v.limiter == UNS_LIM_VKN, corrected = v.limiter == UNS_LIM_BARTH_CORRECTED;
+    double bn[4], bd[4];
+    bool have[4] = {false, false, false, false};
+    auto clamp = [&](double q) {
+        double phj = rmin(1.0, q);
+        return (!vkn && corrected) ? rmax(0.0, phj) : phj;
+    };
     for (int k = k0; k < k1; ++k) {
         int e = v.v2f[k], f = e & EDGE_MASK;
         int2 p = v.fpt[f];
         double2 a = v.pxy[p.x], b = v.pxy[p.y];
         double d0 = b.x - a.x, d1 = b.y - a.y;
-        (void)xi;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             double s = gx[j] * d0 + gy[j] * d1;
-            double phj;
-            if (v.limiter == UNS_LIM_VKN) {
+            double n, d;  // phj = clamp(n / d), or 1 where there is no ratio
+            bool ratio = true;
+            if (vkn) {
                 double D_L = (e & P2_BIT) ? -(0.5 * s) : 0.5 * s;
                 double kk = v.kappa * sq;
                 double TOL = kk * kk * kk;
                 double alfa = D_L > 0.0 ? dmx[j] : dmn[j];
                 if (fabs(alfa) < v.eps) alfa = 0.0;
-                double nr = alfa * alfa + 2.0 * D_L * alfa + TOL;
-                double dr = alfa * alfa + 2.0 * D_L * D_L + D_L * alfa + TOL;
-                phj = rmin(1.0, nr / dr);
+                n = alfa * alfa + 2.0 * D_L * alfa + TOL;
+                d = alfa * alfa + 2.0 * D_L * D_L + D_L * alfa + TOL;
             } else {  // Barth-Jespersen: reference form projects fp2 with +1/2
-                const bool corrected = v.limiter == UNS_LIM_BARTH_CORRECTED;
                 double D_L = 0.5 * s;
                 if (corrected && (e & P2_BIT)) D_L = -D_L;
-                if (D_L > 0.0) phj = rmin(1.0, dmx[j] / D_L);
-                else if (D_L < 0.0) phj = rmin(1.0, dmn[j] / D_L);
-                else phj = 1.0;
-                if (corrected) phj = rmax(0.0, phj);
+                if (D_L > 0.0) { n = dmx[j]; d = D_L; }
+                else if (D_L < 0.0) { n = -dmn[j]; d = -D_L; }  // dmn / D_L with a positive denominator
+                else ratio = false;
             }
-            ph[j] = rmin(ph[j], phj);
+            if (!ratio) {
+                ph[j] = rmin(ph[j], clamp(1.0));
+            } else if (!ratio_ok(n, d)) {
+                ph[j] = rmin(ph[j], clamp(n / d));
+            } else if (!have[j] || ratio_less(n, d, bn[j], bd[j])) {
+                bn[j] = n; bd[j] = d; have[j] = true;
+            }
         }
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (have[j]) ph[j] = rmin(ph[j], clamp(bn[j] / bd[j]));
     v.phi[i] = m4(ph);
 }
 
