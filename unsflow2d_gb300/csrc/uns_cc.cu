@@ -338,14 +338,16 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
     const int inst = cell_inst(v, i);
     if (inst < 0 || stopped(v, inst)) return;
     const int k0 = v.cf_off[i], k1 = v.cf_off[i + 1];
+    const double cvi = v.cv[i];
+    const double rcv = (flags & (CG_DT | CG_GRAD)) ? 1.0 / cvi : 0.0;  // shared by dt/cv and the gradient
     if (flags & CG_DT) {
         double la = 0.0;
         for (int k = k0; k < k1; ++k) la = la + v.fla[v.cf[k] & FACE_MASK];
         v.la[i] = la;
         double cfl = cur_cfl(v, inst, cfl_in);
-        double dt = cfl * v.cv[i] / la;
+        double dt = cfl * cvi / la;
         v.dt[i] = dt;
-        v.dcv[i] = dt / v.cv[i];
+        v.dcv[i] = div_rn_recip(dt, cvi, rcv);
         if (flags & CG_DIAG) {
             v.diag[i] = v.cv[i] / dt + 0.5 * 1.5 * la;
             v.diaginv[i] = 1.0 / v.diag[i];
@@ -378,9 +380,11 @@ __global__ void __launch_bounds__(kBlock) k_cell_grad(CCView v, int flags, doubl
                     for (int j = 0; j < 4; ++j) { gx[j] = gx[j] + q[j] * dx; gy[j] = gy[j] + q[j] * dy; }
                 }
             }
-            const double var = v.cv[i], rv = 1.0 / var;  // eight quotients by cv: one division (Markstein)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) { gx[j] = div_rn_recip(gx[j], var, rv); gy[j] = div_rn_recip(gy[j], var, rv); }
+            for (int j = 0; j < 4; ++j) {  // eight quotients by cv through its reciprocal (Markstein)
+                gx[j] = div_rn_recip(gx[j], cvi, rcv);
+                gy[j] = div_rn_recip(gy[j], cvi, rcv);
+            }
         } else if (v.grad_type == UNS_GRAD_GGFC) {
             for (int k = k0; k < k1; ++k) {
                 int f = v.cf[k] & FACE_MASK;
