@@ -51,6 +51,9 @@ struct NCView {
     const int* rv2f;
     double4* qc;
     double4* qp;
+    float4* qpf;          // FP32 copy of qp (k_nc_save_old), read by the mixed form's gradient pass
+    const float2* wxyf;   // FP32 LSQ weights per v2v entry
+    const float2* edf;    // FP32 edge vector X(fp2) - X(fp1) per edge
     double4* qold;
     double4* res;
     double4* gx;
@@ -102,7 +105,82 @@ __global__ void __launch_bounds__(kBlock) k_nc_save_old(NCView v) {
     double4 q = v.qc[i];
     Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
     v.qp[i] = make_double4(P.rho, P.u, P.v, P.p);
+    v.qpf[i] = make_float4((float)P.rho, (float)P.u, (float)P.v, (float)P.p);
     v.qold[i] = q;
+}
+
+// k_nc_grad_lim in the mixed form: the LSQ gradient and the limiter in FP32
+// on the FP32 primitives, weights and edge vectors (the same gathers,
+// orders and formulas); gradient and phi stored in FP64 for the edge pass
+// (phi stays the FP64 running minimum).
+__global__ void __launch_bounds__(kBlock) k_nc_grad_lim_mixed(NCView v) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nop) return;
+    const float4 q4 = v.qpf[i];
+    const float qi[4] = {q4.x, q4.y, q4.z, q4.w};
+    float gx[4] = {0.f, 0.f, 0.f, 0.f}, gy[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int j = v.v2v_off[i]; j < v.v2v_off[i + 1]; ++j) {
+        const float4 c = v.qpf[v.v2v[j]];
+        const float2 w = v.wxyf[j];
+        const float qc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            gx[k] = gx[k] + (qc[k] - qi[k]) * w.x;
+            gy[k] = gy[k] + (qc[k] - qi[k]) * w.y;
+        }
+    }
+    v.gx[i] = make_double4(gx[0], gx[1], gx[2], gx[3]);
+    v.gy[i] = make_double4(gy[0], gy[1], gy[2], gy[3]);
+    const float eps = (float)v.eps;
+    float dmx[4], dmn[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { dmn[k] = eps; dmx[k] = -eps; }
+    const int k0 = v.v2f_off[i], k1 = v.v2f_off[i + 1];
+    for (int k = k0; k < k1; ++k) {
+        const int e = v.v2f[k], f = e & EDGE_MASK;
+        const int2 p = v.fpt[f];
+        const float4 a = v.qpf[p.x], b = v.qpf[p.y];
+        const float du4[4] = {b.x - a.x, b.y - a.y, b.z - a.z, b.w - a.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float du = (e & P2_BIT) ? -du4[j] : du4[j];
+            dmx[j] = rmax(dmx[j], du);
+            dmn[j] = rmin(dmn[j], du);
+        }
+    }
+    double ph[4];
+    g4(v.phi[i], ph);
+    const float sq = sqrtf((float)v.cv[i]);
+    const bool vkn = v.limiter == UNS_LIM_VKN, corrected = v.limiter == UNS_LIM_BARTH_CORRECTED;
+    for (int k = k0; k < k1; ++k) {
+        const int e = v.v2f[k], f = e & EDGE_MASK;
+        const float2 d = v.edf[f];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float s = gx[j] * d.x + gy[j] * d.y;
+            float phj;
+            if (vkn) {
+                const float D_L = (e & P2_BIT) ? -(0.5f * s) : 0.5f * s;
+                const float kk = (float)v.kappa * sq;
+                const float TOL = kk * kk * kk;
+                float alfa = D_L > 0.f ? dmx[j] : dmn[j];
+                if (fabsf(alfa) < eps) alfa = 0.f;
+                const float nr = alfa * alfa + 2.f * D_L * alfa + TOL;
+                const float dr = alfa * alfa + 2.f * D_L * D_L + D_L * alfa + TOL;
+                phj = rmin(1.f, nr / dr);
+            } else {  // Barth-Jespersen: reference form projects fp2 with +1/2
+                float D_L = 0.5f * s;
+                if (corrected && (e & P2_BIT)) D_L = -D_L;
+                if (D_L > 0.f) phj = rmin(1.f, dmx[j] / D_L);
+                else if (D_L < 0.f) phj = rmin(1.f, dmn[j] / D_L);
+                else phj = 1.f;
+                if (corrected) phj = rmax(0.f, phj);
+            }
+            ph[j] = rmin(ph[j], (double)phj);
+        }
+    }
+    v.phi[i] = m4(ph);
 }
 
 __global__ void __launch_bounds__(kBlock) k_nc_grad_lim(NCView v) {
@@ -903,7 +981,8 @@ int check_err_nc(uns_nc_handle* h) {
     } while (0)
 
 int enqueue_fvres_nc(uns_nc_handle* h, NCView& v, double cfl, int irk, int partial) {
-    NLAUNCH(k_nc_grad_lim, v.nop, v);
+    if (h->P.precision == UNS_PREC_MIXED) NLAUNCH(k_nc_grad_lim_mixed, v.nop, v);
+    else NLAUNCH(k_nc_grad_lim, v.nop, v);
     if (h->P.precision == UNS_PREC_MIXED) NLAUNCH(k_nc_edge<float>, v.nof, v);
     else NLAUNCH(k_nc_edge<double>, v.nof, v);
     NLAUNCH(k_nc_node_res, v.nop, v, cfl, irk, partial);
@@ -1051,10 +1130,17 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     { std::vector<int> t(m->v2v_off, m->v2v_off + nop + 1); UPN(v2v_off, t); }
     { std::vector<int> t(m->v2v, m->v2v + m->v2v_off[nop]); UPN(v2v, t); }
     UPN(wxy, wxy);
+    {  // FP32 copies for the mixed form's gradient pass
+        std::vector<float2> wf(wxy.size()), ef(nof);
+        for (size_t k = 0; k < wxy.size(); ++k) wf[k] = make_float2((float)wxy[k].x, (float)wxy[k].y);
+        for (int f = 0; f < nof; ++f)
+            ef[f] = make_float2((float)(pxy[fpt[f].y].x - pxy[fpt[f].x].x), (float)(pxy[fpt[f].y].y - pxy[fpt[f].x].y));
+        UPN(wxyf, wf); UPN(edf, ef);
+    }
     UPN(v2f_off, cnt); UPN(v2f, vf);
     { std::vector<int> t(m->v2f_off, m->v2f_off + nop + 1); UPN(rv2f_off, t); }
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
-    ALN(qc, nop); ALN(qp, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
+    ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
     ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
     ALN(err, 1);
@@ -1313,7 +1399,11 @@ int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const cha
     for (int r = 0; r < reps && !rc; ++r) {
         rc = timed(0, [&]() -> int { NLAUNCH(k_nc_save_old, v.nop, v); return UNS_OK; });
         for (int irk = 1; irk <= (rk3 ? 3 : 1) && !rc; ++irk) {
-            if (!rc) rc = timed(1, [&]() -> int { NLAUNCH(k_nc_grad_lim, v.nop, v); return UNS_OK; });
+            if (!rc) rc = timed(1, [&]() -> int {
+                if (h->P.precision == UNS_PREC_MIXED) NLAUNCH(k_nc_grad_lim_mixed, v.nop, v);
+                else NLAUNCH(k_nc_grad_lim, v.nop, v);
+                return UNS_OK;
+            });
             if (!rc) rc = timed(2, [&]() -> int {
                 if (h->P.precision == UNS_PREC_MIXED) NLAUNCH(k_nc_edge<float>, v.nof, v);
                 else NLAUNCH(k_nc_edge<double>, v.nof, v);
