@@ -52,6 +52,7 @@ struct NCView {
     double4* qc;
     double4* qp;
     float4* qpf;          // FP32 copy of qp (k_nc_save_old), read by the mixed form's gradient pass
+    float4* packn;        // mixed form, per node: FP32 gx, gy, phi (k_nc_grad_lim_mixed) for the edge pass
     const float2* wxyf;   // FP32 LSQ weights per v2v entry
     const float2* edf;    // FP32 edge vector X(fp2) - X(fp1) per edge
     double4* qold;
@@ -181,6 +182,10 @@ __global__ void __launch_bounds__(kBlock) k_nc_grad_lim_mixed(NCView v) {
         }
     }
     v.phi[i] = m4(ph);
+    float4* pk = v.packn + 3 * (size_t)i;
+    pk[0] = make_float4(gx[0], gx[1], gx[2], gx[3]);
+    pk[1] = make_float4(gy[0], gy[1], gy[2], gy[3]);
+    pk[2] = make_float4((float)ph[0], (float)ph[1], (float)ph[2], (float)ph[3]);
 }
 
 __global__ void __launch_bounds__(kBlock) k_nc_grad_lim(NCView v) {
@@ -282,6 +287,47 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
     if (stopped(v)) return;
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
+    if constexpr (std::is_same<R, float>::value) {
+        // mixed form, an interior edge: FP32 copies only (primitives, the node
+        // pack of gradient and limiter, edge vector), the same formulas
+        const int bc = v.fbc[f];
+        if (bc != 1001 && bc != 2001) {
+            const int2 p = v.fpt[f];
+            const float4 qa = v.qpf[p.x], qb = v.qpf[p.y];
+            const float4* A = v.packn + 3 * (size_t)p.x;
+            const float4* B = v.packn + 3 * (size_t)p.y;
+            const float4 ga = A[0], ha = A[1], pa = A[2], gb = B[0], hb = B[1], pb = B[2];
+            const float2 d = v.edf[f];
+            const float q1[4] = {qa.x, qa.y, qa.z, qa.w}, q2[4] = {qb.x, qb.y, qb.z, qb.w};
+            const float a[4] = {ga.x, ga.y, ga.z, ga.w}, b[4] = {ha.x, ha.y, ha.z, ha.w};
+            const float c[4] = {gb.x, gb.y, gb.z, gb.w}, e[4] = {hb.x, hb.y, hb.z, hb.w};
+            const float f1[4] = {pa.x, pa.y, pa.z, pa.w}, f2[4] = {pb.x, pb.y, pb.z, pb.w};
+            V4<float> L, Rt, F;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {  // fvresidual.f90:576-590
+                float g = a[k] * d.x + b[k] * d.y;
+                L[k] = q1[k] + 0.5f * g * f1[k];
+                g = c[k] * d.x + e[k] * d.y;
+                Rt[k] = q2[k] - 0.5f * g * f2[k];
+            }
+            const double2 n = v.fn[f];
+            const float area = (float)v.farea[f];
+            const float G = (float)v.g.gamma, G1 = (float)v.g.gamma1;
+            float hl, hr;
+            if (v.g.flux == UNS_FLUX_AUSM) ausm_core<float>(G, G1, (float)n.x, (float)n.y, (float)v.g.mref, L, Rt, F, hl, hr);
+            else vanleer_core<float>(G, G1, (float)n.x, (float)n.y, L, Rt, F, hl, hr);
+            v.fF[f] = make_double4(F[0] * area, F[1] * area, F[2] * area, F[3] * area);
+            // Roe-averaged spectral radius (vanleer_flux.f90:417-430)
+            const float RT = sqrtf(Rt[0] / L[0]);
+            const float u = (L[1] + RT * Rt[1]) / (1.f + RT);
+            const float vv = (L[2] + RT * Rt[2]) / (1.f + RT);
+            const float H = (hl + RT * hr) / (1.f + RT);
+            const float aa = sqrtf(G1 * (H - 0.5f * (u * u + vv * vv)));
+            const float un = fabsf(u * (float)n.x + vv * (float)n.y);
+            v.fla[f] = (double)((un + aa) * area);
+            return;
+        }
+    }
     int2 p = v.fpt[f];
     double2 X1 = v.pxy[p.x], X2 = v.pxy[p.y];
     double d0 = X2.x - X1.x, d1 = X2.y - X1.y;
@@ -1140,7 +1186,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     UPN(v2f_off, cnt); UPN(v2f, vf);
     { std::vector<int> t(m->v2f_off, m->v2f_off + nop + 1); UPN(rv2f_off, t); }
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
-    ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
+    ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(packn, 3 * (size_t)nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
     ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
     ALN(err, 1);
