@@ -2,8 +2,8 @@
  * unsflow_host.h -- C-ABI of libunsflow_host.so, the caller side of the drop-in.
  *
  * The reference keeps the Fortran driver, flo.inp and geometry.inp as they
- * are and replaces only the hot-path subroutines.  No Fortran compiler exists
- * in this build environment, so the caller side is provided in C++ here:
+ * are and replaces only the hot-path subroutines.  For hosts without a
+ * Fortran compiler the caller side is also provided in C++:
  * the geometry.inp readers and the geometric preprocessing restated from
  * CCFVM/geometric.F90 and NCFVM/geometric.f90 (connectivity orders matter:
  * they fix summation and LU-SGS sweep order), a flo.inp reader, an analytic
