@@ -248,7 +248,7 @@ TRAFFIC_PER_UNIT = {
     ("cc", "face_conv", True): (156.96e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (138.34e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_grad", True): (261.72e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
-    ("cc", "cell_grad", False): (68.62e6 / 262144, "cells", "profiles/cc_fp64_512x256_full.md"),
+    ("cc", "cell_grad", False): (68.84e6 / 262144, "cells", "profiles/cc_fp64_512x256_full.md"),
 }
 
 # FP64-pipe utilisation (sm__pipe_fp64_cycles_active, fraction of peak while
@@ -256,7 +256,7 @@ TRAFFIC_PER_UNIT = {
 # fraction, the one that bounds the FP64 kernels.
 FP64_PIPE = {
     ("nc", "lusgs_sweeps", False): (0.122, "profiles/nc_lusgs_512x256_full.md"),
-    ("cc", "cell_grad", False): (0.864, "profiles/cc_fp64_512x256_full.md"),
+    ("cc", "cell_grad", False): (0.845, "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", False): (0.847, "profiles/cc_fp64_512x256_full.md"),
     ("cc", "cell_res", False): (0.799, "profiles/cc_fp64_512x256_full.md"),
     ("cc", "cell_grad", True): (0.198, "profiles/cc_mixed_1024x512_full.md"),
