@@ -251,6 +251,9 @@ int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const cha
  * at zero.  ncells > UNS_RMS_NOALLOC_MAX_CELLS, NULL pointers or a misaligned
  * array give UNS_ERR_ARG before any device work.  The first call on each
  * device looks up the scratch address; make it before any stream capture.
+ * The address belongs to the context it was looked up in: the first call in
+ * a new context of the device (after cudaDeviceReset) looks it up again.
+ * Every call synchronises `stream` before it returns.
  * Calls that overlap on one device (other threads or streams) share the
  * scratch and race: serialise them. */
 int uns_residue_rms_noalloc(const double* res, int ncells, double* fres_raw, void* stream);

@@ -29,7 +29,45 @@ static __device__ __align__(256) double g_rms_scratch[kMaxParts + 1];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-double* g_addr[kMaxDevices] = {};  // device address of g_rms_scratch, per device ordinal
+// Device address of g_rms_scratch per device ordinal, with the id of the
+// context it was looked up in.  A module's globals live in one context: after
+// cudaDeviceReset (or any reset of the device's primary context) the library
+// is loaded again in a new context and the old address means nothing, so the
+// address is looked up again whenever the current context's id differs.
+double* g_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
+
+// Driver entry points for the current context's id, resolved through the
+// runtime so the library does not link libcuda itself.
+typedef int (*ctx_get_current_fn)(void**);
+typedef int (*ctx_get_id_fn)(void*, unsigned long long*);
+
+// Id of the current context, 0 when the driver cannot say (then the address
+// is looked up on every call).
+unsigned long long current_ctx_id() {
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q0 == cudaDriverEntryPointSuccess && q1 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<ctx_get_current_fn>(f0);
+            get_id = reinterpret_cast<ctx_get_id_fn>(f1);
+        }
+        cudaGetLastError();
+        resolved = true;
+    }
+    if (!get_current || !get_id) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 __global__ void __launch_bounds__(kBlock) k_rms_partial(const double4* __restrict__ res, int n, double* part) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -62,8 +100,8 @@ __global__ void __launch_bounds__(kBlock) k_rms_final(const double* part, int np
     if (threadIdx.x == 0) *out = sqrt(s[0] / (double)n / 4.0);
 }
 
-// Address of the scratch on the current device, looked up on the first call
-// for that device only.
+// Address of the scratch on the current device: looked up on the first call
+// for that device, and again on the first call in each new context of it.
 int scratch_address(double** out) {
     int dev = -1;
     UNS_CUDA(cudaGetDevice(&dev));
@@ -72,10 +110,12 @@ int scratch_address(double** out) {
         return UNS_ERR_ARG;
     }
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
+    const unsigned long long ctx = current_ctx_id();
+    if (!g_addr[dev] || ctx == 0 || ctx != g_ctx_id[dev]) {
         void* p = nullptr;
         UNS_CUDA(cudaGetSymbolAddress(&p, g_rms_scratch));
         g_addr[dev] = static_cast<double*>(p);
+        g_ctx_id[dev] = ctx;
     }
     *out = g_addr[dev];
     return UNS_OK;
