@@ -37,12 +37,12 @@ typedef struct uns_cc_handle uns_cc_handle;
 
 /* Copies the preprocessed mesh (the `grid` module after geometric,
  * CCFVM/geometric.F90:1-57) and the flo.inp parameters to the device and
- * sets the freestream (CCFVM/read_input.F90:237-262).  The caller may free
+ * sets the freestream (CCFVM/solution.F90:24-45).  The caller may free
  * its arrays afterwards. */
 int uns_cc_create(const uns_cc_mesh* mesh, const uns_params* params, uns_cc_handle** out);
 int uns_cc_destroy(uns_cc_handle* h);
 
-/* initialize (CCFVM/read_input.F90:291-294): qc = freestream on every cell
+/* initialize (CCFVM/solution.F90:18-84): qc = freestream on every cell
  * including ghosts, phi = 1, primitives 0. */
 int uns_cc_initialize(uns_cc_handle* h);
 /* Conserved state of all noc+nbf cells, [noc+nbf][4] row-major. */
@@ -60,12 +60,12 @@ int uns_cc_set_field(uns_cc_handle* h, int field, const double* in);
 int uns_cc_con2prim(uns_cc_handle* h);
 /* avg_c2v (CCFVM/average.F90:1-39). */
 int uns_cc_avg_c2v(uns_cc_handle* h);
-/* time_step02 + spectral02 (CCFVM/timestep.F90:350-429); dtglobal may be NULL. */
+/* time_step02 + spectral02 (CCFVM/timestep.F90:28-107); dtglobal may be NULL. */
 int uns_cc_time_step(uns_cc_handle* h, double cfl, double* dtglobal);
-/* save_old (CCFVM/solution.F90:331-345). */
+/* save_old (CCFVM/solution.F90:118-132). */
 int uns_cc_save_old(uns_cc_handle* h);
 /* Gradient_GG / Gradient_GG_FC / Gradient_LSQR per params.grad_type,
- * followed by limit when params.ilimit == 1 (CCFVM/gradient.F90:293-614). */
+ * followed by limit when params.ilimit == 1 (CCFVM/gradient.F90:2-323). */
 int uns_cc_gradient(uns_cc_handle* h);
 /* limit -> limiter_VKN1 (CCFVM/limiter.F90:3-17,123-296). */
 int uns_cc_limit(uns_cc_handle* h);
@@ -74,16 +74,17 @@ int uns_cc_limit(uns_cc_handle* h);
 int uns_cc_fvresidual(uns_cc_handle* h);
 /* One RK3 stage update, irk = 1..3 (CCFVM/main.F90:90-101). */
 int uns_cc_rk_stage(uns_cc_handle* h, int irk);
-/* lusgs -> lusgs2 (CCFVM/lusgs.F90:5-10,207-379), level-scheduled. */
+/* lusgs -> lusgs2 (CCFVM/lusgs.F90:5-10,207-379): both sweeps as one
+ * list-scheduled dataflow launch in the reference's cell order. */
 int uns_cc_lusgs(uns_cc_handle* h);
 /* check_positivity (CCFVM/main.F90:358-414): UNS_ERR_NONPOSITIVE and the
  * 0-based cell index in *bad_cell (-1 when none). */
 int uns_cc_check_positivity(uns_cc_handle* h, int* bad_cell);
-/* residue (CCFVM/solution.F90:349-372): sqrt(sum res^2 / noc / 4) before the
+/* residue (CCFVM/solution.F90:136-180): sqrt(sum res^2 / noc / 4) before the
  * first-iteration normalisation, which stays with the caller. */
 int uns_cc_residue(uns_cc_handle* h, double* fres_raw);
 /* Flux-based wall forces Fx1, Fy1 of the last fvresidual
- * (CCFVM/fvresidual.F90:99-100, CCFVM/viscous_flux.F90:530-533). */
+ * (CCFVM/fvresidual.F90:99-100, CCFVM/viscous_flux.F90:73-74). */
 int uns_cc_forces(uns_cc_handle* h, double* fx1, double* fy1);
 /* find_cl_cd (CCFVM/main.F90:263-355) on the device, from the last residual:
  * coef[0..4] = C_L, C_D of the pressure + viscous wall integral, C_m about
@@ -124,14 +125,15 @@ int uns_nc_save_old(uns_nc_handle* h);
 /* fvresidual (NCFVM/fvresidual.f90:4-85): Gradient_LSQR, limiter, edge
  * fluxes, wall and farfield closures, then time_step2 with this CFL. */
 int uns_nc_fvresidual(uns_nc_handle* h, double cfl);
-/* One RK3 stage update, irk = 1..3 (NCFVM/main.f90:321-342). */
+/* One RK3 stage update, irk = 1..3 (NCFVM/main.f90:59-80). */
 int uns_nc_rk_stage(uns_nc_handle* h, int irk);
-/* lusgs (NCFVM/lusgs.f90:4-157), level-scheduled; calls fvresidual. */
+/* lusgs (NCFVM/lusgs.f90:4-157): both sweeps as one list-scheduled
+ * dataflow launch in the reference's node order; calls fvresidual. */
 int uns_nc_lusgs(uns_nc_handle* h, double cfl);
 /* residue (NCFVM/common.f90:108-154) before normalisation: L2 over nodes,
  * Linf and its 0-based node (any output pointer may be NULL). */
 int uns_nc_residue(uns_nc_handle* h, double* fres_raw, double* fresi, int* iresi);
-/* Fast path as uns_cc_iterate for the loop body NCFVM/main.f90:315-348;
+/* Fast path as uns_cc_iterate for the loop body NCFVM/main.f90:53-86;
  * fresi may be NULL. */
 int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_iter, double* fres_raw,
                    double* fresi, int* done_iters);

@@ -66,7 +66,7 @@ int uns_host_read_flo_cc(const char* path, uns_params* p, char* grid, int gridle
 int uns_host_read_flo_nc(const char* path, uns_params* p, char* grid, int gridlen);
 
 /* CFL schedules: cfl_number (CCFVM/main.F90:148-168; `prev` is the value kept
- * when the ramp is over) and the fixed tanh ramp of NCFVM/main.f90:316. */
+ * when the ramp is over) and the fixed tanh ramp of NCFVM/main.f90:54. */
 double uns_host_cfl_cc(const uns_params* p, int iter, double prev);
 double uns_host_cfl_nc(const uns_params* p, int iter);
 
@@ -78,7 +78,7 @@ double uns_host_cfl_nc(const uns_params* p, int iter);
 int uns_host_save_flow(const char* path, const double* qc, int n);
 int uns_host_read_flow(const char* path, double* qc, int n);
 
-/* The reference main program (CCFVM/main.F90:4-170, NCFVM/main.f90:266-374)
+/* The reference main program (CCFVM/main.F90:4-170, NCFVM/main.f90:4-112)
  * on the GPU library: reads flo.inp, the geometry named there (relative to
  * flo.inp's directory), runs to MaxIter / MinRes and writes FLO.RES into
  * outdir.  mode 0 calls one entry point per reference subroutine each

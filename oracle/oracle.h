@@ -27,19 +27,19 @@ typedef struct oracle_nc oracle_nc;
 /* ------------------------------------------------------------ CCFVM */
 oracle_cc* oracle_cc_create(const uns_cc_mesh* m, const uns_params* p);
 void oracle_cc_free(oracle_cc* o);
-int oracle_cc_initialize(oracle_cc* o);                 /* solution.F90:231-297 */
+int oracle_cc_initialize(oracle_cc* o);                 /* solution.F90:18-84 */
 int oracle_cc_set_state(oracle_cc* o, const double* qc);/* [noc+nbf][4]          */
 int oracle_cc_con2prim(oracle_cc* o);                   /* main.F90:62-67        */
 int oracle_cc_avg_c2v(oracle_cc* o);                    /* average.F90:1-39      */
 int oracle_cc_time_step(oracle_cc* o, double cfl, double* dtglobal); /* timestep.F90:28-107 */
-int oracle_cc_save_old(oracle_cc* o);                   /* solution.F90:331-345  */
+int oracle_cc_save_old(oracle_cc* o);                   /* solution.F90:118-132  */
 int oracle_cc_gradient(oracle_cc* o);                   /* gradient.F90 (+limit) */
 int oracle_cc_limit(oracle_cc* o);                      /* limiter.F90:3-17,123-296 */
 int oracle_cc_fvresidual(oracle_cc* o);                 /* fvresidual.F90:4-187  */
 int oracle_cc_rk_stage(oracle_cc* o, int irk);          /* main.F90:90-101       */
 int oracle_cc_lusgs(oracle_cc* o);                      /* lusgs.F90:207-379     */
 int oracle_cc_check_positivity(oracle_cc* o, int* bad); /* main.F90:358-414      */
-int oracle_cc_residue(oracle_cc* o, double* fres_raw);  /* solution.F90:349-393  */
+int oracle_cc_residue(oracle_cc* o, double* fres_raw);  /* solution.F90:136-180  */
 int oracle_cc_forces(oracle_cc* o, double* fx1, double* fy1);
 /* One full iteration of main.F90:57-117 (cfl given). */
 int oracle_cc_iteration(oracle_cc* o, double cfl, double* fres_raw);
@@ -75,7 +75,7 @@ int oracle_nc_initialize(oracle_nc* o);                 /* NCFVM/common.f90:19-5
 int oracle_nc_set_state(oracle_nc* o, const double* qc);
 int oracle_nc_save_old(oracle_nc* o);                   /* common.f90:88-104      */
 int oracle_nc_fvresidual(oracle_nc* o, double cfl);     /* fvresidual.f90:4-85    */
-int oracle_nc_rk_stage(oracle_nc* o, int irk);          /* main.f90:321-342       */
+int oracle_nc_rk_stage(oracle_nc* o, int irk);          /* main.f90:59-80       */
 int oracle_nc_lusgs(oracle_nc* o, double cfl);          /* lusgs.f90:4-157        */
 int oracle_nc_residue(oracle_nc* o, double* fres_raw, double* fresi, int* iresi); /* common.f90:108-154 */
 int oracle_nc_iteration(oracle_nc* o, double cfl, double* fres_raw, double* fresi);

@@ -5,7 +5,7 @@
 //
 // The HEAD side of the merge conflict in NCFVM/fvresidual.f90:11-17 is taken
 // (Gradient_LSQR).  AUSM+-up has no compiled NCFVM reference
-// (NCFVM/ausm_up_flux.f90 is not in NCFVM/makefile:459 and references fields
+// (NCFVM/ausm_up_flux.f90 is not in NCFVM/makefile:30-31 and references fields
 // that do not exist); it is restated from the CCFVM formulation
 // (CCFVM/ausm_up_flux.F90:2-162) on the dual face, scaled by the dual-face
 // length, with the Roe-averaged spectral radius of NCFVM/vanleer_flux.f90.
@@ -130,7 +130,7 @@ void limiter_barth(NC& s) {
     }
 }
 
-// Roe-averaged spectral radius accumulation (vanleer_flux.f90:417-430).
+// Roe-averaged spectral radius accumulation (vanleer_flux.f90:102-115).
 void edge_lambda(NC& s, int ie, int c1, int c2, double rL, double uL, double vL, double HL,
                  double rR, double uR, double vR, double HR) {
     double nx = s.fnx[ie], ny = s.fny[ie], area = s.farea[ie];

@@ -62,7 +62,7 @@ def test_cc_freestream_preserved_in_interior(cc, flux):
 
 
 def test_cc_ausm_unit_area_quirk(cc):
-    """CCFVM's AUSM+-up scales by |n| of the unit normal (ausm_up_flux.F90:372),
+    """CCFVM's AUSM+-up scales by |n| of the unit normal (ausm_up_flux.F90:38),
     not the face length, so a closed cell does NOT preserve freestream."""
     res = _first_residual(cc, "ausm")
     far = ~boundary_layers(cc.arrays, 3)
@@ -94,7 +94,7 @@ def test_cc_gradients_exact_for_linear_fields(cc, grad):
     exact = np.broadcast_to(g, got.shape)
     if grad == "gg":
         # the boundary term of Gradient_GG has the opposite sign
-        # (CCFVM/gradient.F90:426-427), so only interior cells are exact
+        # (CCFVM/gradient.F90:135-136), so only interior cells are exact
         mask = ~boundary_layers(m, 1)
     else:
         mask = np.ones(m["noc"], bool)

@@ -396,7 +396,7 @@ int write_geometry_nc(const std::string& path, const RawNC& m, std::string& err)
 // ------------------------------------------------------- CC geometric
 namespace {
 
-// dotprod (CCFVM/solution.F90:576-597): cosine between the unit normal
+// dotprod (CCFVM/solution.F90:363-384): cosine between the unit normal
 // (dy,-dx)/ds of p1->p2 and the unit vector from p1 to (xc,yc).
 double dotprod(const std::vector<double>& px, const std::vector<double>& py, int n1, int n2, double xc, double yc) {
     double x1 = px[n1], y1 = py[n1], x2 = px[n2], y2 = py[n2];

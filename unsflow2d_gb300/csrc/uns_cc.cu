@@ -13,9 +13,11 @@
 //   * cell kernels fuse what the reference runs as separate cell loops
 //     (con2prim + save_old + the limiter's global min/max; spectral radius
 //     gather + dt + gradient + limiter; residual gather + RK stage + norm);
-//   * LU-SGS forward/backward sweeps are level-scheduled on the cell DAG of
-//     the reference ordering inside one cooperative launch with a bounded
-//     grid barrier, which reproduces the sequential sweep exactly;
+//   * LU-SGS forward/backward sweeps run as a list-scheduled dataflow sweep
+//     over the cell DAG of the reference ordering inside one cooperative
+//     launch: each warp works through its own list of (cell, pass) items and
+//     waits (bounded) on the published records of the items it depends on,
+//     which reproduces the sequential sweep exactly;
 //   * one iteration of the main loop is captured once as a CUDA graph and
 //     replayed; iteration number, CFL schedule and the convergence stop live
 //     in device memory.
@@ -72,7 +74,7 @@ __device__ __forceinline__ unsigned long long grp_max_u64(unsigned grp, unsigned
 }
 
 // ---------------------------------------------------------------- kernels
-// con2prim (main.F90:62-67) + save_old (solution.F90:331-345) + the global
+// con2prim (main.F90:62-67) + save_old (solution.F90:118-132) + the global
 // min/max of every cell's primitives incl. ghosts (limiter.F90:146-149) +
 // the positivity check of main.F90:384-411, fused over one pass of the cells.
 enum { BEGIN_PRIM = 1, BEGIN_OLD = 2, BEGIN_MINMAX = 4, BEGIN_POS = 8 };
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(kBlock) k_begin(CCView v, int flags) {
     }
 }
 
-// avg_c2v vertex part (average.F90:263-281): pseudo-Laplacian weighted mean.
+// avg_c2v vertex part (average.F90:11-29): pseudo-Laplacian weighted mean.
 __global__ void __launch_bounds__(512) k_vertex_avg(CCView v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nop || stopped(v, vert_inst(v, i))) return;
@@ -212,8 +214,8 @@ __global__ void __launch_bounds__(512) k_vertex_avg(CCView v) {
     v.ppT[i] = c4 / wt;
 }
 
-// avg_c2v face part (average.F90:284-288) + spectral02 face radius
-// (timestep.F90:399-423).
+// avg_c2v face part (average.F90:31-36) + spectral02 face radius
+// (timestep.F90:77-104).
 __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(kBlock) k_face_prim_spec(CCView v) {
     v.fla[f] = ll;
 }
 
-// Diamond-path face gradient (gradient.F90:474-556, gradtrixy :572-612).
+// Diamond-path face gradient (gradient.F90:183-261, gradtrixy :281-321).
 __device__ __forceinline__ bool gradtri(const double* pr0, const double* pr1, const double* pr2, double x0, double y0,
                                         double x1, double y1, double x2, double y2, double gxo[5], double gyo[5],
                                         double& tarea) {
@@ -314,8 +316,8 @@ __device__ __forceinline__ void d4get(const double4& q, double o[4]) { o[0] = q.
 __device__ __forceinline__ double4 d4(const double o[4]) { return make_double4(o[0], o[1], o[2], o[3]); }
 
 // Per-cell gather over the index-sorted face list: spectral radius + dt
-// (timestep.F90:364-371, 424-425), the cell gradient (Gradient_GG
-// gradient.F90:399-443, Gradient_GG_FC :511-564, Gradient_LSQR :308-377) and
+// (timestep.F90:40-49, 101-103), the cell gradient (Gradient_GG
+// gradient.F90:95-156, Gradient_GG_FC :159-323, Gradient_LSQR :2-93) and
 // limiter_VKN1 (limiter.F90:146-279).  Face order is the reference's loop
 // order (interior faces, then boundary faces).
 // CG_DIAG: also the LU-SGS diagonal and its reciprocal (with CG_DT; only an
@@ -847,7 +849,7 @@ __global__ void __launch_bounds__(512, std::is_same<R, float>::value ? 2 : 1) k_
     }
 }
 
-// Sutherland viscosity of every interior cell (viscous_flux.F90:478-480,585-597).
+// Sutherland viscosity of every interior cell (viscous_flux.F90:20-22,127-141).
 __global__ void __launch_bounds__(kBlock) k_cell_mul(CCView v) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
@@ -861,7 +863,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_mul(CCView v) {
     v.mul[i] = (num / den) * pow(P.t, 1.5);
 }
 
-// Laminar viscous face flux (viscous_flux.F90:488-534), stored as flux*area.
+// Laminar viscous face flux (viscous_flux.F90:30-76), stored as flux*area.
 __global__ void __launch_bounds__(kBlock) k_face_visc(CCView v) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
@@ -1186,7 +1188,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_rk23(CCView v) {
     }
 }
 
-// One Jacobi sweep of cirs (ImpResiSmoothening.F90:626-643).
+// One Jacobi sweep of cirs (ImpResiSmoothening.F90:27-44).
 __global__ void __launch_bounds__(kBlock) k_cirs(CCView v, const double4* src, double4* dst, double eps) {
     if (stopped(v)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1241,7 +1243,7 @@ __global__ void __launch_bounds__(kBlock) k_res_partial(CCView v) {
 
 // Deterministic final sum of the block partials; in the graph path it also
 // records the history, the first-iteration normalisation and the stop flag
-// (solution.F90:365-379, main.F90:57).
+// (solution.F90:159-166, main.F90:57).
 __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, double* out) {
     const int inst = blockIdx.x;  // one block per instance
     if (stopped(v, inst)) return;
@@ -1298,7 +1300,7 @@ __global__ void k_reset_minmax(CCView v) {
 }
 
 // Sequential wall-force sums in face order (fvresidual.F90:99-100 then
-// viscous_flux.F90:530-533).
+// viscous_flux.F90:73-74).
 __global__ void k_forces(CCView v, double* out) {
     double fx = 0.0, fy = 0.0;
 #pragma unroll 8
@@ -1372,9 +1374,8 @@ __global__ void k_unpack_f32(CCView v) {
     v.phi[i] = make_double4(c.x, c.y, c.z, c.w);
 }
 
-// lusgs2 sweeps (lusgs.F90:245-318), one level of the dependency DAG per
-// grid-barrier phase.  The per-cell neighbour sum keeps the reference c2f
-// order, so the result equals the sequential sweep.
+// lusgs2 sweep pieces (lusgs.F90:245-318).  The per-cell neighbour sum keeps
+// the reference c2f order, so the result equals the sequential sweep.
 __device__ __forceinline__ void normal_flux_d(const Gas& g, const double4& qo, const double4& dq, double nx, double ny,
                                               double area, double out[4]) {
     Prim P = con2prim(g, qo.x, qo.y, qo.z, qo.w);
@@ -2040,7 +2041,7 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
 
 }  // namespace uns
 
-// Gas constants of one case: math + initialize (CCFVM/read_input.F90:217-262),
+// Gas constants of one case: math + initialize (CCFVM/solution.F90:4-84),
 // and its freestream conserved state.
 static Gas make_gas(const uns_params* p, double4* qinf) {
     Gas g;
@@ -2140,7 +2141,7 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
         cf[pos[m->fin[f]]++] = f;
         if (m->fout[f] < noc) cf[pos[m->fout[f]]++] = f | SIDE_BIT;
     }
-    // LSQ weights (gradient.F90:308-369), host-side in the reference's
+    // LSQ weights (gradient.F90:27-44, 72-78), host-side in the reference's
     // expression order (-ffp-contract=off translation unit).
     std::vector<double4> lsw(nof);
     for (int f = 0; f < nof; ++f) {

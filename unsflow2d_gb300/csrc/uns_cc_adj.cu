@@ -171,7 +171,7 @@ __global__ void k_rec_conv(CCView v, AdjView a, int s) {
 }
 
 // d mul / d qc of the Sutherland viscosity at the current stage state
-// (viscous_flux.F90:478-480, 585-597), as k_cell_mul evaluates it.
+// (viscous_flux.F90:20-22, 127-141), as k_cell_mul evaluates it.
 __global__ void k_rec_mul(CCView v, AdjView a, int s) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.noc) return;
@@ -188,7 +188,7 @@ __global__ void k_rec_mul(CCView v, AdjView a, int s) {
     ((double4*)a.DM)[(size_t)s * v.noc + i] = make_double4(d[0], d[1], d[2], d[3]);
 }
 
-// Inputs of the viscous face flux (viscous_flux.F90:488-534) after k_face_visc.
+// Inputs of the viscous face flux (viscous_flux.F90:30-76) after k_face_visc.
 __global__ void k_rec_visc(CCView v, AdjView a, int s) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= v.nof) return;
@@ -285,7 +285,7 @@ __global__ void k_adj_mul(CCView v, AdjView a, int s) {
     a.qc[i] = add(a.qc[i], scl(m, a.DM[(size_t)s * v.noc + i]));
 }
 
-// Weights of the diamond-path face gradient (gradient.F90:474-556): the
+// Weights of the diamond-path face gradient (gradient.F90:183-261): the
 // derivative of (gx, gy) of the face with respect to the value at each of its
 // four points, per unit gradient adjoint (gb_x, gb_y), as
 // w = 0.5 (edge terms of the two edges at the point) / (a1 + a2).

@@ -138,7 +138,7 @@ int uns_cc_find_cl_cd(uns_cc_handle* h, double xref, double yref, double* coef, 
     if ((rc = uns_cc_forces(h, &fx1, &fy1))) return rc;
     const double fx = r[0], fy = r[1];
     const int n = (int)r[3];
-    // cos / sin of the angle of attack are u_inf, v_inf (read_input.F90:237-262)
+    // cos / sin of the angle of attack are u_inf, v_inf (solution.F90:35-36)
     coef[0] = (fy * g.u_inf - fx * g.v_inf) / dyna;
     coef[1] = (fy * g.v_inf + fx * g.u_inf) / dyna;
     coef[2] = r[2];

@@ -11,7 +11,7 @@
 //   k_nc_node_res  node gather over v2f in edge-index order (the
 //                  reference's accumulation order), time_step2, optionally
 //                  fused with the RK3 stage and the residual-norm partials.
-// LU-SGS (lusgs.f90:4-157) runs level-scheduled in one cooperative launch.
+// LU-SGS (lusgs.f90:4-157) runs as a list-scheduled dataflow sweep in one cooperative launch.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
             const float f1[4] = {pa.x, pa.y, pa.z, pa.w}, f2[4] = {pb.x, pb.y, pb.z, pb.w};
             V4<float> L, Rt, F;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {  // fvresidual.f90:576-590
+            for (int k = 0; k < 4; ++k) {  // fvresidual.f90:41-54
                 float g = a[k] * d.x + b[k] * d.y;
                 L[k] = q1[k] + 0.5f * g * f1[k];
                 g = c[k] * d.x + e[k] * d.y;
@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
             if (v.g.flux == UNS_FLUX_AUSM) ausm_core<float>(G, G1, (float)n.x, (float)n.y, (float)v.g.mref, L, Rt, F, hl, hr);
             else vanleer_core<float>(G, G1, (float)n.x, (float)n.y, L, Rt, F, hl, hr);
             v.fF[f] = make_double4(F[0] * area, F[1] * area, F[2] * area, F[3] * area);
-            // Roe-averaged spectral radius (vanleer_flux.f90:417-430)
+            // Roe-averaged spectral radius (vanleer_flux.f90:102-115)
             const float RT = sqrtf(Rt[0] / L[0]);
             const float u = (L[1] + RT * Rt[1]) / (1.f + RT);
             const float vv = (L[2] + RT * Rt[2]) / (1.f + RT);
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
     g4(v.phi[p.x], f1); g4(v.phi[p.y], f2);
     V4<R> L, Rt, F;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {  // fvresidual.f90:576-590
+    for (int k = 0; k < 4; ++k) {  // fvresidual.f90:41-54
         double g = a[k] * d0 + b[k] * d1;
         L[k] = (R)(q1[k] + 0.5 * g * f1[k]);
         g = c[k] * d0 + d[k] * d1;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
     if (v.g.flux == UNS_FLUX_AUSM) ausm_core<R>(G, G1, (R)n.x, (R)n.y, (R)v.g.mref, L, Rt, F, hl, hr);
     else vanleer_core<R>(G, G1, (R)n.x, (R)n.y, L, Rt, F, hl, hr);
     v.fF[f] = make_double4((double)F[0] * area, (double)F[1] * area, (double)F[2] * area, (double)F[3] * area);
-    // Roe-averaged spectral radius (vanleer_flux.f90:417-430).
+    // Roe-averaged spectral radius (vanleer_flux.f90:102-115).
     double rL = (double)L[0], rR = (double)Rt[0];
     double RT = sqrt(rR / rL);
     double u = ((double)L[1] + RT * (double)Rt[1]) / (1.0 + RT);
@@ -363,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
     if (bc != 1001 && bc != 2001) return;
     int s = v.fslot[f];
     const Gas& g = v.g;
-    if (bc == 1001) {  // solid_flux (solid_flux.f90:460-475)
+    if (bc == 1001) {  // solid_flux (solid_flux.f90:26-41)
         double pa = 0.75 * q1[3] + 0.25 * q2[3];
         double pb = 0.25 * q1[3] + 0.75 * q2[3];
         double nx = 0.5 * (X2.y - X1.y);
@@ -402,8 +402,8 @@ __global__ void __launch_bounds__(kBlock) k_nc_edge(NCView v) {
 }
 
 // Node gather in edge-index order (the reference's accumulation order):
-// residual, spectral radius, time_step2 (timestep.f90:173-191), optional RK3
-// stage (main.f90:325-334) and residual-norm block partials
+// residual, spectral radius, time_step2 (timestep.f90:16-34), optional RK3
+// stage (main.f90:63-72) and residual-norm block partials
 // (common.f90:130-141: sum, max with first-index tie-break).
 __global__ void __launch_bounds__(kBlock) k_nc_node_res(NCView v, double cfl_in, int irk, int partial) {
     if (stopped(v)) return;
@@ -597,7 +597,7 @@ constexpr int kSweepBlock = 128;
 // One sweep block per SM: one warp per SM sub-partition, so concurrently
 // active items never share an FP64 unit.
 constexpr int kSweepBlocksPerSM = 1;
-constexpr double kOmega = 1.5;  // lusgs.f90:28
+constexpr double kOmega = 1.5;  // lusgs.f90:26
 
 // Per LU-SGS call: everything a sweep item needs from an edge that does not
 // change during the sweeps, laid out contiguously in schedule order so a

@@ -59,7 +59,7 @@ __device__ __forceinline__ V4<R> prim2con(R gamma, const V4<R>& pr) {
     return c;
 }
 
-// Mach-number polynomials (CCFVM/solution.F90:478-572)
+// Mach-number polynomials (CCFVM/solution.F90:265-359)
 template <class R> __device__ __forceinline__ R m1p(R m) { return R(0.5) * (m + fabs(m)); }
 template <class R> __device__ __forceinline__ R m1m(R m) { return R(0.5) * (m - fabs(m)); }
 template <class R> __device__ __forceinline__ R m2p(R m) { return R(0.25) * (m + R(1)) * (m + R(1)); }
@@ -166,7 +166,7 @@ __device__ __forceinline__ void rusanov_flux(R G, R G1, R nx, R ny, R area, V4<R
 }
 
 // van Leer flux-vector splitting per unit face length
-// (CCFVM/vanleer_flux.F90:1-101, NCFVM/vanleer_flux.f90:342-415).
+// (CCFVM/vanleer_flux.F90:1-101, NCFVM/vanleer_flux.f90:2-118).
 template <class R>
 __device__ __forceinline__ void vanleer_core(R G, R G1, R nx, R ny, const V4<R>& ql, const V4<R>& qr, V4<R>& flux,
                                              R& hl_o, R& hr_o) {

@@ -1,6 +1,6 @@
 // uns_sched.hpp -- host-side warp schedule of the LU-SGS sweeps.
 //
-// The forward sweep of lusgs (CCFVM/lusgs.F90:245-280, NCFVM/lusgs.f90:48-86)
+// The forward sweep of lusgs2 (CCFVM/lusgs.F90:245-280, NCFVM/lusgs.f90:48-86)
 // updates entity i from its already-updated neighbours j < i; the backward
 // sweep (CCFVM/lusgs.F90:283-318, NCFVM/lusgs.f90:88-124) from j > i and from
 // i's own forward value.  Each (entity, pass) is one item of a DAG whose

@@ -118,7 +118,7 @@ def read_flo_inp(path: str, kind: str = "cc") -> tuple[abi.Params, str]:
 
 
 def cfl_schedule(p: abi.Params, first: int, n: int, kind: str = "cc", prev: float = 0.0) -> np.ndarray:
-    """CFL of iterations first..first+n-1 (CCFVM/main.F90:148-168, NCFVM/main.f90:316)."""
+    """CFL of iterations first..first+n-1 (CCFVM/main.F90:148-168, NCFVM/main.f90:54)."""
     lib = abi.host_lib()
     out = np.zeros(n)
     c = prev

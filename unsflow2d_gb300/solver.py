@@ -253,7 +253,7 @@ class NCSolver(_Solver):
         return f.value, fi.value, ii.value
 
     def iteration(self, cfl: float) -> tuple[float, float, int]:
-        """One main-loop iteration (NCFVM/main.f90:315-347)."""
+        """One main-loop iteration (NCFVM/main.f90:53-86)."""
         self.save_old()
         if self.params.time_mode == abi.TIME["rk3"]:
             for irk in (1, 2, 3):
