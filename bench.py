@@ -491,6 +491,18 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
     achieved = nbytes / (ms / 1e3 / args.steps) / 1e9
     peak, peak_src = peaks()
     clocks = clk.summary()
+    # the face kernel of all cases: CUDA events around its launches (the
+    # phase profile of the packed handle, after the timed region)
+    face = None
+    if packed:
+        prof = batch.profile(float(params[0].cfl_max), reps=3)
+        fb = sum(algorithmic_bytes("cc", m.arrays, True, sides=True)["face_conv"] for m in meshes)
+        if prof.get("face_conv", 0.0) > 0:
+            gbs = fb / (prof["face_conv"] * 1e-3) / 1e9
+            face = {"kernel": "k_face_conv<float> (all cases, one launch)", "ms_per_launch": round(prof["face_conv"], 4),
+                    "alg_MB_per_launch": round(fb / 1e6, 2), "achieved": round(gbs, 1), "peak": peak,
+                    "unit": "GB/s", "frac": round(gbs / peak, 4),
+                    "phases_ms": {k: round(v, 4) for k, v in prof.items()}}
     if rank != 0:
         return None
     n = n_inst
@@ -512,7 +524,8 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": "whole batch iteration (all kernels of all instances)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "traffic": None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "face_kernel": face},
     }
 
 
@@ -670,7 +683,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
         "kernels": kernels,
     }
     if not args.no_cpu_baseline and args.gpus == 1:
-        out["cpu_baseline"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
+        out["cpu_baseline"], out["parity"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
     if accuracy is not None:
         out["accuracy_vs_fp64"] = accuracy
     if w.get("adjoint"):
@@ -680,26 +693,49 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     return out
 
 
-def cpu_baseline(w, m, p, budget_s=15.0) -> dict:
-    """The oracle (serial C++ restatement of the reference) on this host, one core."""
+def cpu_baseline(w, m, p, budget_s=15.0) -> tuple[dict, dict]:
+    """The oracle (serial C++ restatement of the reference) on this host, one
+    core; then the same iterations from freestream on a fresh GPU handle,
+    compared with the oracle's (the parity object of the bench line)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     from oracle import OracleCC, OracleNC
-    O = OracleNC if w["kind"] == "nc" else OracleCC
-    o = O(m, p)
+    from unsflow2d_gb300.solver import CCSolver, NCSolver
     kind = w["kind"]
+    O = OracleNC if kind == "nc" else OracleCC
+    o = O(m, p)
     c = cfl_list(p, kind, 1, 64)
+    first = lambda r: r[0] if isinstance(r, tuple) else r
     t0 = time.perf_counter()
-    o.iteration(c[0])
+    fo = [first(o.iteration(c[0]))]
     t1 = time.perf_counter() - t0
     n = max(1, min(63, int(budget_s / max(t1, 1e-6))))
     t0 = time.perf_counter()
     for k in range(n):
-        o.iteration(c[1 + k])
+        fo.append(first(o.iteration(c[1 + k])))
     dt = time.perf_counter() - t0
     units = units_of(w, m)
-    return {"value": round(units * n / dt / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+    base = {"value": round(units * n / dt / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
             "host_cores": os.cpu_count(),
             "sample": f"{n} iterations of the full {units}-unit mesh after 1 untimed ({dt:.1f} s, serial oracle)"}
+    g = (NCSolver if kind == "nc" else CCSolver)(m, p)
+    fg = np.asarray(first(g.iterate(c[:n + 1], first_iter=True)))
+    fo = np.asarray(fo)
+    qg, qo = g.get_state(), o.get_state()
+    rg, ro = g.get("res"), o.get("res")
+    nu = len(ro)
+    scale = np.asarray(o.get("la"))[:nu, None] * np.abs(qo[:nu]).max(axis=0)[None, :4]
+    parity = {"iterations": int(n + 1), "units": int(units), "from": "uniform freestream, fresh GPU handle",
+              "max_rel_state_err": float(np.max(np.abs(qg - qo)) / np.max(np.abs(qo))),
+              "max_res_err": float(np.max(np.abs(rg[:nu] - ro) / np.maximum(scale, 1e-300))),
+              "fres_max_rel_diff": float(np.max(np.abs(fg - fo) / np.abs(fo))),
+              "state_bit_identical": bool(np.array_equal(qg, qo)),
+              "criterion": "state 1e-12 of its max magnitude; residual 1e-12 of the flux scale lambda_i*max|q|",
+              "oracle": "serial C++ restatement of the reference (oracle/), same mesh and inputs"}
+    parity["pass"] = bool(parity["max_rel_state_err"] <= 1e-12 and parity["max_res_err"] <= 1e-12
+                          and parity["fres_max_rel_diff"] <= 1e-12)
+    g.close()
+    o.close()
+    return base, parity
 
 
 def run_reference(args, w) -> dict:
@@ -738,6 +774,45 @@ def run_reference(args, w) -> dict:
             "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# The other benchmark configurations, measured in the same default run after
+# the headline (one GPU): key -> workload.  "3_fp64" is configuration 3's mesh
+# in the plain FP64 form, the denominator of the mixed and batched speed-ups.
+CONFIG_RUNS = [("1", "cc_small"), ("3_fp64", "cc"), ("3", "cc_mixed"), ("4", "cc_batched"), ("5", "cc_adjoint")]
+SUMMARY_KEYS = ("value", "unit", "ms_per_step", "steps", "dtype", "gpu_launches", "clocks", "roofline",
+                "accuracy_vs_fp64", "adjoint", "time_to_1e-8")
+
+
+def run_configs(args, dist, rank, local_rank) -> dict:
+    """Configurations 1, 3, 4 and 5 (and configuration 3's mesh in plain FP64),
+    each timed like the headline: CUDA events on the library stream around
+    `--steps` graph-replayed iterations after the warm-up, clocks sampled
+    during the timed region.  No end-to-end leg and no CPU baseline here."""
+    import copy
+    out = {}
+    for key, name in CONFIG_RUNS:
+        a = copy.copy(args)
+        a.no_e2e, a.no_cpu_baseline = True, True
+        a.no_converge = name != "cc_small"  # configuration 1 is the time-to-drop mesh itself
+        w = dict(WORKLOADS[name])
+        r = (run_batched if w["kind"] == "cc_batch" else run_ours)(a, w, dist, rank, local_rank)
+        if r is None:
+            continue
+        d = {"workload": w["desc"], "units": r["config"]["units"]}
+        d.update({k: r[k] for k in SUMMARY_KEYS if k in r})
+        if "kernels" in r:
+            d["kernels_ms_per_iter"] = {k: v["ms_per_iter"] for k, v in r["kernels"].items()}
+        if r["config"].get("block_sizes"):
+            d["block_sizes"] = r["config"]["block_sizes"]
+        out[key] = d
+    plain = out.get("3_fp64", {}).get("value")
+    if plain:
+        for key in ("3", "4"):
+            if key in out:
+                out[key]["speedup_vs_plain_fp64"] = round(out[key]["value"] / plain, 3)
+                out[key]["plain_fp64_reference"] = "configuration 3's 2048x1024 mesh in the plain FP64 form (key 3_fp64)"
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -754,6 +829,8 @@ def main():
                     help="skip the mixed forms' FP64 comparison run (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default block sizes (profiling runs: no tuning launches before the captured ones)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other configurations that the default one-GPU run measures after the headline")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -769,6 +846,10 @@ def main():
         return 0
     dist = replicas.init("nccl")
     out = (run_batched if w["kind"] == "cc_batch" else run_ours)(args, w, dist, rank, local_rank)
+    if args.gpus == 1 and args.workload == "nc" and not args.mesh and not args.no_configs:
+        configs = run_configs(args, dist, rank, local_rank)
+        if out is not None:
+            out["configs"] = configs
     if out is not None:
         print(json.dumps(out))
     if dist is not None:

@@ -364,6 +364,16 @@ class CCPacked:
     def set_precision(self, precision: str) -> None:
         abi.check(self._lib.uns_cc_set_precision(self._h, abi.PREC[precision]), self._lib, "uns_cc_set_precision")
 
+    def profile(self, cfl: float, reps: int = 3) -> dict:
+        """Average device time [ms] of each phase of one iteration of all the
+        cases (uns_cc_profile; one CFL for every case)."""
+        n = 16
+        ms = np.zeros(n)
+        names = (C.c_char_p * n)()
+        abi.check(self._lib.uns_cc_profile(self._h, C.c_double(cfl), reps, _dp(ms), names, n), self._lib,
+                  "uns_cc_profile")
+        return {names[k].decode(): float(ms[k]) for k in range(n) if names[k] and names[k].decode()}
+
     def autotune(self, reps: int = 3) -> dict:
         """Block sizes of the face, vertex and cell-gradient kernels picked by
         timing them on the packed mesh (uns_cc_autotune)."""
