@@ -407,6 +407,16 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- runs
+def timed_steps(args, s_per_step: float) -> int:
+    """`--steps`, raised where needed so the timed region lasts at least
+    args.min_timed_s (the clock sampler's 200 ms period needs a few samples
+    inside it)."""
+    need = getattr(args, "min_timed_s", 0.0)
+    if need <= 0 or s_per_step <= 0:
+        return args.steps
+    return max(args.steps, int(math.ceil(need / s_per_step)))
+
+
 def build_mesh(w):
     cls = mesh.NCMesh if w["kind"] == "nc" else mesh.CCMesh
     return cls.airfoil(w["ni"], w["nj"], 0.12, 20.0, w["dwall"])
@@ -467,7 +477,10 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
 
     step(1)
     blocks = batch.autotune() if packed and not args.no_autotune else None  # launch geometry picked on the packed mesh
-    step(max(args.warmup - 1, 2))
+    t_w = time.perf_counter()
+    nw = max(args.warmup - 1, 2)
+    step(nw)
+    args.steps = timed_steps(args, (time.perf_counter() - t_w) / nw)
     stream = torch.cuda.ExternalStream(batch.stream(), device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     replicas.barrier(dist, local_rank)
@@ -561,7 +574,10 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     # first step, before the rest of the warm-up (which re-captures the step)
     iterate(1)
     blocks = solver.autotune() if kind == "cc" and not args.no_autotune else None
-    iterate(max(args.warmup - 1, 2))
+    t_w = time.perf_counter()
+    nw = max(args.warmup - 1, 2)
+    iterate(nw)
+    args.steps = timed_steps(args, (time.perf_counter() - t_w) / nw)
     stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     replicas.barrier(dist, local_rank)
@@ -792,6 +808,7 @@ def run_configs(args, dist, rank, local_rank) -> dict:
     for key, name in CONFIG_RUNS:
         a = copy.copy(args)
         a.no_e2e, a.no_cpu_baseline = True, True
+        a.min_timed_s = 0.6
         a.no_converge = name != "cc_small"  # configuration 1 is the time-to-drop mesh itself
         w = dict(WORKLOADS[name])
         r = (run_batched if w["kind"] == "cc_batch" else run_ours)(a, w, dist, rank, local_rank)

@@ -1,8 +1,8 @@
-// fp64_issue.cu -- GB300 arithmetic and memory latencies that bound the
+// bench_fp64_issue.cu -- GB300 arithmetic and memory latencies that bound the
 // LU-SGS sweeps and the FP64 face kernels (not part of the library).
 //
 //   nvcc -gencode arch=compute_103a,code=sm_103a -O3 --fmad=false \
-//        -o fp64_issue unsflow2d_gb300/microbench/fp64_issue.cu && ./fp64_issue
+//        -o fp64_issue bench_fp64_issue.cu && ./fp64_issue
 //
 // Prints, for FP64 add / mul / fma / divide, FP32 add / divide and an
 // FP64 -> FP32 conversion, the

@@ -79,7 +79,8 @@ int uns_host_save_flow(const char* path, const double* qc, int n);
 int uns_host_read_flow(const char* path, double* qc, int n);
 
 /* The reference main program (CCFVM/main.F90:4-170, NCFVM/main.f90:4-112)
- * on the GPU library: reads flo.inp, the geometry named there (relative to
+ * on the GPU library; exported by libunsflow_driver.so (every other function
+ * here by libunsflow_host.so, which needs no GPU library): reads flo.inp, the geometry named there (relative to
  * flo.inp's directory), runs to MaxIter / MinRes and writes FLO.RES into
  * outdir.  mode 0 calls one entry point per reference subroutine each
  * iteration; mode 1 uses the graph-replayed uns_*_iterate fast path.

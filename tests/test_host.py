@@ -214,13 +214,32 @@ def _declared(header: Path) -> set[str]:
     return set(re.findall(r"^\s*(?:const\s+)?\w+[\s\*]+(uns_\w+)\s*\(", text, flags=re.M))
 
 
+DRIVER = {"uns_host_cc_main", "uns_host_nc_main"}  # libunsflow_driver.so
+
+
 def test_c_abi_exports_every_declared_symbol():
-    gpu, host = abi.gpu_lib(), abi.host_lib()
+    gpu, host, drv = abi.gpu_lib(), abi.host_lib(), abi.driver_lib()
     for header, lib in (("unsflow_gpu.h", gpu), ("unsflow_host.h", host)):
         names = _declared(ROOT / "include" / header)
         assert len(names) > 10
-        missing = [n for n in names if not hasattr(lib, n)]
+        missing = [n for n in names if not hasattr(drv if n in DRIVER else lib, n)]
         assert not missing, (header, missing)
+
+
+def test_host_library_needs_no_gpu_library():
+    """The mesh / flo.inp / CFL library loads and works on its own (the CPU
+    reference arm of the benchmark uses it without the GPU library)."""
+    import subprocess
+    import sys
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from unsflow2d_gb300 import abi, mesh\n"
+            "m = mesh.CCMesh.airfoil(8, 4)\n"
+            "assert m.arrays['noc'] == 64\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libunsflow_host.so' in maps and 'libunsflow_gpu.so' not in maps, 'gpu library mapped'\n"
+            % str(ROOT))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
 
 
 def test_gpu_create_validates_mesh_on_the_host(cc):

@@ -234,7 +234,7 @@ def gpu_lib() -> C.CDLL:
 
 
 def host_lib() -> C.CDLL:
-    gpu_lib()
+    """libunsflow_host.so: meshes, flo.inp, CFL schedules, FLO.DAT (no GPU)."""
     lib = _load("unsflow_host")
     if not getattr(lib, "_typed", False):
         vp, i32, dp = C.c_void_p, C.c_int, C.c_double
@@ -256,13 +256,25 @@ def host_lib() -> C.CDLL:
             "uns_host_read_flo_nc": ([C.c_char_p, C.POINTER(Params), C.c_char_p, i32], i32),
             "uns_host_cfl_cc": ([C.POINTER(Params), i32, dp], dp),
             "uns_host_cfl_nc": ([C.POINTER(Params), i32], dp),
-            "uns_host_cc_main": ([C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_int), _D], i32),
-            "uns_host_nc_main": ([C.c_char_p, C.c_char_p, i32, C.POINTER(C.c_int), _D], i32),
             "uns_host_save_flow": ([C.c_char_p, _D, i32], i32), "uns_host_read_flow": ([C.c_char_p, _D, i32], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)
             f.argtypes, f.restype = args, res
+        lib._typed = True
+        lib._kind = "host"
+    return lib
+
+
+def driver_lib() -> C.CDLL:
+    """libunsflow_driver.so: the main programs on the GPU library."""
+    gpu_lib()
+    host_lib()
+    lib = _load("unsflow_driver")
+    if not getattr(lib, "_typed", False):
+        for fn in ("uns_host_cc_main", "uns_host_nc_main"):
+            f = getattr(lib, fn)
+            f.argtypes, f.restype = [C.c_char_p, C.c_char_p, C.c_int, C.POINTER(C.c_int), _D], C.c_int
         lib._typed = True
         lib._kind = "host"
     return lib

@@ -3,10 +3,12 @@
     libunsflow_gpu.so   CUDA kernels + the drop-in C-ABI (include/unsflow_gpu.h),
                         sm_103a only, static CUDA runtime.
     libunsflow_host.so  caller side: geometry.inp / flo.inp, geometric
-                        preprocessing, airfoil O-mesh generator, main-loop driver
-                        (include/unsflow_host.h).
+                        preprocessing, airfoil O-mesh generator, CFL schedules,
+                        FLO.DAT I/O (include/unsflow_host.h); no GPU dependency.
+    libunsflow_driver.so  the main programs (uns_host_*_main in unsflow_host.h)
+                        on the two libraries above.
 
-Both land in unsflow2d_gb300/lib/.  Translation units compile in parallel; host
+All three land in unsflow2d_gb300/lib/.  Translation units compile in parallel; host
 code is built with -ffp-contract=off so x86 and Arm hosts round identically.
 """
 from __future__ import annotations
@@ -37,6 +39,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
 
 GPU_SOURCES = ["uns_api.cu", "uns_cc.cu", "uns_cc_adj.cu", "uns_cc_post.cu", "uns_nc.cu", "uns_noalloc.cu"]
 HOST_SOURCES = ["host/host_mesh.cpp", "host/host_api.cpp"]
+DRIVER_SOURCES = ["host/host_main.cpp"]
 
 
 def nvcc() -> str:
@@ -67,15 +70,17 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     OBJ.mkdir(exist_ok=True)
     gpu_so = LIB / "libunsflow_gpu.so"
     host_so = LIB / "libunsflow_host.so"
+    driver_so = LIB / "libunsflow_driver.so"
     deps = _deps()
-    if not force and _newer(gpu_so, deps) and _newer(host_so, deps):
-        return {"gpu": gpu_so, "host": host_so}
+    out = {"gpu": gpu_so, "host": host_so, "driver": driver_so}
+    if not force and all(_newer(f, deps) for f in out.values()):
+        return out
     nv = nvcc()
     jobs = []
     for src in GPU_SOURCES:
         o = OBJ / (Path(src).stem + ".o")
         jobs.append([nv, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(o)])
-    for src in HOST_SOURCES:
+    for src in HOST_SOURCES + DRIVER_SOURCES:
         o = OBJ / (Path(src).stem + ".o")
         jobs.append(["g++", *CXX_FLAGS, "-c", str(CSRC / src), "-o", str(o)])
     with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
@@ -84,10 +89,13 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     gpu_objs = [str(OBJ / (Path(s).stem + ".o")) for s in GPU_SOURCES]
     _run([nv, *ARCH, "-shared", "-Xcompiler", "-fPIC", *gpu_objs, "-o", str(gpu_so)])
     host_objs = [str(OBJ / (Path(s).stem + ".o")) for s in HOST_SOURCES]
-    _run(["g++", "-shared", *host_objs, "-L", str(LIB), "-lunsflow_gpu", "-Wl,-rpath,$ORIGIN", "-o", str(host_so)])
+    _run(["g++", "-shared", *host_objs, "-o", str(host_so)])
+    drv_objs = [str(OBJ / (Path(s).stem + ".o")) for s in DRIVER_SOURCES]
+    _run(["g++", "-shared", *drv_objs, "-L", str(LIB), "-lunsflow_host", "-lunsflow_gpu", "-Wl,-rpath,$ORIGIN",
+          "-o", str(driver_so)])
     if verbose:
-        print(f"built {gpu_so} and {host_so}")
-    return {"gpu": gpu_so, "host": host_so}
+        print(f"built {gpu_so}, {host_so} and {driver_so}")
+    return out
 
 
 def ptxas_report() -> str:

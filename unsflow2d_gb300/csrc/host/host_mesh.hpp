@@ -105,4 +105,12 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err);
 int read_flo_inp_cc(const std::string& path, uns_params& p, std::string& gridfile, std::string& err);
 int read_flo_inp_nc(const std::string& path, uns_params& p, std::string& gridfile, std::string& err);
 
+// Shared by libunsflow_host.so and libunsflow_driver.so: the calling thread's
+// message for uns_host_last_error (returns code), the Fortran Ew.d edit
+// descriptor, and path helpers.
+int fail(int code, const std::string& msg);
+std::string fort_e(double x, int w, int d);
+std::string dir_of(const std::string& p);
+std::string join(const std::string& d, const std::string& f);
+
 }  // namespace unshost

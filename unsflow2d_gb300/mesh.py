@@ -133,7 +133,7 @@ def cfl_schedule(p: abi.Params, first: int, n: int, kind: str = "cc", prev: floa
 
 def run_main(flo_inp: str, outdir: str, kind: str = "cc", mode: int = 1) -> tuple[int, float]:
     """Reference main program on the GPU library; writes outdir/FLO.RES."""
-    lib = abi.host_lib()
+    lib = abi.driver_lib()
     it = C.c_int()
     fr = C.c_double()
     fn = lib.uns_host_cc_main if kind == "cc" else lib.uns_host_nc_main
