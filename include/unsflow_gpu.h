@@ -28,9 +28,12 @@ const char* uns_version(void);
 /* Test hooks (no reference counterpart), n host values each:
  * out[i] = a[i] / b[i] by the kernels' division through the reciprocal
  * (must equal IEEE division), and lt[i] = whether a[i]/b[i] < c[i]/d[i]
- * by the kernels' exact ratio comparison (-1 where it does not apply). */
+ * by the kernels' exact ratio comparison (-1 where it does not apply), and
+ * out[i] = 0.5 * a[i] by the kernels' integer halving (must equal the FP64
+ * multiply). */
 int uns_selftest_div(const double* a, const double* b, double* out, int n);
 int uns_selftest_ratio(const double* a, const double* b, const double* c, const double* d, int* lt, int n);
+int uns_selftest_half(const double* a, double* out, int n);
 
 /* ============================================================ CCFVM =====*/
 typedef struct uns_cc_handle uns_cc_handle;
@@ -237,6 +240,18 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
  * sizes: faces, vertices, cell gradient. */
 int uns_cc_autotune(uns_cc_handle* h, int reps, int* blocks);
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
+/* Bound of every wait in the handle's LU-SGS sweeps, in device clock cycles
+ * (default 4e9, about 2 s); a sweep whose wait runs out returns
+ * UNS_ERR_TIMEOUT with the context intact.  No reference counterpart (the
+ * reference sweeps are sequential and never wait). */
+int uns_cc_set_wait_limit(uns_cc_handle* h, long long cycles);
+int uns_nc_set_wait_limit(uns_nc_handle* h, long long cycles);
+/* Test hook, no reference counterpart: the sweep item of cell / node
+ * `entity` in sweep `pass` (0 forward, 1 backward) publishes no record, so
+ * the items that depend on it wait until the wait limit runs out; entity -1
+ * clears it. */
+int uns_cc_debug_unpublish(uns_cc_handle* h, int entity, int pass);
+int uns_nc_debug_unpublish(uns_nc_handle* h, int entity, int pass);
 
 /* ===================================================== no-allocation ====*/
 /* Largest ncells uns_residue_rms_noalloc accepts: its scratch is a static

@@ -210,6 +210,8 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_autotune": ([vp, i32, C.POINTER(C.c_int)], i32),
             "uns_nc_profile": ([vp, C.c_double, i32, dp, C.POINTER(C.c_char_p), i32], i32),
             "uns_residue_rms_noalloc": ([vp, i32, dp, vp], i32),
+            "uns_cc_set_wait_limit": ([vp, C.c_longlong], i32), "uns_nc_set_wait_limit": ([vp, C.c_longlong], i32),
+            "uns_cc_debug_unpublish": ([vp, i32, i32], i32), "uns_nc_debug_unpublish": ([vp, i32, i32], i32),
             "uns_cc_batch_create": ([C.POINTER(C.c_void_p), i32, pp], i32), "uns_cc_batch_destroy": ([vp], i32),
             "uns_cc_batch_stream": ([vp], vp),
             "uns_cc_batch_iterate": ([vp, i32, dp, i32, dp, C.POINTER(C.c_int)], i32),

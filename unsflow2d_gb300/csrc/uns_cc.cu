@@ -1271,6 +1271,7 @@ __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, doub
         const int nc = v.ninst ? v.ncell[inst] : v.noc;
         double fres = sqrt(s[0] / (double)nc / 4.0);
         if (out) out[inst] = fres;
+        if (!isfinite(fres)) set_err(v.err, UNS_ERR_NAN, inst);
         if (v.iter) {
             int it = v.iter[inst];
             v.fres_hist[(size_t)inst * v.cfl_stride + it] = fres;
@@ -1562,7 +1563,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
                     rho = E.rho_old + w[5];
                 } else {
                     const size_t rs = (size_t)pass * n + E.nb;
-                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
+                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err, v.wait_cycles);
                     rho = E.rho_old + w[5];
                 }
                 // normal_flux (lusgs.F90:348-357) component k, then the face term
@@ -1585,7 +1586,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own lower
             if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
-            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
+            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
         }
         if (__ballot_sync(full, !ok)) return;
         // lower / upper (lusgs.F90:276-279 / 314-317), component k in lane k
@@ -1610,7 +1611,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
         Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
-        if (lane == 0) {
+        if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
+            last = -1;
+        } else if (lane == 0) {
             double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
             st_relaxed2(a, Lu, Lv);
             st_relaxed2(a + 1, Lp, Le);
@@ -1695,7 +1698,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
                 } else if (base == 0 && spec && set_f4(Sf)) {
                     dq[0] = Sf[0]; dq[1] = Sf[1]; dq[2] = Sf[2]; dq[3] = Sf[3];
                 } else {
-                    ok = poll_f4(recf + (size_t)pass * n + E.nb, dq, v.err);
+                    ok = poll_f4(recf + (size_t)pass * n + E.nb, dq, v.err, v.wait_cycles);
                 }
                 const float df = dflux_k(E, gm1, dq, k);
                 const float dqk = k == 0 ? dq[0] : (k == 1 ? dq[1] : (k == 2 ? dq[2] : dq[3]));
@@ -1710,7 +1713,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own lower
             if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
-            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
+            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
         }
         if (__ballot_sync(full, !ok)) return;
         const double d = pass == 0 ? (-r - 0.5 * cres) * X.D : r - 0.5 * cres * X.D;
@@ -1733,7 +1736,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
                      Q3 = __shfl_sync(full, q, 3);
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
-        if (lane == 0) {
+        if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
+            last = -1;
+        } else if (lane == 0) {
             st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, LF[0], LF[1], LF[2], LF[3]);
         } else if (lane == 1) {
             double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
@@ -2248,6 +2253,8 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     AL(qpf, ntot); AL(fqf, nof); AL(flaf, nof); AL(packf, 4 * (size_t)noc); AL(ppf, nop); AL(dcv, noc);
     { std::vector<float> t(m->v2c_wt, m->v2c_wt + m->v2c_off[nop]); UP(v2c_wtf, t); }
     AL(minmax, 8); AL(dtmin, 1); AL(err, 1);
+    h->v.wait_cycles = kWaitCycles;
+    h->v.skip_code = -1;
     h->nparts = nblocks(noc);
     AL(partial, h->nparts);
     if ((rc = h->alloc(h->d_scalar, 4))) return fail(rc);
@@ -2700,6 +2707,22 @@ static int iterate_graph(uns_cc_handle* h, int niter, const double* cfl, int fir
 }
 
 extern "C" {
+
+int uns_cc_set_wait_limit(uns_cc_handle* h, long long cycles) {
+    if (!h || cycles <= 0) return UNS_ERR_ARG;
+    h->v.wait_cycles = cycles;
+    ++h->gen;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return UNS_OK;
+}
+
+int uns_cc_debug_unpublish(uns_cc_handle* h, int cell, int pass) {
+    if (!h || cell < -1 || cell >= h->v.noc || pass < 0 || pass > 1) return UNS_ERR_ARG;
+    h->v.skip_code = cell < 0 ? -1 : (cell << 1) | pass;
+    ++h->gen;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return UNS_OK;
+}
 
 int uns_cc_set_precision(uns_cc_handle* h, int precision) {
     if (!h || precision < UNS_PREC_FP64 || precision > UNS_PREC_MIXED_SWEEP) return UNS_ERR_ARG;

@@ -90,6 +90,8 @@ struct CCView {
     unsigned long long* dtmin;   // encoded dtglobal
     double* partial;
     DevErr* err;
+    long long wait_cycles;  // bound of the sweeps' waits (kWaitCycles unless a caller set one)
+    int skip_code;          // test hook: the sweep item (cell << 1 | pass) that publishes nothing, or -1
     // iteration control (graph fast path)
     const double* cfl_sched;
     int* iter;

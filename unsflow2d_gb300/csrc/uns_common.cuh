@@ -45,7 +45,8 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Bound on every spin-wait in the library's kernels (~2 s at 2 GHz).
+// Default bound on every spin-wait in the library's kernels (~2 s at
+// 2 GHz); a handle may set a shorter one (uns_*_set_wait_limit).
 constexpr long long kWaitCycles = 4000000000LL;
 
 // ---------------------------------------------------------------------------
@@ -72,10 +73,10 @@ __device__ __forceinline__ void st_relaxed2(double2* p, double a, double b) {
 }
 
 // Bounded wait shared by the record polls: false (and UNS_ERR_TIMEOUT
-// recorded) once kWaitCycles have passed or another thread has timed out.
-__device__ __forceinline__ bool poll_continue(int spins, long long& t0, DevErr* err) {
+// recorded) once `limit` cycles have passed or another thread has timed out.
+__device__ __forceinline__ bool poll_continue(int spins, long long& t0, DevErr* err, long long limit = kWaitCycles) {
     if (spins == 0) t0 = clock64();
-    if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > kWaitCycles) {
+    if (*((volatile int*)&err->code) == UNS_ERR_TIMEOUT || clock64() - t0 > limit) {
         set_err(err, UNS_ERR_TIMEOUT, -1);
         return false;
     }
@@ -85,7 +86,8 @@ __device__ __forceinline__ bool poll_continue(int spins, long long& t0, DevErr* 
 
 // Reads the 2 x 32-byte record (a, b) of a sweep item into out[0..8), all
 // four loads in flight together, waiting (bounded) until none is kUnset.
-__device__ __forceinline__ bool poll_record2(const double4* a, const double4* b, double out[8], DevErr* err) {
+__device__ __forceinline__ bool poll_record2(const double4* a, const double4* b, double out[8], DevErr* err,
+                                             long long limit = kWaitCycles) {
     const double2* pa = reinterpret_cast<const double2*>(a);
     const double2* pb = reinterpret_cast<const double2*>(b);
     long long t0 = 0;
@@ -97,17 +99,17 @@ __device__ __forceinline__ bool poll_record2(const double4* a, const double4* b,
 #pragma unroll
         for (int j = 0; j < 8; ++j) ready = ready && !is_unset(out[j]);
         if (ready) return true;
-        if (!poll_continue(spins, t0, err)) return false;
+        if (!poll_continue(spins, t0, err, limit)) return false;
     }
 }
 
 // One published value, waiting (bounded) until it is not kUnset.
-__device__ __forceinline__ bool poll_value(const double* p, double& out, DevErr* err) {
+__device__ __forceinline__ bool poll_value(const double* p, double& out, DevErr* err, long long limit = kWaitCycles) {
     long long t0 = 0;
     for (int spins = 0;; ++spins) {
         asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(out) : "l"(p) : "memory");
         if (!is_unset(out)) return true;
-        if (!poll_continue(spins, t0, err)) return false;
+        if (!poll_continue(spins, t0, err, limit)) return false;
     }
 }
 
@@ -126,12 +128,12 @@ __device__ __forceinline__ bool set_f4(const float w[4]) {
 }
 
 // A float4 record, waiting (bounded) until none of its values is kUnsetF.
-__device__ __forceinline__ bool poll_f4(const float4* a, float w[4], DevErr* err) {
+__device__ __forceinline__ bool poll_f4(const float4* a, float w[4], DevErr* err, long long limit = kWaitCycles) {
     long long t0 = 0;
     for (int spins = 0;; ++spins) {
         peek_f4(a, w);
         if (set_f4(w)) return true;
-        if (!poll_continue(spins, t0, err)) return false;
+        if (!poll_continue(spins, t0, err, limit)) return false;
     }
 }
 

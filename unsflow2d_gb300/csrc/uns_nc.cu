@@ -79,10 +79,13 @@ struct NCView {
     double* diag;    // LU-SGS diagonal cv/dt + 0.5*omega*la (lusgs.f90:36)
     double* diaginv; // its FP64 reciprocal, read by the FP32 sweeps (a multiply on their critical path)
     double4* rec_a;  // sweep records [pass * nop + node]: (u, v, p, e*rho) of qc
-    double4* rec_b;  //   and dqc; rho is rebuilt as qold.rho + dqc.rho
+    double4* rec_b;  //   and dqc
+    double* rec_r;   //   and rho (FP64 sweep)
     double* partial;   // [2*nblk]: sum, max
     int* partial_i;    // argmax
     DevErr* err;
+    long long wait_cycles;  // bound of the sweeps' waits (kWaitCycles unless a caller set one)
+    int skip_code;          // test hook: the sweep item (node << 1 | pass) that publishes nothing, or -1
     const double* cfl_sched;
     int* iter;
     int* done;
@@ -563,6 +566,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_res_final(NCView v, int nparts, d
         double fresi = sm[0] > 0.0 ? sm[0] : 0.0;
         int iresi = sm[0] > 0.0 ? si[0] : -1;
         if (out) { out[0] = fres; out[1] = fresi; out[2] = (double)iresi; }
+        if (!isfinite(fres)) set_err(v.err, UNS_ERR_NAN, -1);
         if (v.iter) {
             int it = *v.iter;
             v.fres_hist[it] = fres;
@@ -639,44 +643,13 @@ __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep_mixed(NCView v) {
     rf[3] = make_float4((float)v.rec_sign[r], __int_as_float(nb), 0.f, 0.f);
 }
 
-// normalflux (lusgs.f90:137-155) from primitives a sweep has published.
-__device__ __forceinline__ void normalflux_prims(double rho, double u, double vv, double p, double et, double nx,
-                                                 double ny, double ds, double o[4]) {
-    double un = u * nx + vv * ny;
-    o[0] = (et + p) * un;
-    o[1] = rho * un;
-    o[2] = o[1] * u + p * nx;
-    o[3] = o[1] * vv + p * ny;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) o[k] = o[k] * ds;
-}
-
 __device__ __forceinline__ double pick4(int k, double a, double b, double c, double d) {
     return k == 0 ? a : (k == 1 ? b : (k == 2 ? c : d));
 }
 
-// Lanes of a sweep item: lane = 4 * slot + k, slot = the taken edge (up to 8
-// per round), k = the variable.  An FP64 instruction costs its SM
-// sub-partition the same whatever the number of active lanes, so each item's
-// arithmetic is spread over the lanes: the four flux components of up to
-// eight edges in one pass, the per-variable sums and divides in lanes 0..3,
-// and the three divisions of con2prim in lanes 0, 2 and 3 at once.
-struct SweepIn {
-    double f1, nx, ny, ds, ol, rho_old, sign;  // the slot's record; f1 = component k
-    int nb;
-    double D, o, r;  // lanes 0..3: the node's diagonal, qold and res, variable k
-};
-
-__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
-    const double4* p = v.rec + 3 * (size_t)rec;
-    x.f1 = reinterpret_cast<const double*>(p)[k];
-    double4 b = p[1], c = p[2];
-    x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-    x.rho_old = c.x; x.sign = c.y; x.nb = (int)__double_as_longlong(c.z);
-}
-
 // The node's own diagonal, qold and res (variable `lane`) in lanes 0..3;
 // benign operands elsewhere, so the warp-wide divides meet no 0 or inf.
+// (The mixed form's sweep.)
 __device__ __forceinline__ void own_load(const NCView& v, const int4& S, int lane, double& D, double& o, double& r) {
     if (lane < 4) {
         D = v.diag[S.x];
@@ -689,26 +662,98 @@ __device__ __forceinline__ void own_load(const NCView& v, const int4& S, int lan
     }
 }
 
-__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
-    if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
-    own_load(v, S, lane, x.D, x.o, x.r);
+// Lanes of a sweep item: lane = 4 * slot + k, slot = the taken edge (up to 8
+// per round), k = the variable.  An FP64 instruction costs its SM
+// sub-partition the same whatever the number of active lanes (about 70
+// cycles on GB300), so each item's arithmetic is spread over the lanes: the
+// four flux components of up to eight edges in one pass, the per-variable
+// sums and divides in lanes 0..3, and the three divisions of con2prim in
+// lanes 0, 2 and 3 at once.  Exact operations that need no FP64 instruction
+// run on the integer pipe: halving (half_rn), the edge orientation sign and
+// the first term of a sum; the division by the diagonal goes through its
+// reciprocal (div_rn_recip, correctly rounded).
+#ifndef SW_RHO_REC
+#define SW_RHO_REC 1
+#endif
+#ifndef SW_NBN
+#define SW_NBN 1
+#endif
+#ifndef SW_FWD_SPEC
+#define SW_FWD_SPEC 1
+#endif
+#ifndef SW_MARK
+#define SW_MARK 1
+#endif
+#ifndef SW_HALF
+#define SW_HALF 1
+#endif
+#ifndef SW_SUM
+#define SW_SUM 1
+#endif
+struct SweepIn {
+    double f1, nx, ny, ds, ol, rho_old;  // the slot's record; f1 = component k
+    bool neg;                   // orientation sign -1
+    int nb;
+    double D, y, o, r;          // lanes 0..3: the diagonal, its reciprocal, qold and res (pass 0) / the
+                                // speculatively read forward dqc (pass 1), variable k
+};
+
+__device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
+    const double4* p = v.rec + 3 * (size_t)rec;
+    x.f1 = reinterpret_cast<const double*>(p)[k];
+    double4 b = p[1], c = p[2];
+    x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
+    x.neg = __double_as_longlong(c.y) < 0;
+    x.rho_old = c.x;
+    x.nb = (int)__double_as_longlong(c.z);
 }
 
-// One unconditional read of a neighbour record, issued early; the values are
-// checked (record_set) only when the item that needs them starts.
-__device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, double w[4], double dq[4]) {
+__device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int lane, SweepIn& x) {
+    if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
+    if (lane < 4) {
+        x.D = v.diag[S.x];
+        x.y = v.diaginv[S.x];
+        x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
+        if (S.y == 0) {
+            x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
+        } else if (SW_FWD_SPEC) {  // the node's forward dqc: usually published long before; checked when used
+            asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];"
+                         : "=d"(x.r) : "l"(reinterpret_cast<const double*>(v.rec_b + S.x) + lane) : "memory");
+        }
+    } else {
+        x.D = 1.0;
+        x.y = 1.0;
+        x.o = 1.0;
+        x.r = 0.0;
+    }
+}
+
+// A neighbour's record: (u, v, p, e*rho) in w[0..4), dqc in w[4..8), rho.
+__device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, double w[8], double& rho) {
     const double2* pa = reinterpret_cast<const double2*>(v.rec_a + rs);
     const double2* pb = reinterpret_cast<const double2*>(v.rec_b + rs);
     double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1), x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
+    if (SW_RHO_REC) asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(rho) : "l"(v.rec_r + rs) : "memory");
+    else rho = 1.0;
     w[0] = x0.x; w[1] = x0.y; w[2] = x1.x; w[3] = x1.y;
-    dq[0] = x2.x; dq[1] = x2.y; dq[2] = x3.x; dq[3] = x3.y;
+    w[4] = x2.x; w[5] = x2.y; w[6] = x3.x; w[7] = x3.y;
 }
 
-__device__ __forceinline__ bool record_set(const double w[4], const double dq[4]) {
-    bool ready = true;
+__device__ __forceinline__ bool record_set(const double w[8], double rho) {
+    bool ready = !is_unset(rho);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) ready = ready && !is_unset(w[j]) && !is_unset(dq[j]);
+    for (int j = 0; j < 8; ++j) ready = ready && !is_unset(w[j]);
     return ready;
+}
+
+// A neighbour's record, waiting (bounded) until every value is published.
+__device__ __forceinline__ bool poll_neighbour(const NCView& v, size_t rs, double w[8], double& rho) {
+    long long t0 = 0;
+    for (int spins = 0;; ++spins) {
+        peek_neighbour(v, rs, w, rho);
+        if (record_set(w, rho)) return true;
+        if (!poll_continue(spins, t0, v.err, v.wait_cycles)) return false;
+    }
 }
 
 // lusgs sweeps (lusgs.f90:48-124) as one cooperative launch.  Each warp runs
@@ -716,13 +761,13 @@ __device__ __forceinline__ bool record_set(const double w[4], const double dq[4]
 // order, loading the next item's inputs while it works on the current one.
 // Per item, for each edge whose neighbour precedes the node in this pass
 // (reference v2f order): the neighbour's values come from registers when the
-// warp itself computed that neighbour last, else from its record (read early
-// or polled); the edge term 0.5*(sign*(F(qc) - F(qold)) - omega*la*dqc) is
-// formed per component; lanes 0..3 add the terms in edge order (the
-// reference's summation order) and divide by the diagonal; the new state is
-// spread to all lanes, which keep its primitives for the next item while
-// lanes 0 and 1 publish the record.  Every operation and operand order is the
-// reference's.
+// warp itself computed that neighbour last, else from its record (read
+// during the previous item, or polled); the edge term
+// 0.5*(sign*(F(qc) - F(qold)) - omega*la*dqc) is formed per component; lanes
+// 0..3 add the terms in edge order (the reference's summation order) and
+// divide by the diagonal; the new state is spread to all lanes, which keep
+// its primitives for the next item while lanes 0..2 publish the record.
+// Every rounded operation and its operand order is the reference's.
 __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -742,10 +787,12 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
     double Lrho = 0.0, Lu = 0.0, Lv = 0.0, Lp = 0.0, Le = 0.0, L0 = 0.0, L1 = 0.0, L2 = 0.0, L3 = 0.0;
     // early read of the current item's first-round neighbour record, issued
     // during the previous item (usually already published)
-    double Sw[4] = {0.0, 0.0, 0.0, 0.0}, Sdq[4] = {0.0, 0.0, 0.0, 0.0};
+    double Sw[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0}, Srho = 0.0;
     bool spec = false;
     for (int kk = kbeg; kk < kend; ++kk) {
         const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
+        // the next item's first-round neighbour, for its early record read
+        const int nbn = (SW_NBN && kk + 1 < kend && slot < Sn.w) ? v.rec_nb[Sn.z + slot] : -1;
         const int it = S.x, pass = S.y, ntake = S.w;
         double cres = 0.0;  // lanes 0..3: sum over edges of component k
         for (int base = 0; base < ntake; base += 8) {
@@ -758,14 +805,13 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
                 if (((E.nb << 1) | pass) == last) {
                     w[0] = Lu; w[1] = Lv; w[2] = Lp; w[3] = Le; w[4] = L0; w[5] = L1; w[6] = L2; w[7] = L3;
                     rho = Lrho;
-                } else if (base == 0 && spec && record_set(Sw, Sdq)) {
-                    w[0] = Sw[0]; w[1] = Sw[1]; w[2] = Sw[2]; w[3] = Sw[3];
-                    w[4] = Sdq[0]; w[5] = Sdq[1]; w[6] = Sdq[2]; w[7] = Sdq[3];
-                    rho = E.rho_old + w[5];
+                } else if (base == 0 && spec && record_set(Sw, Srho)) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) w[j] = Sw[j];
+                    rho = SW_RHO_REC ? Srho : E.rho_old + w[5];
                 } else {
-                    const size_t rs = (size_t)pass * n + E.nb;
-                    ok = poll_record2(v.rec_a + rs, v.rec_b + rs, w, v.err);
-                    rho = E.rho_old + w[5];
+                    ok = poll_neighbour(v, (size_t)pass * n + E.nb, w, rho);
+                    if (!SW_RHO_REC) rho = E.rho_old + w[5];
                 }
                 // normalflux (lusgs.f90:144-150) component k, then the edge term
                 const double u = w[0], vv = w[1], p = w[2], et = w[3];
@@ -777,11 +823,27 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
                 o = o * E.ds;
                 const double diff = o - E.f1;
                 const double dqk = pick4(k, w[4], w[5], w[6], w[7]);
-                t = 0.5 * ((E.sign < 0.0 ? -diff : diff) - E.ol * dqk);
+                t = SW_HALF ? half_rn((E.neg ? -diff : diff) - E.ol * dqk) : 0.5 * ((E.neg ? -diff : diff) - E.ol * dqk);
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
+            // the terms in edge order: every shuffle first, then the dependent adds
             const int nr = min(8, ntake - base);
+#if SW_SUM
+            double tt[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) tt[e] = __shfl_sync(full, t, 4 * e + k);
+            if (base == 0)  // 0.0 + t0 = t0, except that -0 becomes +0
+                cres = (__double_as_longlong(tt[0]) == (long long)0x8000000000000000ULL) ? 0.0 : tt[0];
+            else
+                cres = cres + tt[0];
+#pragma unroll
+            for (int e = 1; e < 8; ++e) {
+                if (e >= nr) break;
+                cres = cres + tt[e];
+            }
+#else
             for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
+#endif
         }
         // next item's inputs (independent of the sweep), issued once this
         // item's polls are done so they do not queue ahead of them
@@ -790,25 +852,31 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
             if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
-            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
+            else if (!SW_FWD_SPEC || is_unset(r)) ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
         }
         if (__ballot_sync(full, !ok)) return;
         // dqc and qc = qold + dqc (lusgs.f90:78-81 / 117-120), component k in lane k
+#if SW_MARK
+        const double d = pass == 0 ? div_rn_recip(-r - cres, X.D, X.y) : r - div_rn_recip(cres, X.D, X.y);
+#else
         const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
+#endif
         const double q = X.o + d;
         // the next item's first-round neighbour records, while this item finishes
         spec = false;
-        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
-            peek_neighbour(v, (size_t)Sn.y * n + Xn.nb, Sw, Sdq);
+        const int nbx = SW_NBN ? nbn : ((kk + 1 < kend && slot < Sn.w) ? Xn.nb : -1);
+        if (nbx >= 0 && ((nbx << 1) | Sn.y) != ((it << 1) | pass)) {
+            peek_neighbour(v, (size_t)Sn.y * n + nbx, Sw, Srho);
             spec = true;
         }
-        // con2prim (pri.f90): rho = q1, then E/rho, rhou/rho, rhov/rho in lanes 0, 2, 3
+        // con2prim (All_modules.f90:146-169): rho = q1, then E/rho, rhou/rho,
+        // rhov/rho in lanes 0, 2, 3
         const double rho = __shfl_sync(full, q, 1);
         const double quo = q / rho;
         const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
         const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
         const double qq = u * u + vv * vv;
-        const double p = gm1 * (E0 - 0.5 * rho * qq);
+        const double p = gm1 * (E0 - (SW_HALF ? half_rn(rho) : 0.5 * rho) * qq);
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
@@ -816,7 +884,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
-        if (lane == 0) {
+        if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
+            last = -1;
+        } else if (lane == 0) {
             double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
             st_relaxed2(a, Lu, Lv);
             st_relaxed2(a + 1, Lp, Le);
@@ -824,8 +894,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
             double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
-        } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(E0, rho, Q2, Q3);
+        } else if (lane == 2) {
+            if (SW_RHO_REC) asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" : : "l"(v.rec_r + slotr), "d"(rho) : "memory");
+            if (pass == 1) v.qc[it] = make_double4(E0, rho, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
@@ -900,7 +971,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
                 } else if (base == 0 && spec && set_f4(Sf)) {
                     dq[0] = Sf[0]; dq[1] = Sf[1]; dq[2] = Sf[2]; dq[3] = Sf[3];
                 } else {
-                    ok = poll_f4(recf + (size_t)pass * n + E.nb, dq, v.err);
+                    ok = poll_f4(recf + (size_t)pass * n + E.nb, dq, v.err, v.wait_cycles);
                 }
                 const float df = dflux_k(E, gm1, dq, k);
                 const float dqk = k == 0 ? dq[0] : (k == 1 ? dq[1] : (k == 2 ? dq[2] : dq[3]));
@@ -915,7 +986,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
             if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
-            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err);
+            else ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
         }
         if (__ballot_sync(full, !ok)) return;
         const double d = pass == 0 ? (-r - cres) * X.D : r - cres * X.D;
@@ -938,7 +1009,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
                      Q3 = __shfl_sync(full, q, 3);
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
-        if (lane == 0) {
+        if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
+            last = -1;
+        } else if (lane == 0) {
             st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, LF[0], LF[1], LF[2], LF[3]);
         } else if (lane == 1) {
             double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
@@ -1041,8 +1114,11 @@ int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
     if (mixed)
         k_fill_unset_f<<<std::min<long long>(nblocks(2LL * v.nop), 4096), kBlock, 0, h->stream>>>((float4*)v.rec_a,
                                                                                                    2LL * v.nop);
-    else
+    else {
         k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_a, n2);
+        k_fill_unset<<<std::min<long long>(nblocks(v.nop), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_r,
+                                                                                           (long long)v.nop);
+    }
     k_fill_unset<<<std::min<long long>(nblocks(n2), 4096), kBlock, 0, h->stream>>>((double2*)v.rec_b, n2);
     UNS_CUDA(cudaGetLastError());
     cudaLaunchConfig_t cfg = {};
@@ -1188,8 +1264,10 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
     ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(packn, 3 * (size_t)nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
-    ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop);
+    ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop); ALN(rec_r, 2 * (size_t)nop);
     ALN(err, 1);
+    h->v.wait_cycles = kWaitCycles;
+    h->v.skip_code = -1;
     h->nparts = nblocks(nop);
     ALN(partial, 2 * h->nparts);
     ALN(partial_i, h->nparts);
@@ -1406,6 +1484,20 @@ int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_ite
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     if (done_iters) *done_iters = it;
     return check_err_nc(h);
+}
+
+int uns_nc_set_wait_limit(uns_nc_handle* h, long long cycles) {
+    if (!h || cycles <= 0) return UNS_ERR_ARG;
+    h->v.wait_cycles = cycles;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return UNS_OK;
+}
+
+int uns_nc_debug_unpublish(uns_nc_handle* h, int node, int pass) {
+    if (!h || node < -1 || node >= h->v.nop || pass < 0 || pass > 1) return UNS_ERR_ARG;
+    h->v.skip_code = node < 0 ? -1 : (node << 1) | pass;
+    if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+    return UNS_OK;
 }
 
 int uns_nc_set_precision(uns_nc_handle* h, int precision) {

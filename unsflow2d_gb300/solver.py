@@ -15,6 +15,14 @@ import numpy as np
 from . import abi
 
 
+def _raise_with_history(rc: int, lib, where: str, history) -> None:
+    if rc != abi.UNS_OK:
+        msg = lib.uns_last_error()
+        err = abi.UnsError(rc, f"{where}: {msg.decode() if msg else ''}")
+        err.history = history
+        raise err
+
+
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
@@ -81,6 +89,16 @@ class _Solver:
         b = (C.c_int * 3)()
         self._call("autotune", reps, b)
         return {"face": b[0], "vertex": b[1], "cell_grad": b[2]}
+
+    def set_wait_limit(self, cycles: int) -> None:
+        """Bound of the LU-SGS sweeps' waits, in device clock cycles."""
+        self._call("set_wait_limit", C.c_longlong(int(cycles)))
+
+    def debug_unpublish(self, entity: int, sweep: int) -> None:
+        """Test hook: sweep item (entity, sweep 0 forward / 1 backward)
+        publishes nothing, so the items that need it wait until the wait
+        limit and the sweep returns UNS_ERR_TIMEOUT; entity -1 clears it."""
+        self._call("debug_unpublish", int(entity), int(sweep))
 
     def get(self, field: str) -> np.ndarray:
         shape = self._field_shape(field)
@@ -212,11 +230,15 @@ class CCSolver(_Solver):
         return self.residue()
 
     def iterate(self, cfl: np.ndarray, first_iter: bool) -> np.ndarray:
-        """Graph-replayed iterations; returns the raw residual norms of the iterations run."""
+        """Graph-replayed iterations; returns the raw residual norms of the
+        iterations run.  A device error (a non-positive state, a negative Roe
+        sound speed, a non-finite residual norm) raises abi.UnsError, whose
+        `history` holds the norms of the iterations run until then."""
         cfl = np.ascontiguousarray(cfl, dtype=np.float64)
         out = np.zeros(len(cfl))
         done = C.c_int()
-        self._call("iterate", len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), C.byref(done))
+        rc = self._lib.uns_cc_iterate(self._h, len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), C.byref(done))
+        _raise_with_history(rc, self._lib, "uns_cc_iterate", out[:done.value])
         return out[:done.value]
 
 
@@ -268,7 +290,9 @@ class NCSolver(_Solver):
         out = np.zeros(len(cfl))
         outi = np.zeros(len(cfl))
         done = C.c_int()
-        self._call("iterate", len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), _dp(outi), C.byref(done))
+        rc = self._lib.uns_nc_iterate(self._h, len(cfl), _dp(cfl), 1 if first_iter else 0, _dp(out), _dp(outi),
+                                      C.byref(done))
+        _raise_with_history(rc, self._lib, "uns_nc_iterate", (out[:done.value], outi[:done.value]))
         return out[:done.value], outi[:done.value]
 
 
