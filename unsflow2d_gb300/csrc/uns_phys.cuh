@@ -102,7 +102,7 @@ __device__ __forceinline__ bool roe_flux(R G, R G1, R nx, R ny, R area, const V4
     R ha = (hl * rl12 + hr * rr12) * rd;
     R qa2 = ua * ua + va * va;
     R aa2 = G1 * (ha - R(0.5) * qa2);
-    bool ok = aa2 > R(0);
+    bool ok = !(aa2 <= R(0));  // roe_flux.F90:73: `if (aa2 .le. 0)` -- a NaN goes on, as there
     R aa = sqrt(aa2);
     R una = ua * nx + va * ny;
     R vna = -ua * ny + va * nx;
