@@ -28,12 +28,9 @@ const char* uns_version(void);
 /* Test hooks (no reference counterpart), n host values each:
  * out[i] = a[i] / b[i] by the kernels' division through the reciprocal
  * (must equal IEEE division), and lt[i] = whether a[i]/b[i] < c[i]/d[i]
- * by the kernels' exact ratio comparison (-1 where it does not apply), and
- * out[i] = 0.5 * a[i] by the kernels' integer halving (must equal the FP64
- * multiply). */
+ * by the kernels' exact ratio comparison (-1 where it does not apply). */
 int uns_selftest_div(const double* a, const double* b, double* out, int n);
 int uns_selftest_ratio(const double* a, const double* b, const double* c, const double* d, int* lt, int n);
-int uns_selftest_half(const double* a, double* out, int n);
 
 /* ============================================================ CCFVM =====*/
 typedef struct uns_cc_handle uns_cc_handle;

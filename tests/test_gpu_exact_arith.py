@@ -19,7 +19,6 @@ def _lib():
     lib = abi.gpu_lib()
     lib.uns_selftest_div.argtypes = [D, D, D, C.c_int]
     lib.uns_selftest_ratio.argtypes = [D, D, D, D, C.POINTER(C.c_int), C.c_int]
-    lib.uns_selftest_half.argtypes = [D, D, C.c_int]
     return lib
 
 
@@ -73,22 +72,3 @@ def test_exact_ratio_comparison():
     exact = np.array([Fraction(x) / Fraction(y) < Fraction(z) / Fraction(w) for x, y, z, w in zip(a, b, c, d)])
     assert np.array_equal(lt[applies].astype(bool), exact[applies])
 
-
-def test_integer_halving_equals_the_multiply():
-    """half_rn, the sweeps' 0.5*x on the integer pipe, against IEEE 0.5*x:
-    normal values, the smallest binade (half subnormal, ties to even),
-    subnormals, zeros, infinities."""
-    rng = np.random.default_rng(7)
-    n = 1 << 20
-    a = rng.standard_normal(n) * np.exp2(rng.integers(-1074, 1023, n).astype(float))
-    bits = rng.integers(0, 1 << 53, n // 4, dtype=np.uint64)  # exponent field 0 or 1, any significand
-    sub = bits.view(np.float64) * np.where(rng.integers(0, 2, n // 4) == 1, -1.0, 1.0)
-    special = np.array([0.0, -0.0, 5e-324, -5e-324, 1e-323, 3 * 5e-324, np.finfo(float).tiny,
-                        np.nextafter(np.finfo(float).tiny, 0.0), 2 * np.finfo(float).tiny, np.finfo(float).max,
-                        np.inf, -np.inf, 1.0, -3.0])
-    a = np.concatenate([a, sub, special])
-    out = np.zeros_like(a)
-    assert _lib().uns_selftest_half(_p(a), _p(out), len(a)) == 0
-    ref = 0.5 * a
-    bad = np.flatnonzero(out.view(np.uint64) != ref.view(np.uint64))
-    assert len(bad) == 0, [(float(a[i]).hex(), float(out[i]).hex(), float(ref[i]).hex()) for i in bad[:8]]

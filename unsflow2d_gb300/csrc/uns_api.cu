@@ -13,10 +13,6 @@ __global__ void k_selftest_div(const double* a, const double* b, double* out, in
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = uns::div_rn_recip(a[i], b[i], 1.0 / b[i]);
 }
-__global__ void k_selftest_half(const double* a, double* out, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = uns::half_rn(a[i]);
-}
 __global__ void k_selftest_ratio(const double* a, const double* b, const double* c, const double* d, int* lt, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -62,12 +58,6 @@ const char* uns_version(void) { return "unsflow_gpu 0.1 (sm_103a)"; }
 int uns_selftest_div(const double* a, const double* b, double* out, int n) {
     return run_selftest("uns_selftest_div", n, {a, b}, out, [&](std::vector<double*>& d, double* o, int nb) {
         k_selftest_div<<<nb, 256>>>(d[0], d[1], o, n);
-    });
-}
-
-int uns_selftest_half(const double* a, double* out, int n) {
-    return run_selftest("uns_selftest_half", n, {a}, out, [&](std::vector<double*>& d, double* o, int nb) {
-        k_selftest_half<<<nb, 256>>>(d[0], o, n);
     });
 }
 

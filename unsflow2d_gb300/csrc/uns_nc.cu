@@ -668,34 +668,19 @@ __device__ __forceinline__ void own_load(const NCView& v, const int4& S, int lan
 // cycles on GB300), so each item's arithmetic is spread over the lanes: the
 // four flux components of up to eight edges in one pass, the per-variable
 // sums and divides in lanes 0..3, and the three divisions of con2prim in
-// lanes 0, 2 and 3 at once.  Exact operations that need no FP64 instruction
-// run on the integer pipe: halving (half_rn), the edge orientation sign and
-// the first term of a sum; the division by the diagonal goes through its
-// reciprocal (div_rn_recip, correctly rounded).
-#ifndef SW_RHO_REC
-#define SW_RHO_REC 1
-#endif
-#ifndef SW_NBN
-#define SW_NBN 1
-#endif
-#ifndef SW_FWD_SPEC
-#define SW_FWD_SPEC 1
-#endif
-#ifndef SW_MARK
-#define SW_MARK 1
-#endif
-#ifndef SW_HALF
-#define SW_HALF 1
-#endif
-#ifndef SW_SUM
-#define SW_SUM 1
-#endif
+// lanes 0, 2 and 3 at once.  Chosen by measurement on GB300 (sweeps at
+// 1024x512, bit-identical variants): the consumer reads rho from the record
+// rather than forming qold.rho + dqc.rho; the warp exchanges its per-lane
+// values through shared memory rather than shuffles; the division by the
+// diagonal stays an IEEE division (through a precomputed reciprocal with
+// Markstein's correction it was slower, as was halving on the integer pipe);
+// the next item's inputs are loaded after this item's polls.
 struct SweepIn {
-    double f1, nx, ny, ds, ol, rho_old;  // the slot's record; f1 = component k
-    bool neg;                   // orientation sign -1
+    double f1, nx, ny, ds, ol;  // the slot's record; f1 = component k
+    double sgn;                 // orientation sign +-1 (tested where used, so no load is waited on here)
     int nb;
-    double D, y, o, r;          // lanes 0..3: the diagonal, its reciprocal, qold and res (pass 0) / the
-                                // speculatively read forward dqc (pass 1), variable k
+    double D, o, r;             // lanes 0..3: the diagonal, qold and res (pass 0) / the early-read
+                                // forward dqc (pass 1), variable k
 };
 
 __device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k, SweepIn& x) {
@@ -703,8 +688,7 @@ __device__ __forceinline__ void sweep_load_edge(const NCView& v, int rec, int k,
     x.f1 = reinterpret_cast<const double*>(p)[k];
     double4 b = p[1], c = p[2];
     x.nx = b.x; x.ny = b.y; x.ds = b.z; x.ol = b.w;
-    x.neg = __double_as_longlong(c.y) < 0;
-    x.rho_old = c.x;
+    x.sgn = c.y;
     x.nb = (int)__double_as_longlong(c.z);
 }
 
@@ -712,17 +696,15 @@ __device__ __forceinline__ void sweep_load(const NCView& v, const int4& S, int l
     if ((lane >> 2) < S.w) sweep_load_edge(v, S.z + (lane >> 2), lane & 3, x);
     if (lane < 4) {
         x.D = v.diag[S.x];
-        x.y = v.diaginv[S.x];
         x.o = reinterpret_cast<const double*>(&v.qold[S.x])[lane];
         if (S.y == 0) {
             x.r = reinterpret_cast<const double*>(&v.res[S.x])[lane];
-        } else if (SW_FWD_SPEC) {  // the node's forward dqc: usually published long before; checked when used
+        } else {  // the node's forward dqc: usually published long before; checked when used
             asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];"
                          : "=d"(x.r) : "l"(reinterpret_cast<const double*>(v.rec_b + S.x) + lane) : "memory");
         }
     } else {
         x.D = 1.0;
-        x.y = 1.0;
         x.o = 1.0;
         x.r = 0.0;
     }
@@ -733,8 +715,7 @@ __device__ __forceinline__ void peek_neighbour(const NCView& v, size_t rs, doubl
     const double2* pa = reinterpret_cast<const double2*>(v.rec_a + rs);
     const double2* pb = reinterpret_cast<const double2*>(v.rec_b + rs);
     double2 x0 = ld_relaxed2(pa), x1 = ld_relaxed2(pa + 1), x2 = ld_relaxed2(pb), x3 = ld_relaxed2(pb + 1);
-    if (SW_RHO_REC) asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(rho) : "l"(v.rec_r + rs) : "memory");
-    else rho = 1.0;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(rho) : "l"(v.rec_r + rs) : "memory");
     w[0] = x0.x; w[1] = x0.y; w[2] = x1.x; w[3] = x1.y;
     w[4] = x2.x; w[5] = x2.y; w[6] = x3.x; w[7] = x3.y;
 }
@@ -771,6 +752,8 @@ __device__ __forceinline__ bool poll_neighbour(const NCView& v, size_t rs, doubl
 __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int* __restrict__ woff) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    __shared__ __align__(16) double wxs[kSweepBlock / 32][32];  // per-warp exchange of lane values
+    double* wx = wxs[wib];
     const int gw = blockIdx.x * (kSweepBlock / 32) + wib;
     const int slot = lane >> 2, k = lane & 3;
     if (stopped(v)) return;
@@ -791,8 +774,6 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
     bool spec = false;
     for (int kk = kbeg; kk < kend; ++kk) {
         const int4 Snn = kk + 2 < kend ? v.sched[kk + 2] : none;
-        // the next item's first-round neighbour, for its early record read
-        const int nbn = (SW_NBN && kk + 1 < kend && slot < Sn.w) ? v.rec_nb[Sn.z + slot] : -1;
         const int it = S.x, pass = S.y, ntake = S.w;
         double cres = 0.0;  // lanes 0..3: sum over edges of component k
         for (int base = 0; base < ntake; base += 8) {
@@ -808,10 +789,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
                 } else if (base == 0 && spec && record_set(Sw, Srho)) {
 #pragma unroll
                     for (int j = 0; j < 8; ++j) w[j] = Sw[j];
-                    rho = SW_RHO_REC ? Srho : E.rho_old + w[5];
+                    rho = Srho;
                 } else {
                     ok = poll_neighbour(v, (size_t)pass * n + E.nb, w, rho);
-                    if (!SW_RHO_REC) rho = E.rho_old + w[5];
                 }
                 // normalflux (lusgs.f90:144-150) component k, then the edge term
                 const double u = w[0], vv = w[1], p = w[2], et = w[3];
@@ -823,27 +803,15 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
                 o = o * E.ds;
                 const double diff = o - E.f1;
                 const double dqk = pick4(k, w[4], w[5], w[6], w[7]);
-                t = SW_HALF ? half_rn((E.neg ? -diff : diff) - E.ol * dqk) : 0.5 * ((E.neg ? -diff : diff) - E.ol * dqk);
+                t = 0.5 * ((__double_as_longlong(E.sgn) < 0 ? -diff : diff) - E.ol * dqk);
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
-            // the terms in edge order: every shuffle first, then the dependent adds
+            // the terms in edge order
             const int nr = min(8, ntake - base);
-#if SW_SUM
-            double tt[8];
-#pragma unroll
-            for (int e = 0; e < 8; ++e) tt[e] = __shfl_sync(full, t, 4 * e + k);
-            if (base == 0)  // 0.0 + t0 = t0, except that -0 becomes +0
-                cres = (__double_as_longlong(tt[0]) == (long long)0x8000000000000000ULL) ? 0.0 : tt[0];
-            else
-                cres = cres + tt[0];
-#pragma unroll
-            for (int e = 1; e < 8; ++e) {
-                if (e >= nr) break;
-                cres = cres + tt[e];
-            }
-#else
-            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
-#endif
+            wx[lane] = t;
+            __syncwarp();
+            for (int e = 0; e < nr; ++e) cres = cres + wx[4 * e + k];
+            __syncwarp();
         }
         // next item's inputs (independent of the sweep), issued once this
         // item's polls are done so they do not queue ahead of them
@@ -852,35 +820,33 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         bool ok = true;
         if (pass == 1 && lane < 4) {  // own forward dqc
             if ((it << 1) == last) r = pick4(lane, L0, L1, L2, L3);
-            else if (!SW_FWD_SPEC || is_unset(r)) ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
+            else if (is_unset(r)) ok = poll_value(reinterpret_cast<const double*>(v.rec_b + it) + lane, r, v.err, v.wait_cycles);
         }
         if (__ballot_sync(full, !ok)) return;
         // dqc and qc = qold + dqc (lusgs.f90:78-81 / 117-120), component k in lane k
-#if SW_MARK
-        const double d = pass == 0 ? div_rn_recip(-r - cres, X.D, X.y) : r - div_rn_recip(cres, X.D, X.y);
-#else
         const double d = pass == 0 ? (-r - cres) / X.D : r - cres / X.D;
-#endif
         const double q = X.o + d;
         // the next item's first-round neighbour records, while this item finishes
         spec = false;
-        const int nbx = SW_NBN ? nbn : ((kk + 1 < kend && slot < Sn.w) ? Xn.nb : -1);
-        if (nbx >= 0 && ((nbx << 1) | Sn.y) != ((it << 1) | pass)) {
-            peek_neighbour(v, (size_t)Sn.y * n + nbx, Sw, Srho);
+        if (kk + 1 < kend && slot < Sn.w && ((Xn.nb << 1) | Sn.y) != ((it << 1) | pass)) {
+            peek_neighbour(v, (size_t)Sn.y * n + Xn.nb, Sw, Srho);
             spec = true;
         }
         // con2prim (All_modules.f90:146-169): rho = q1, then E/rho, rhou/rho,
         // rhov/rho in lanes 0, 2, 3
-        const double rho = __shfl_sync(full, q, 1);
+        if (lane < 4) { wx[lane] = q; wx[4 + lane] = d; }
+        __syncwarp();
+        const double2 qa = reinterpret_cast<const double2*>(wx)[0], qb = reinterpret_cast<const double2*>(wx)[1];
+        const double E0 = qa.x, rho = qa.y, Q2 = qb.x, Q3 = qb.y;
         const double quo = q / rho;
-        const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
-        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        if (lane < 4) wx[8 + lane] = quo;
+        __syncwarp();
+        const double2 da = reinterpret_cast<const double2*>(wx)[2], db = reinterpret_cast<const double2*>(wx)[3];
+        const double e = wx[8], u = wx[10], vv = wx[11];
+        L0 = da.x; L1 = da.y; L2 = db.x; L3 = db.y;
+        __syncwarp();
         const double qq = u * u + vv * vv;
-        const double p = gm1 * (E0 - (SW_HALF ? half_rn(rho) : 0.5 * rho) * qq);
-        L0 = __shfl_sync(full, d, 0);
-        L1 = __shfl_sync(full, d, 1);
-        L2 = __shfl_sync(full, d, 2);
-        L3 = __shfl_sync(full, d, 3);
+        const double p = gm1 * (E0 - 0.5 * rho * qq);
         Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
@@ -895,7 +861,7 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
             st_relaxed2(b, L0, L1);
             st_relaxed2(b + 1, L2, L3);
         } else if (lane == 2) {
-            if (SW_RHO_REC) asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" : : "l"(v.rec_r + slotr), "d"(rho) : "memory");
+            asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" : : "l"(v.rec_r + slotr), "d"(rho) : "memory");
             if (pass == 1) v.qc[it] = make_double4(E0, rho, Q2, Q3);
         }
         S = Sn;

@@ -444,20 +444,6 @@ __device__ __forceinline__ double div_rn_recip(double a, double b, double y) {
     return q1;
 }
 
-// RN(0.5 x) for every x, on the integer pipe: a normal x with a normal half
-// loses one from its exponent; a half that is subnormal (x subnormal, zero
-// or in the smallest binade) is the significand shifted right by one,
-// rounded to nearest even; infinities and NaNs pass through.
-__device__ __forceinline__ double half_rn(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned long long e = (b >> 52) & 0x7ffULL;
-    const unsigned long long m = (b & 0x000FFFFFFFFFFFFFULL) | (e == 1 ? (1ULL << 52) : 0ULL);
-    const unsigned long long h = (m >> 1) + (m & (m >> 1) & 1ULL);
-    unsigned long long r = e >= 2 ? b - (1ULL << 52) : ((b & 0x8000000000000000ULL) | h);
-    if (e == 0x7ffULL) r = b;
-    return __longlong_as_double((long long)r);
-}
-
 // Whether n1/d1 < n2/d2 exactly (d1, d2 > 0, all finite and normal, the
 // cross products inside the normal range): n1 d2 and n2 d1 as exact
 // double-double values (product and its FMA error term) compared.  The
