@@ -811,7 +811,12 @@ def run_configs(args, dist, rank, local_rank) -> dict:
         a.min_timed_s = 0.6
         a.no_converge = name != "cc_small"  # configuration 1 is the time-to-drop mesh itself
         w = dict(WORKLOADS[name])
-        r = (run_batched if w["kind"] == "cc_batch" else run_ours)(a, w, dist, rank, local_rank)
+        print(f"bench: configuration {key} ({name})", file=sys.stderr, flush=True)
+        try:
+            r = (run_batched if w["kind"] == "cc_batch" else run_ours)(a, w, dist, rank, local_rank)
+        except (abi.UnsError, RuntimeError) as e:  # recorded, the other configurations still run
+            out[key] = {"workload": w["desc"], "error": str(e)}
+            continue
         if r is None:
             continue
         d = {"workload": w["desc"], "units": r["config"]["units"]}

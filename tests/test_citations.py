@@ -37,11 +37,19 @@ def _ranges(spec: str):
         yield int(a), int(b) if b else int(a)
 
 
+NOT_SOURCE = {"_work", "gpurun_out", "_build", "lib", "baseline", "build", "__pycache__", ".git", ".pytest_cache"}
+
+
 def _tracked():
+    """The repository's text files: git's list where there is a checkout, else
+    a walk of the tree without build, scratch and output folders."""
     out = subprocess.run(["git", "ls-files"], cwd=ROOT, capture_output=True, text=True)
-    if out.returncode != 0:
-        pytest.skip("not a git checkout")
-    return [f for f in out.stdout.split() if f not in SKIP and f.endswith(TEXT) and not f.startswith("_work/")]
+    if out.returncode == 0 and out.stdout.strip():
+        files = out.stdout.split()
+    else:
+        files = [str(f.relative_to(ROOT)) for f in ROOT.rglob("*")
+                 if f.is_file() and not (set(f.relative_to(ROOT).parts[:-1]) & NOT_SOURCE)]
+    return sorted(f for f in files if f not in SKIP and f.endswith(TEXT) and not f.startswith("_work/"))
 
 
 def _citations():
