@@ -388,6 +388,93 @@ class CCPacked:
     def set_precision(self, precision: str) -> None:
         abi.check(self._lib.uns_cc_set_precision(self._h, abi.PREC[precision]), self._lib, "uns_cc_set_precision")
 
+    def _field(self, field: str, rows: int, cols: int) -> np.ndarray:
+        out = np.zeros((rows, cols))
+        abi.check(self._lib.uns_cc_get_field(self._h, abi.CC_FIELDS[field], _dp(out)), self._lib, "uns_cc_get_field")
+        return out
+
+    def forces(self, fbc: list) -> np.ndarray:
+        """Flux-based wall forces (Fx1, Fy1) of every case from the last
+        residual, summed in each case's boundary-face order as the single-case
+        path does (CCFVM/fvresidual.F90:99-100); fbc[i] = case i's boundary
+        codes.  Returns [cases, 2]."""
+        fw = self._field("fwall", int(self.ghost_off[-1]), 4)
+        out = np.zeros((self.n, 2))
+        for i in range(self.n):
+            g0, g1 = int(self.ghost_off[i]), int(self.ghost_off[i + 1])
+            fx = fy = 0.0
+            walls = [k for k in range(g1 - g0) if fbc[i][k] == 1001]
+            for k in walls:  # convective wall fluxes, then the viscous ones (viscous_flux.F90:73-74)
+                fx, fy = fx + fw[g0 + k, 0], fy + fw[g0 + k, 1]
+            if np.any(fw[g0:g1, 2:] != 0.0):
+                for k in walls:
+                    fx, fy = fx - fw[g0 + k, 2], fy - fw[g0 + k, 3]
+            out[i] = fx, fy
+        return out
+
+    def density_residual_l2(self) -> np.ndarray:
+        """L2 of the density residual (component 1 of E, rho, rho u, rho v) of
+        every case's interior cells."""
+        res = self._field("res", int(self.cell_off[-1]), 4)
+        return np.array([np.sqrt(np.mean(res[int(self.cell_off[i]):int(self.cell_off[i]) + self.noc[i], 1] ** 2))
+                         for i in range(self.n)])
+
+    def converge(self, params_list, target: float, max_iter: int, switch_drop: float | None = 1e-4,
+                 chunk: int = 500) -> dict:
+        """Every case from iteration 1 to a `target` drop of its normalised
+        residual (each case stops on the device there, CCFVM/main.F90:57) or
+        `max_iter` iterations.  With `switch_drop`, the handle's current form
+        (the mixed one: FP32 fluxes) runs until every case still running has
+        dropped by `switch_drop` or stopped falling (its FP32 rounding floor),
+        then the whole handle switches to FP64.  A case that has stopped runs
+        one more iteration per chunk (the stop test is re-armed per call),
+        which leaves it converged.  Returns per case the normalised history,
+        the iteration where it reached the target (or None) and the density
+        residual of iteration 1 and of the end."""
+        from . import mesh as _mesh
+        n = self.n
+        hist = [[] for _ in range(n)]
+        norm = [None] * n
+        it = np.zeros(n, dtype=np.int64)
+        prev_cfl = np.zeros(n)
+        reached_at = [None] * n
+        best_prev = np.full(n, np.inf)
+        switched = None
+        total = 0
+        rho1 = None
+        while total < max_iter and not all(r is not None for r in reached_at):
+            m = 1 if total == 0 else min(chunk, max_iter - total)
+            cfl = np.stack([_mesh.cfl_schedule(params_list[i], int(it[i]) + 1, m, "cc", float(prev_cfl[i]))
+                            for i in range(n)])
+            h, done = self.iterate(cfl, first_iter=(total == 0))
+            if total == 0:
+                rho1 = self.density_residual_l2()
+            best = np.full(n, np.inf)
+            for i in range(n):
+                if done[i] == 0:
+                    continue
+                if norm[i] is None:
+                    norm[i] = h[i][0]
+                f = h[i] / norm[i]
+                if reached_at[i] is None:
+                    hist[i].extend(f.tolist())
+                    if done[i] < m or f[-1] <= target:
+                        reached_at[i] = int(it[i] + done[i])
+                it[i] += done[i]
+                prev_cfl[i] = cfl[i, done[i] - 1]
+                best[i] = f.min()
+            total += m
+            if switch_drop is not None and switched is None and total > 1:
+                live = [i for i in range(n) if reached_at[i] is None]
+                floor = [best[i] <= switch_drop or (best[i] < 100 * switch_drop and best[i] > 0.9 * best_prev[i])
+                         for i in live]
+                if all(floor):
+                    self.set_precision("fp64")
+                    switched = total
+                best_prev = np.minimum(best_prev, best)
+        return {"history": [np.array(x) for x in hist], "reached_at": reached_at, "switched_at": switched,
+                "iterations": total, "density_l2_first": rho1, "density_l2_last": self.density_residual_l2()}
+
     def profile(self, cfl: float, reps: int = 3) -> dict:
         """Average device time [ms] of each phase of one iteration of all the
         cases (uns_cc_profile; one CFL for every case)."""
