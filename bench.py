@@ -448,18 +448,22 @@ def batch_instances(w: dict):
     return out
 
 
-def batch_convergence(w: dict, count: int, max_iter: int = 20000, target: float = 1e-8) -> dict:
-    """A seeded subset of the batched workload's instances (`count` of them,
-    spread evenly over the seeded list, so over the size range) run to a
-    `target` drop of the normalised residual or `max_iter` iterations, twice
-    on one packed handle each: the mixed form with the precision ramp (FP32
-    fluxes until every running case has reached its FP32 floor, then FP64)
-    and plain FP64.  Per instance: the iteration of the drop, the density
-    residual's drop, C_L and C_D of both runs and their difference."""
+def batch_convergence(w: dict, count: int, max_iter: int = 20000, target: float = 1e-8, smallest: bool = False) -> dict:
+    """A seeded subset of the batched workload's instances (`count` of them:
+    spread evenly over the seeded list, so over the size range, or the
+    smallest) run to a `target` drop of the normalised residual or `max_iter`
+    iterations, twice on one packed handle each: the mixed form with the
+    precision ramp (FP32 fluxes until every running case has reached its FP32
+    floor, then FP64) and plain FP64.  Per instance: the iteration of the
+    drop, the density residual's drop, C_L and C_D of both runs and their
+    difference."""
     from unsflow2d_gb300.solver import CCPacked
     inst = batch_instances(w)
-    step = max(1, len(inst) // max(count, 1))
-    sel = [inst[k] for k in range(0, len(inst), step)][:count]
+    if smallest:
+        sel = sorted(inst, key=lambda x: x[0] * x[1])[:count]
+    else:
+        step = max(1, len(inst) // max(count, 1))
+        sel = [inst[k] for k in range(0, len(inst), step)][:count]
     meshes = [mesh.CCMesh.airfoil(ni, nj, 0.12, 20.0, w["dwall"]) for ni, nj, _ in sel]
     fbc = [np.asarray(m.arrays["fbc"])[m.arrays["nfi"]:] for m in meshes]
     cells = np.array([int(m.arrays["noc"]) for m in meshes])
@@ -489,7 +493,8 @@ def batch_convergence(w: dict, count: int, max_iter: int = 20000, target: float 
                     "CD_mixed": a["cl_cd"][i][1], "CD_fp64": f["cl_cd"][i][1],
                     "dCL": abs(a["cl_cd"][i][0] - f["cl_cd"][i][0]), "dCD": abs(a["cl_cd"][i][1] - f["cl_cd"][i][1])})
     both = [q for q in per if q["mixed_reached_at"] is not None and q["fp64_reached_at"] is not None]
-    return {"instances": len(sel), "of": len(inst), "target_drop": target, "max_iterations": max_iter,
+    return {"instances": len(sel), "of": len(inst), "selection": "smallest" if smallest else "spread over the list",
+            "target_drop": target, "max_iterations": max_iter,
             "reached": {"mixed_ramp": sum(q["mixed_reached_at"] is not None for q in per),
                         "fp64": sum(q["fp64_reached_at"] is not None for q in per)},
             "fp64_from_iteration": runs["mixed"]["r"]["switched_at"],
@@ -596,7 +601,11 @@ def run_batched(args, w, dist, rank, local_rank) -> dict | None:
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": None, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                      "face_kernel": face},
-        **({"convergence": batch_convergence(w, args.batch_converge)} if packed and args.batch_converge > 0 else {}),
+        # configuration 4's stop rule (1e-8 drop or 20k iterations) on a seeded
+        # subset, and the smallest instances run on to the 1e-8 drop
+        **({"convergence": batch_convergence(w, args.batch_converge),
+            "convergence_to_1e-8": batch_convergence(w, 4, max_iter=150000, smallest=True)}
+           if packed and args.batch_converge > 0 else {}),
     }
 
 
@@ -910,7 +919,7 @@ def main():
                     help="skip the mixed forms' FP64 comparison run (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default block sizes (profiling runs: no tuning launches before the captured ones)")
-    ap.add_argument("--batch-converge", type=int, default=16,
+    ap.add_argument("--batch-converge", type=int, default=8,
                     help="instances of the batched workload run to a 1e-8 drop (mixed ramp and FP64); 0 skips it")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the other configurations that the default one-GPU run measures after the headline")

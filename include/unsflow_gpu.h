@@ -97,6 +97,11 @@ int uns_cc_find_cl_cd(uns_cc_handle* h, double xref, double yref, double* coef, 
  * cells from the current state: out[2k], out[2k+1] = min, max of density, u,
  * v, pressure, temperature, Mach number, entropy log10(p / rho^gamma / ent_inf). */
 int uns_cc_screen_minmax(uns_cc_handle* h, double* out);
+/* tecplt's vertex table (CCFVM/main.F90:417-480) on the device: the avg_c2v
+ * vertex average of the current cell primitives and viscosity, then per
+ * vertex x, y, density, u, v, Mach, pressure, temperature, entropy, |V|, mu:
+ * out[nop][11].  The solver's own vertex values are not changed. */
+int uns_cc_tecplt(uns_cc_handle* h, double* out);
 /* Fast path: `niter` whole iterations of the main loop body
  * (CCFVM/main.F90:59-115) replayed from one captured CUDA graph.  cfl[k] is
  * the CFL of iteration k; fres_raw[k] receives that iteration's raw residual
@@ -237,6 +242,14 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
  * sizes: faces, vertices, cell gradient. */
 int uns_cc_autotune(uns_cc_handle* h, int reps, int* blocks);
 int uns_nc_profile(uns_nc_handle* h, double cfl, int reps, double* ms, const char** names, int nphase);
+/* NCFVM tecplt's vertex table (NCFVM/main.f90:190-233): per node x, y and the
+ * primitives of the last save_old (rho, u, v, p) with the Mach number:
+ * out[nop][7]. */
+int uns_nc_tecplt(uns_nc_handle* h, double* out);
+/* NCFVM screen's min/max diagnostics (NCFVM/main.f90:115-187) over the nodes
+ * from the current state: out[6][2] = min, max of density, u, v, pressure,
+ * Mach number, entropy. */
+int uns_nc_screen_minmax(uns_nc_handle* h, double* out);
 /* Bound of every wait in the handle's LU-SGS sweeps, in device clock cycles
  * (default 4e9, about 2 s); a sweep whose wait runs out returns
  * UNS_ERR_TIMEOUT with the context intact.  No reference counterpart (the

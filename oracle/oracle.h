@@ -51,6 +51,8 @@ int oracle_cc_set(oracle_cc* o, int field, const double* in);
 int oracle_cc_find_cl_cd(oracle_cc* o, double xref, double yref, double* coef, double* wall, int* nwall);
 /* screen's min/max diagnostics (main.F90:187-221): out[14]. */
 int oracle_cc_screen_minmax(oracle_cc* o, double* out);
+/* tecplt's vertex table (main.F90:417-480) after avg_c2v: out[nop][11]. */
+int oracle_cc_tecplt(oracle_cc* o, double* out);
 
 /* Complex-step instance of the CCFVM oracle (oracle_cc_cs.cpp): the same
  * routines on a complex scalar whose branches follow the real part.  Inputs
@@ -78,6 +80,10 @@ int oracle_nc_fvresidual(oracle_nc* o, double cfl);     /* fvresidual.f90:4-85  
 int oracle_nc_rk_stage(oracle_nc* o, int irk);          /* main.f90:59-80       */
 int oracle_nc_lusgs(oracle_nc* o, double cfl);          /* lusgs.f90:4-157        */
 int oracle_nc_residue(oracle_nc* o, double* fres_raw, double* fresi, int* iresi); /* common.f90:108-154 */
+/* tecplt's vertex table (NCFVM/main.f90:190-233): out[nop][7]; screen's
+ * min/max (NCFVM/main.f90:115-187): out[12]. */
+int oracle_nc_tecplt(oracle_nc* o, double* out);
+int oracle_nc_screen_minmax(oracle_nc* o, double* out);
 int oracle_nc_iteration(oracle_nc* o, double cfl, double* fres_raw, double* fresi);
 int oracle_nc_get(oracle_nc* o, int field, double* out);
 /* Test hook: overwrite QC, QP, GRAD or PHI. */

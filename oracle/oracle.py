@@ -53,7 +53,8 @@ def lib() -> C.CDLL:
             "oracle_cc_cs_get": ([vp, i32, dp, dp], i32), "oracle_cc_cs_iteration": ([vp, C.c_double], i32),
             "oracle_cc_cs_forces": ([vp, dp, dp], i32),
             "oracle_cc_find_cl_cd": ([vp, C.c_double, C.c_double, dp, dp, ip], i32),
-            "oracle_cc_screen_minmax": ([vp, dp], i32),
+            "oracle_cc_screen_minmax": ([vp, dp], i32), "oracle_cc_tecplt": ([vp, dp], i32),
+            "oracle_nc_tecplt": ([vp, dp], i32), "oracle_nc_screen_minmax": ([vp, dp], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(L, fn)
@@ -144,6 +145,11 @@ class OracleCC(_Oracle):
         self._call("screen_minmax", _dp(out))
         return out.reshape(7, 2)
 
+    def tecplt(self):
+        out = np.zeros((self.m["nop"], 11))
+        self._call("tecplt", _dp(out))
+        return out
+
     def con2prim(self): self._call("con2prim")
     def avg_c2v(self): self._call("avg_c2v")
     def save_old(self): self._call("save_old")
@@ -213,6 +219,16 @@ class OracleNC(_Oracle):
         f, fi = C.c_double(), C.c_double()
         self._call("iteration", C.c_double(cfl), C.byref(f), C.byref(fi))
         return f.value, fi.value
+
+    def tecplt(self):
+        out = np.zeros((self.nop, 7))
+        self._call("tecplt", _dp(out))
+        return out
+
+    def screen_minmax(self):
+        out = np.zeros(12)
+        self._call("screen_minmax", _dp(out))
+        return out.reshape(6, 2)
 
 
 class OracleCCComplexStep:

@@ -168,4 +168,9 @@ int oracle_cc_screen_minmax(oracle_cc* o, double* out) {
     return UNS_OK;
 }
 
+int oracle_cc_tecplt(oracle_cc* o, double* out) {
+    cc_tecplt(o->s, out);
+    return UNS_OK;
+}
+
 }  // extern "C"

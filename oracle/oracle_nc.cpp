@@ -455,6 +455,41 @@ int oracle_nc_iteration(oracle_nc* o, double cfl, double* fres, double* fresi) {
     return oracle_nc_residue(o, fres, fresi, nullptr);
 }
 
+// tecplt's vertex table (NCFVM/main.f90:190-233): per node x, y and the
+// primitives of the last save_old, rho, u, v, p, Mach.
+int oracle_nc_tecplt(oracle_nc* o, double* out) {
+    NC& s = o->s;
+    for (int i = 0; i < s.nop; ++i) {
+        const double* q = &s.qp[(size_t)i * 4];
+        double ro = q[0], uo = q[1], vo = q[2], po = q[3];
+        double q2 = uo * uo + vo * vo;
+        double mach = std::sqrt(q2 * ro / (s.gamma * po));
+        double* r = out + (size_t)i * 7;
+        r[0] = s.px[i]; r[1] = s.py[i]; r[2] = ro; r[3] = uo; r[4] = vo; r[5] = po; r[6] = mach;
+    }
+    return UNS_OK;
+}
+
+// screen's min/max diagnostics (NCFVM/main.f90:115-187) over the nodes from
+// the current conserved state: out = min, max of density, u, v, pressure,
+// Mach number, entropy.
+int oracle_nc_screen_minmax(oracle_nc* o, double* out) {
+    NC& s = o->s;
+    double lo[6], hi[6];
+    for (int k = 0; k < 6; ++k) { lo[k] = 1.0e10; hi[k] = -1.0e10; }
+    for (int is = 0; is < s.nop; ++is) {
+        Prim r;
+        con2prim(s, &s.qc[(size_t)is * 4], r);
+        double q2 = r.u * r.u + r.v * r.v;
+        double mach = std::sqrt(q2 * r.rho / (s.gamma * r.p));
+        double ent = std::log10(r.p / std::pow(r.rho, s.gamma) / s.ent_inf);
+        const double x[6] = {r.rho, r.u, r.v, r.p, mach, ent};
+        for (int k = 0; k < 6; ++k) { lo[k] = std::min(lo[k], x[k]); hi[k] = std::max(hi[k], x[k]); }
+    }
+    for (int k = 0; k < 6; ++k) { out[2 * k] = lo[k]; out[2 * k + 1] = hi[k]; }
+    return UNS_OK;
+}
+
 int oracle_nc_get(oracle_nc* o, int field, double* out) {
     NC& s = o->s;
     switch (field) {

@@ -282,3 +282,22 @@ def test_plot3d_rejects_bad_grids(tmp_path):
     open_grid.write_text(f"1\n{nx} {ny} 1\n" + "\n".join(map(str, xs + ys + [0.0] * (nx * ny))) + "\n")
     with pytest.raises(abi.UnsError):
         mesh.CCMesh.plot3d(open_grid)
+
+
+def test_tecplt_writer_layout(tmp_path):
+    """tecplt.dat as the reference lays it out: header, N/E line, node rows
+    of at most seven values, 1-based triangle vertex lists."""
+    m = mesh.CCMesh.airfoil(8, 4)
+    cells = mesh.cc_cell_vertices(m.arrays)
+    assert cells.shape == (m.arrays["noc"], 3) and cells.min() == 0 and cells.max() < m.arrays["nop"]
+    table = np.arange(m.arrays["nop"] * 11, dtype=float).reshape(-1, 11)
+    path = tmp_path / "tecplt.dat"
+    mesh.write_tecplt(path, table, [f"v{k}" for k in range(11)], cells)
+    lines = path.read_text().splitlines()
+    assert lines[2].strip() == "ZONE F=FEPOINT,ET=TRIANGLE"
+    assert lines[3].strip() == f"N={m.arrays['nop']},E={m.arrays['noc']}"
+    nodes = lines[4:4 + 2 * m.arrays["nop"]]
+    vals = np.array([float(x) for ln in nodes for x in ln.split()]).reshape(-1, 11)
+    assert np.array_equal(vals, table)
+    elems = np.array([[int(x) for x in ln.split()] for ln in lines[4 + 2 * m.arrays["nop"]:]])
+    assert np.array_equal(elems, cells + 1)

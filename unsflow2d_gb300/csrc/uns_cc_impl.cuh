@@ -167,6 +167,7 @@ struct uns_cc_handle {
     long long res_gen = -1;
     uns::CCAdj* adj = nullptr;  // discrete-adjoint state, created by uns_cc_adjoint_prepare
     double* d_post = nullptr;   // post-processing scratch (uns_cc_post.cu), created on first use
+    double* d_tec = nullptr;    // tecplt vertex table (uns_cc_post.cu), created on first use
 
     template <class T>
     int alloc(T*& p, size_t n) {

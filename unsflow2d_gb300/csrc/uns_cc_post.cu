@@ -102,6 +102,38 @@ __global__ void k_screen_minmax(CCView v, double ent_inf, unsigned long long* mm
         for (int k = 0; k < 7; ++k) { atomicMin(&mm[2 * k], lo[k]); atomicMax(&mm[2 * k + 1], hi[k]); }
 }
 
+// tecplt's vertex table (CCFVM/main.F90:417-480): the avg_c2v vertex average
+// (the FP64 k_vertex_avg's operations and order, plus the viscosity as
+// average.F90:23-28 forms it) and per vertex x, y, density, u, v, Mach,
+// pressure, temperature, entropy, |V|, mu.  The solver's own vertex values
+// are left untouched.
+__global__ void __launch_bounds__(kBlock) k_tecplt(CCView v, double ent_inf, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nop) return;
+    double wt = 0.0, c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0, c4 = 0.0, c5 = 0.0;
+    for (int k = v.v2c_off[i]; k < v.v2c_off[i + 1]; ++k) {
+        const int c = v.v2c[k];
+        const double w = v.v2c_wt[k];
+        wt = wt + w;
+        const double4 q = v.qp[c];
+        c0 = c0 + q.x * w;
+        c1 = c1 + q.y * w;
+        c2 = c2 + q.z * w;
+        c3 = c3 + q.w * w;
+        c4 = c4 + v.qT[c] * w;
+        c5 = c5 + v.mul[c] * w;
+    }
+    const double ro = c0 / wt, uo = c1 / wt, vo = c2 / wt, po = c3 / wt, to = c4 / wt, mu = c5 / wt;
+    const double vmag = sqrt(uo * uo + vo * vo);
+    const double q2 = uo * uo + vo * vo;
+    const double mach = sqrt(q2 * ro / (v.g.gamma * po));
+    const double entropy = log10(po / pow(ro, v.g.gamma) / ent_inf);
+    const double2 x = v.pxy[i];
+    double* o = out + (size_t)i * 11;
+    o[0] = x.x; o[1] = x.y; o[2] = ro; o[3] = uo; o[4] = vo; o[5] = mach;
+    o[6] = po; o[7] = to; o[8] = entropy; o[9] = vmag; o[10] = mu;
+}
+
 __global__ void k_screen_init(unsigned long long* mm) {
     const int k = threadIdx.x;
     if (k < 7) { mm[2 * k] = ~0ULL; mm[2 * k + 1] = 0ULL; }
@@ -146,6 +178,19 @@ int uns_cc_find_cl_cd(uns_cc_handle* h, double xref, double yref, double* coef, 
     coef[4] = (fy1 * g.v_inf + fx1 * g.u_inf) / dyna;
     if (wall) std::copy(r.begin() + 4, r.begin() + 4 + 4 * (size_t)n, wall);
     if (nwall) *nwall = n;
+    return cc_check_dev_err(h);
+}
+
+int uns_cc_tecplt(uns_cc_handle* h, double* out) {
+    if (!h || !out) { set_last_error("uns_cc_tecplt: null argument"); return UNS_ERR_ARG; }
+    if (h->v.ninst) { set_last_error("uns_cc_tecplt: a packed handle has no single vertex table"); return UNS_ERR_ARG; }
+    const CCView& v = h->v;
+    if (!h->d_tec) { int rc = h->alloc(h->d_tec, 11 * (size_t)v.nop); if (rc) return rc; }
+    const double ent_inf = v.g.p_inf / std::pow(v.g.r_inf, v.g.gamma);
+    k_tecplt<<<std::max(1, nblocks(v.nop)), kBlock, 0, h->stream>>>(v, ent_inf, h->d_tec);
+    UNS_CUDA(cudaGetLastError());
+    UNS_CUDA(cudaMemcpyAsync(out, h->d_tec, sizeof(double) * 11 * (size_t)v.nop, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
     return cc_check_dev_err(h);
 }
 

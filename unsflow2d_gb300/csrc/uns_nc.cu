@@ -992,6 +992,50 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
     }
 }
 
+// tecplt's vertex table (NCFVM/main.f90:190-233): per node x, y and the
+// primitives of the last save_old (rho, u, v, p) with the Mach number.
+__global__ void __launch_bounds__(kBlock) k_nc_tecplt(NCView v, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nop) return;
+    const double4 q = v.qp[i];
+    const double2 x = v.pxy[i];
+    const double q2 = q.y * q.y + q.z * q.z;
+    const double mach = sqrt(q2 * q.x / (v.g.gamma * q.w));
+    double* o = out + (size_t)i * 7;
+    o[0] = x.x; o[1] = x.y; o[2] = q.x; o[3] = q.y; o[4] = q.z; o[5] = q.w; o[6] = mach;
+}
+
+// screen's min/max (NCFVM/main.f90:115-187) over the nodes from the current
+// conserved state: density, u, v, pressure, Mach number, entropy; exact and
+// order-free (warp reduction, then encoded atomics).
+__global__ void __launch_bounds__(kBlock) k_nc_screen(NCView v, double ent_inf, unsigned long long* mm) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long lo[6], hi[6];
+    for (int k = 0; k < 6; ++k) { lo[k] = ~0ULL; hi[k] = 0ULL; }
+    if (i < v.nop) {
+        const double4 q = v.qc[i];
+        const Prim r = con2prim(v.g, q.x, q.y, q.z, q.w);
+        const double q2 = r.u * r.u + r.v * r.v;
+        const double mach = sqrt(q2 * r.rho / (v.g.gamma * r.p));
+        const double ent = log10(r.p / pow(r.rho, v.g.gamma) / ent_inf);
+        const double x[6] = {r.rho, r.u, r.v, r.p, mach, ent};
+        for (int k = 0; k < 6; ++k) { lo[k] = enc_ord(x[k]); hi[k] = lo[k]; }
+    }
+    for (int k = 0; k < 6; ++k) {
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long a = __shfl_xor_sync(0xffffffffu, lo[k], o), c = __shfl_xor_sync(0xffffffffu, hi[k], o);
+            lo[k] = a < lo[k] ? a : lo[k];
+            hi[k] = c > hi[k] ? c : hi[k];
+        }
+    }
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 6; ++k) { atomicMin(&mm[2 * k], lo[k]); atomicMax(&mm[2 * k + 1], hi[k]); }
+}
+
+__global__ void k_nc_screen_init(unsigned long long* mm) {
+    if (threadIdx.x < 6) { mm[2 * threadIdx.x] = ~0ULL; mm[2 * threadIdx.x + 1] = 0ULL; }
+}
+
 __global__ void k_nc_initialize(NCView v, double4 qinf, double phi0) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.nop) return;
@@ -1021,6 +1065,8 @@ struct uns_nc_handle {
     int* d_done = nullptr;
     double* d_fres1 = nullptr;
     double* d_scalar = nullptr;
+    double* d_tec = nullptr;              // tecplt vertex table, created on first use
+    unsigned long long* d_mm = nullptr;   // screen min/max slots, created on first use
 
     template <class T>
     int alloc(T*& p, size_t n) {
@@ -1449,6 +1495,31 @@ int uns_nc_iterate(uns_nc_handle* h, int niter, const double* cfl, int first_ite
     UNS_CUDA(cudaMemcpyAsync(&it, h->d_iter, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     if (done_iters) *done_iters = it;
+    return check_err_nc(h);
+}
+
+int uns_nc_tecplt(uns_nc_handle* h, double* out) {
+    if (!h || !out) { set_last_error("uns_nc_tecplt: null argument"); return UNS_ERR_ARG; }
+    if (!h->d_tec) { int rc = h->alloc(h->d_tec, 7 * (size_t)h->v.nop); if (rc) return rc; }
+    k_nc_tecplt<<<nblocks(h->v.nop), kBlock, 0, h->stream>>>(h->v, h->d_tec);
+    UNS_CUDA(cudaGetLastError());
+    UNS_CUDA(cudaMemcpyAsync(out, h->d_tec, sizeof(double) * 7 * (size_t)h->v.nop, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    return check_err_nc(h);
+}
+
+int uns_nc_screen_minmax(uns_nc_handle* h, double* out) {
+    if (!h || !out) { set_last_error("uns_nc_screen_minmax: null argument"); return UNS_ERR_ARG; }
+    if (!h->d_mm) { int rc = h->alloc(h->d_mm, 12); if (rc) return rc; }
+    const double ent_inf = h->v.g.p_inf / std::pow(h->v.g.r_inf, h->v.g.gamma);
+    k_nc_screen_init<<<1, 32, 0, h->stream>>>(h->d_mm);
+    UNS_CUDA(cudaGetLastError());
+    k_nc_screen<<<nblocks(h->v.nop), kBlock, 0, h->stream>>>(h->v, ent_inf, h->d_mm);
+    UNS_CUDA(cudaGetLastError());
+    unsigned long long e[12];
+    UNS_CUDA(cudaMemcpyAsync(e, h->d_mm, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 12; ++k) out[k] = dec_ord(e[k]);
     return check_err_nc(h);
 }
 

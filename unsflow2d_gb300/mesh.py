@@ -139,3 +139,38 @@ def run_main(flo_inp: str, outdir: str, kind: str = "cc", mode: int = 1) -> tupl
     fn = lib.uns_host_cc_main if kind == "cc" else lib.uns_host_nc_main
     abi.check(fn(str(flo_inp).encode(), str(outdir).encode(), mode, C.byref(it), C.byref(fr)), lib, "main")
     return it.value, fr.value
+
+
+def cc_cell_vertices(arrays: dict) -> np.ndarray:
+    """Vertices of each interior cell (0-based), from its faces' end points in
+    c2f order: the first face's two points, then the others' new points."""
+    off, c2f, fp1, fp2 = arrays["c2f_off"], arrays["c2f"], arrays["fp1"], arrays["fp2"]
+    out = []
+    for i in range(int(arrays["noc"])):
+        vs: list[int] = []
+        for f in c2f[off[i]:off[i + 1]]:
+            for p in (int(fp1[f]), int(fp2[f])):
+                if p not in vs:
+                    vs.append(p)
+        out.append(vs)
+    return np.array(out, dtype=np.int64)
+
+
+def write_tecplt(path, table: np.ndarray, variables: list[str], elements: np.ndarray | None = None) -> None:
+    """The reference's tecplt.dat (CCFVM/main.F90:417-480, NCFVM/main.f90:
+    190-233) from a device vertex table (uns_cc_tecplt / uns_nc_tecplt): node
+    rows written 7 values per line (format 1x,7(f15.6,2x), reused for longer
+    rows) and, when given, the elements' 1-based vertex lists."""
+    with open(path, "w") as f:
+        f.write(' TITLE = "flo2d output" \n')
+        f.write(" VARIABLES=" + ",".join(f'"{v}"' for v in variables) + "\n")
+        ne = 0 if elements is None else len(elements)
+        et = "TRIANGLE" if elements is not None and elements.shape[1] == 3 else "quadrilateral"
+        f.write(f" ZONE F=FEPOINT,ET={et}\n" if ne else " ZONE F=POINT\n")
+        f.write(f" N={len(table)},E={ne}\n")
+        for row in table:
+            for k in range(0, len(row), 7):
+                f.write(" " + "".join(f"{x:15.6f}  " for x in row[k:k + 7]) + "\n")
+        if elements is not None:
+            for e in elements:
+                f.write(" " + " ".join(str(int(x) + 1) for x in e) + "\n")

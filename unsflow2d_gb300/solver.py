@@ -180,6 +180,12 @@ class CCSolver(_Solver):
         self._call("screen_minmax", _dp(out))
         return out.reshape(7, 2)
 
+    def tecplt(self) -> np.ndarray:
+        """tecplt's [nop][11] vertex table: x, y, density, u, v, Mach, p, T, entropy, |V|, mu."""
+        out = np.zeros((self.m["nop"], 11))
+        self._call("tecplt", _dp(out))
+        return out
+
     def cl_cd(self) -> tuple[float, float]:
         """Flux-based C_L, C_D of the last residual (CCFVM/main.F90:348-353)."""
         fx, fy = self.forces()
@@ -273,6 +279,18 @@ class NCSolver(_Solver):
         f, fi, ii = C.c_double(), C.c_double(), C.c_int()
         self._call("residue", C.byref(f), C.byref(fi), C.byref(ii))
         return f.value, fi.value, ii.value
+
+    def tecplt(self) -> np.ndarray:
+        """tecplt's [nop][7] vertex table: x, y, rho, u, v, p, Mach."""
+        out = np.zeros((self.nop, 7))
+        self._call("tecplt", _dp(out))
+        return out
+
+    def screen_minmax(self) -> np.ndarray:
+        """screen's [6][2] min/max of density, u, v, p, Mach, entropy."""
+        out = np.zeros(12)
+        self._call("screen_minmax", _dp(out))
+        return out.reshape(6, 2)
 
     def iteration(self, cfl: float) -> tuple[float, float, int]:
         """One main-loop iteration (NCFVM/main.f90:53-86)."""
