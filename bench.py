@@ -743,7 +743,7 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None,
+        "scaling": "weak", "vs_baseline": None, "gpu_library": abi.gpu_library_name(),
         "dtype": "f64" if p.precision == abi.PREC["fp64"] else "f32-face/f64-accumulate",
         "data": "synthetic: seeded analytic-airfoil O-mesh, uniform freestream start",
         "config": {"workload": w["desc"], "units": units, "edges_or_faces": int(m["nof"] if kind == "nc" else m["nfi"] + m["nbf"]),
@@ -894,6 +894,25 @@ def run_configs(args, dist, rank, local_rank) -> dict:
         if r["config"].get("block_sizes"):
             d["block_sizes"] = r["config"]["block_sizes"]
         out[key] = d
+    # the FP64 forms again with multiply-add contraction (the other build of
+    # the GPU library, chosen per process): the cost of bit-exactness
+    fma = {}
+    for key, name in (("2", "nc"), ("3_fp64", "cc")):
+        cmd = [sys.executable, str(ROOT / "bench.py"), "--workload", name, "--steps", str(args.steps), "--warmup",
+               str(args.warmup), "--no-configs", "--no-cpu-baseline", "--no-e2e", "--no-converge", "--no-accuracy"]
+        r = subprocess.run(cmd, capture_output=True, text=True, env=dict(os.environ, UNSFLOW_FP64_FMA="1"),
+                           timeout=1200)
+        try:
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            fma[key] = {"workload": d["config"]["workload"], "gpu_library": d.get("gpu_library"), "value": d["value"],
+                        "ms_per_step": d["ms_per_step"], "clocks": d["clocks"],
+                        "kernels_ms_per_iter": {k: v["ms_per_iter"] for k, v in d["kernels"].items()}}
+            plain_v = out.get(key, {}).get("value") if key != "2" else None
+            if plain_v:
+                fma[key]["speedup_vs_bit_exact"] = round(d["value"] / plain_v, 3)
+        except Exception:
+            fma[key] = {"error": (r.stderr or "")[-400:]}
+    out["fp64_fma"] = fma
     plain = out.get("3_fp64", {}).get("value")
     if plain:
         for key in ("3", "4"):
@@ -942,6 +961,9 @@ def main():
         configs = run_configs(args, dist, rank, local_rank)
         if out is not None:
             out["configs"] = configs
+            fma2 = configs.get("fp64_fma", {}).get("2", {})
+            if fma2.get("value"):
+                fma2["speedup_vs_bit_exact"] = round(fma2["value"] / out["value"], 3)
     if out is not None:
         print(json.dumps(out))
     if dist is not None:

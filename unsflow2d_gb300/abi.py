@@ -7,6 +7,7 @@ no CPU fallback for the GPU library.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
@@ -180,8 +181,14 @@ def _load(name: str) -> C.CDLL:
     return lib
 
 
+def gpu_library_name() -> str:
+    """The GPU library this process uses: the bit-exact build, or with
+    UNSFLOW_FP64_FMA=1 the one whose FP64 kernels contract multiply-adds."""
+    return "unsflow_gpu_fma" if os.environ.get("UNSFLOW_FP64_FMA", "0") == "1" else "unsflow_gpu"
+
+
 def gpu_lib() -> C.CDLL:
-    lib = _load("unsflow_gpu")
+    lib = _load(gpu_library_name())
     if not getattr(lib, "_typed", False):
         vp, i32, dp = C.c_void_p, C.c_int, _D
         pp = C.POINTER(C.c_void_p)

@@ -7,6 +7,10 @@
                         FLO.DAT I/O (include/unsflow_host.h); no GPU dependency.
     libunsflow_driver.so  the main programs (uns_host_*_main in unsflow_host.h)
                         on the two libraries above.
+    libunsflow_gpu_fma.so the GPU library again with FP64 multiply-add
+                        contraction: the same entry points, faster FP64
+                        kernels, results within rounding of the bit-exact
+                        build (chosen per process, UNSFLOW_FP64_FMA=1).
 
 All three land in unsflow2d_gb300/lib/.  Translation units compile in parallel; host
 code is built with -ffp-contract=off so x86 and Arm hosts round identically.
@@ -34,6 +38,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # and square roots are correctly rounded either way.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
+# The contracted FP64 build: the compiler may fuse a multiply and an add into
+# one FMA (one rounding instead of two).
+NVCC_FMA_FLAGS = [f if f != "--fmad=false" else "--fmad=true" for f in NVCC_FLAGS]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
              "-I", str(INCLUDE), "-I", str(CSRC / "host")]
 
@@ -72,7 +79,9 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     host_so = LIB / "libunsflow_host.so"
     driver_so = LIB / "libunsflow_driver.so"
     deps = _deps()
-    out = {"gpu": gpu_so, "host": host_so, "driver": driver_so}
+    fma_so = LIB / "libunsflow_gpu_fma.so"
+    out = {"gpu": gpu_so, "host": host_so, "driver": driver_so, "gpu_fma": fma_so}
+    (OBJ / "fma").mkdir(exist_ok=True)
     if not force and all(_newer(f, deps) for f in out.values()):
         return out
     nv = nvcc()
@@ -80,14 +89,19 @@ def build(force: bool = False, verbose: bool = False) -> dict[str, Path]:
     for src in GPU_SOURCES:
         o = OBJ / (Path(src).stem + ".o")
         jobs.append([nv, *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(o)])
+    for src in GPU_SOURCES:
+        o = OBJ / "fma" / (Path(src).stem + ".o")
+        jobs.append([nv, *ARCH, *NVCC_FMA_FLAGS, "-c", str(CSRC / src), "-o", str(o)])
     for src in HOST_SOURCES + DRIVER_SOURCES:
         o = OBJ / (Path(src).stem + ".o")
         jobs.append(["g++", *CXX_FLAGS, "-c", str(CSRC / src), "-o", str(o)])
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(max(os.cpu_count() or 8, 8), len(jobs))) as ex:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()
     gpu_objs = [str(OBJ / (Path(s).stem + ".o")) for s in GPU_SOURCES]
     _run([nv, *ARCH, "-shared", "-Xcompiler", "-fPIC", *gpu_objs, "-o", str(gpu_so)])
+    fma_objs = [str(OBJ / "fma" / (Path(s).stem + ".o")) for s in GPU_SOURCES]
+    _run([nv, *ARCH, "-shared", "-Xcompiler", "-fPIC", *fma_objs, "-o", str(fma_so)])
     host_objs = [str(OBJ / (Path(s).stem + ".o")) for s in HOST_SOURCES]
     _run(["g++", "-shared", *host_objs, "-o", str(host_so)])
     drv_objs = [str(OBJ / (Path(s).stem + ".o")) for s in DRIVER_SOURCES]
