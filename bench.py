@@ -862,7 +862,7 @@ def run_reference(args, w) -> dict:
 # in the plain FP64 form, the denominator of the mixed and batched speed-ups.
 CONFIG_RUNS = [("1", "cc_small"), ("3_fp64", "cc"), ("3", "cc_mixed"), ("4", "cc_batched"), ("5", "cc_adjoint")]
 SUMMARY_KEYS = ("value", "unit", "ms_per_step", "steps", "dtype", "gpu_launches", "clocks", "roofline",
-                "accuracy_vs_fp64", "adjoint", "time_to_1e-8")
+                "accuracy_vs_fp64", "adjoint", "time_to_1e-8", "convergence", "convergence_to_1e-8")
 
 
 def run_configs(args, dist, rank, local_rank) -> dict:
