@@ -443,8 +443,9 @@ class CCPacked:
         residual (each case stops on the device there, CCFVM/main.F90:57) or
         `max_iter` iterations.  With `switch_drop`, the handle's current form
         (the mixed one: FP32 fluxes) runs until every case still running has
-        dropped by `switch_drop` or stopped falling (its FP32 rounding floor),
-        then the whole handle switches to FP64.  A case that has stopped runs
+        dropped by `switch_drop` or stopped falling over a chunk (its FP32
+        rounding floor, or a stall at any level), then the whole handle
+        switches to FP64.  A case that has stopped runs
         one more iteration per chunk (the stop test is re-armed per call),
         which leaves it converged.  Returns per case the normalised history,
         the iteration where it reached the target (or None) and the density
@@ -484,8 +485,10 @@ class CCPacked:
             total += m
             if switch_drop is not None and switched is None and total > 1:
                 live = [i for i in range(n) if reached_at[i] is None]
-                floor = [best[i] <= switch_drop or (best[i] < 100 * switch_drop and best[i] > 0.9 * best_prev[i])
-                         for i in live]
+                # a case is done with the FP32 form once it has dropped by
+                # switch_drop or stopped falling, at whatever level (a case
+                # held up by a limiter cycle must not keep the others in FP32)
+                floor = [best[i] <= switch_drop or best[i] > 0.9 * best_prev[i] for i in live]
                 if all(floor):
                     self.set_precision("fp64")
                     switched = total
