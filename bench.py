@@ -358,6 +358,42 @@ def time_to_drop(w: dict, target: float = 1e-8) -> dict:
     return out
 
 
+def converge_history(w: dict, max_iter: int, target: float, every: int = 500) -> dict:
+    """The workload's case from freestream until the density residual has
+    dropped by `target` or `max_iter` iterations: every `every` iterations the
+    normalised all-variable residual (FLO.RES), the density-only drop and the
+    wall time.  For solves far longer than a benchmark step."""
+    from unsflow2d_gb300.solver import CCSolver, NCSolver
+    kind = w["kind"]
+    m = build_mesh(w)
+    units = units_of(w, m)
+    p = abi.make_params(**dict(w["params"], min_res=0.0))
+    S = NCSolver if kind == "nc" else CCSolver
+    s = S(m, p)
+    rho = lambda: float(np.sqrt(np.mean(s.get("res")[:units, 1] ** 2)))
+    first = True
+    prev_cfl = 0.0
+    it, f1, rho1 = 0, None, None
+    rows = []
+    t0 = time.perf_counter()
+    while it < max_iter:
+        n = 1 if first else min(every, max_iter - it)
+        c = mesh.cfl_schedule(p, it + 1, n, kind, prev_cfl)
+        prev_cfl = float(c[-1])
+        r = s.iterate(c, first_iter=first)
+        f = np.asarray(r if kind == "cc" else r[0])
+        if first:
+            f1, rho1, first = f[0], rho(), False
+        it += len(f)
+        d = rho() / rho1
+        rows.append({"iteration": it, "drop": float(f[-1] / f1), "density_drop": d,
+                     "seconds": round(time.perf_counter() - t0, 2)})
+        if d <= target or not np.isfinite(f[-1]):
+            break
+    return {"workload": w["desc"], "units": int(units), "target_density_drop": target, "iterations": it,
+            "reached": bool(rows and rows[-1]["density_drop"] <= target), "history": rows}
+
+
 # ---------------------------------------------------------------- clocks
 class ClockSampler:
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -938,6 +974,10 @@ def main():
                     help="skip the mixed forms' FP64 comparison run (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default block sizes (profiling runs: no tuning launches before the captured ones)")
+    ap.add_argument("--converge-history", type=int, default=0,
+                    help="instead of the benchmark: run the workload from freestream for up to this many iterations "
+                         "or a --target density drop, printing its residual history")
+    ap.add_argument("--target", type=float, default=1e-10, help="density drop that ends --converge-history")
     ap.add_argument("--batch-converge", type=int, default=8,
                     help="instances of the batched workload run to a 1e-8 drop (mixed ramp and FP64); 0 skips it")
     ap.add_argument("--no-configs", action="store_true",
@@ -954,6 +994,9 @@ def main():
         if rank != 0:
             return 0
         print(json.dumps(run_reference(args, w)))
+        return 0
+    if args.converge_history > 0:
+        print(json.dumps(converge_history(w, args.converge_history, args.target)))
         return 0
     dist = replicas.init("nccl")
     out = (run_batched if w["kind"] == "cc_batch" else run_ours)(args, w, dist, rank, local_rank)
