@@ -245,7 +245,7 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = Fal
 # a quarter-size case (reads grow in proportion to the units; see the
 # summaries under profiles/): scaled here to the benchmark's size.
 TRAFFIC_PER_UNIT = {
-    ("nc", "lusgs_sweeps", False): (103.81e6 / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
+    ("nc", "lusgs_sweeps", False): ((103.37e6 + 6.57e6) / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
     ("cc", "face_conv", False): (58.58e6 / 393728, "faces", "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", True): (156.96e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (138.34e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
@@ -257,7 +257,7 @@ TRAFFIC_PER_UNIT = {
 # active) of the same kernels from the same captures: the second roofline
 # fraction, the one that bounds the FP64 kernels.
 FP64_PIPE = {
-    ("nc", "lusgs_sweeps", False): (0.122, "profiles/nc_lusgs_512x256_full.md"),
+    ("nc", "lusgs_sweeps", False): (0.123, "profiles/nc_lusgs_512x256_full.md"),
     ("cc", "cell_grad", False): (0.845, "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", False): (0.847, "profiles/cc_fp64_512x256_full.md"),
     ("cc", "cell_res", False): (0.799, "profiles/cc_fp64_512x256_full.md"),
