@@ -241,11 +241,12 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = Fal
 
 
 # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per launch of
-# the dominant kernels, per unit of the workload, from one ncu capture each of
-# a quarter-size case (reads grow in proportion to the units; see the
+# the dominant kernels, per unit of the workload, from one ncu capture each
+# (the NCFVM sweep's from the full-size launch list, the others from a
+# quarter-size case, whose reads grow in proportion to the units; see the
 # summaries under profiles/): scaled here to the benchmark's size.
 TRAFFIC_PER_UNIT = {
-    ("nc", "lusgs_sweeps", False): ((103.37e6 + 6.57e6) / 131584, "nodes", "profiles/nc_lusgs_512x256_full.md"),
+    ("nc", "lusgs_sweeps", False): ((454.23e6 + 75.36e6) / 525312, "nodes", "profiles/nc_lusgs_1024x512_launches.md"),
     ("cc", "face_conv", False): (58.58e6 / 393728, "faces", "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", True): (156.96e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (138.34e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
