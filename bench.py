@@ -268,6 +268,19 @@ FP64_PIPE = {
 }
 
 
+# Latency floor of one LU-SGS sweep item on the critical path, in cycles of
+# the dependent FP64 chain from a predecessor's published values to this
+# item's (measured per-operation latencies, profiles/gb300_fp64_issue_microbench.md:
+# add / mul 76, divide 605): the edge term u*nx + v*ny, rho*un, *u, + p*n,
+# *ds, - F(qold), - omega*la*dq, *0.5 (8 mul/add after the first product
+# pair, 9 in all), one add of the edge sum, -res - sum, the division by the
+# diagonal, qold + dq, con2prim's division, and the two operations by which
+# the pressure (u*u + v*v, then three more) trails u and v where the next
+# item first needs it.
+FP64_ADD, FP64_DIV = 76.0, 605.0
+SWEEP_ITEM_FLOOR_CYCLES = 9 * FP64_ADD + FP64_ADD + FP64_ADD + FP64_DIV + FP64_ADD + FP64_DIV + 2 * FP64_ADD
+
+
 def launches_per_iter(kind: str, rk3: bool, laminar: bool, irs: bool = False, sides: bool = False) -> dict:
     """How many launches of each profiled phase one iteration makes.  An
     inviscid CCFVM RK3 step without smoothing computes its face fluxes once
@@ -802,6 +815,19 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
                      "fp64_pipe_source": FP64_PIPE.get((kind, rl_kernel, mixed_cc), (None, None))[1]},
         "kernels": kernels,
     }
+    if kind == "nc" and rl_kernel == "lusgs_sweeps":
+        # the sweep is bound by its critical path, not by bytes: its time per
+        # critical-path item against the FP64 latency floor of one item
+        lf, lb = solver.sweep_levels()
+        mhz = clocks.get("sm_mhz") or 2070.0
+        per_item = per_launch[rl_kernel] * 1e3 / (lf + lb)
+        floor = SWEEP_ITEM_FLOOR_CYCLES / mhz
+        out["roofline"]["latency_floor"] = {
+            "critical_path_items": lf + lb, "levels_forward": lf, "levels_backward": lb,
+            "us_per_item": round(per_item, 3), "floor_us_per_item": round(floor, 3),
+            "frac": round(floor / per_item, 3),
+            "basis": "dependent FP64 chain of one item (9 mul/add of the edge term, the sum, two divisions, "
+                     "the update, the pressure's lag) at the measured add 76 / divide 605 cycles, at the sampled SM clock"}
     if not args.no_cpu_baseline and args.gpus == 1:
         out["cpu_baseline"], out["parity"] = cpu_baseline(w, m, p, budget_s=args.cpu_budget)
     if accuracy is not None:

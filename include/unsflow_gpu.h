@@ -250,6 +250,10 @@ int uns_nc_tecplt(uns_nc_handle* h, double* out);
  * from the current state: out[6][2] = min, max of density, u, v, pressure,
  * Mach number, entropy. */
 int uns_nc_screen_minmax(uns_nc_handle* h, double* out);
+/* Dependency levels of the LU-SGS forward and backward sweeps on the
+ * handle's node order (NCFVM/lusgs.f90:48-124): their sum is the sweep's
+ * critical path in items.  No reference counterpart (measurement). */
+int uns_nc_sweep_levels(uns_nc_handle* h, int* forward, int* backward);
 /* Bound of every wait in the handle's LU-SGS sweeps, in device clock cycles
  * (default 4e9, about 2 s); a sweep whose wait runs out returns
  * UNS_ERR_TIMEOUT with the context intact.  No reference counterpart (the

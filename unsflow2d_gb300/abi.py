@@ -227,6 +227,7 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_find_cl_cd": ([vp, C.c_double, C.c_double, dp, dp, C.POINTER(C.c_int)], i32),
             "uns_cc_screen_minmax": ([vp, dp], i32), "uns_cc_tecplt": ([vp, dp], i32),
             "uns_nc_tecplt": ([vp, dp], i32), "uns_nc_screen_minmax": ([vp, dp], i32),
+            "uns_nc_sweep_levels": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], i32),
             "uns_cc_create_packed": ([C.POINTER(CCMeshView), C.POINTER(Params), i32, pp], i32),
             "uns_cc_packed_layout": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int)], i32),
             "uns_cc_packed_iterate": ([vp, i32, dp, i32, dp, C.POINTER(C.c_int)], i32),

@@ -1054,6 +1054,7 @@ struct uns_nc_handle {
     int nparts = 0;
     int* woff = nullptr;    // LU-SGS warp schedule: per-warp ranges of v.sched
     int coop_blocks = 0;
+    int lev_fwd = 0, lev_bwd = 0;  // dependency levels of the two sweeps (their critical path)
     double4 qinf;
     cudaGraphExec_t graph = nullptr;
     int graph_first = -1;
@@ -1313,6 +1314,8 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
                 nbr[k] = other(i, m->v2f[k], &sg);
             }
         WarpSchedule ws = list_schedule(nop, m->v2f_off, nbr.data(), h->coop_blocks * (kSweepBlock / 32));
+        h->lev_fwd = ws.nlev_fwd;
+        h->lev_bwd = ws.nlev_bwd;
         std::vector<int4> sched(ws.items.size());
         std::vector<int> re, rn, rs;
         for (size_t pos = 0; pos < ws.items.size(); ++pos) {
@@ -1521,6 +1524,13 @@ int uns_nc_screen_minmax(uns_nc_handle* h, double* out) {
     UNS_CUDA(cudaStreamSynchronize(h->stream));
     for (int k = 0; k < 12; ++k) out[k] = dec_ord(e[k]);
     return check_err_nc(h);
+}
+
+int uns_nc_sweep_levels(uns_nc_handle* h, int* forward, int* backward) {
+    if (!h || !forward || !backward) return UNS_ERR_ARG;
+    *forward = h->lev_fwd;
+    *backward = h->lev_bwd;
+    return UNS_OK;
 }
 
 int uns_nc_set_wait_limit(uns_nc_handle* h, long long cycles) {

@@ -280,6 +280,12 @@ class NCSolver(_Solver):
         self._call("residue", C.byref(f), C.byref(fi), C.byref(ii))
         return f.value, fi.value, ii.value
 
+    def sweep_levels(self) -> tuple[int, int]:
+        """Dependency levels of the forward and backward LU-SGS sweeps."""
+        f, b = C.c_int(), C.c_int()
+        self._call("sweep_levels", C.byref(f), C.byref(b))
+        return f.value, b.value
+
     def tecplt(self) -> np.ndarray:
         """tecplt's [nop][7] vertex table: x, y, rho, u, v, p, Mach."""
         out = np.zeros((self.nop, 7))
