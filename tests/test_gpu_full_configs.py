@@ -128,3 +128,38 @@ def test_cc_euler_2048x1024_one_iteration(assert_close):
     p = abi.make_params(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="rk3", cfl_max=0.9, min_res=0.0)
     g, o = CCSolver(m, p), OracleCC(m, p)
     cc_routines_check(g, o, m, p, mesh.cfl_schedule(p, 1, 1, "cc")[0], assert_close)
+
+
+def test_cc_lusgs_2048x1024_one_iteration(assert_close):
+    """Configuration 3's mesh with the implicit scheme (lusgs2 sweeps over
+    4.2 M cells): one iteration routine by routine."""
+    m = mesh.CCMesh.airfoil(2048, 1024, 0.12, 20.0, 1e-3)
+    p = abi.make_params(m_inf=0.75, aoa_deg=2.0, flux="roe", grad="gg", time="lusgs", cfl_max=5.0, cfl_type="ramp",
+                        cfl_min=0.5, cfl_ramp_steps=50, min_res=0.0)
+    g, o = CCSolver(m, p), OracleCC(m, p)
+    cfl = mesh.cfl_schedule(p, 1, 1, "cc")[0]
+    for s in (g, o):
+        s.con2prim(); s.avg_c2v(); s.time_step(cfl); s.save_old(); s.gradient(); s.lusgs()
+    assert res_err(g.get("res"), o.get("res"), o.get("la"), o.get("qc")[:o.noc]) <= RTOL
+    assert_close("qc", g.get("qc"), o.get("qc"), RTOL)
+
+
+def test_nc_rk3_vanleer_1024x512_two_iterations(assert_close):
+    """Configuration 2's mesh with the explicit scheme the NCFVM reference
+    hard-wires (van Leer + Venkatakrishnan, RK3): two iterations, stage by
+    stage."""
+    m = mesh.NCMesh.airfoil(1024, 512, 0.12, 20.0, 1e-3)
+    p = abi.make_params(m_inf=0.8, aoa_deg=1.25, flux="vanleer", limiter="vkn", time="rk3", cfl_max=0.9, min_res=0.0)
+    g, o = NCSolver(m, p), OracleNC(m, p)
+    for it in (1, 2):
+        cfl = mesh.cfl_schedule(p, it, 1, "nc")[0]
+        for s in (g, o):
+            s.save_old()
+        for irk in (1, 2, 3):
+            for s in (g, o):
+                s.fvresidual(cfl)
+            assert res_err(g.get("res"), o.get("res"), o.get("la"), o.get("qc")) <= RTOL
+            for s in (g, o):
+                s.rk_stage(irk)
+            assert_close("qc", g.get("qc"), o.get("qc"), RTOL)
+    assert_close("phi", g.get("phi"), o.get("phi"), RTOL_PHI)
