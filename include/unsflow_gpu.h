@@ -192,6 +192,21 @@ int uns_cc_adjoint_solve(uns_cc_handle* h, int objective, int max_iter, double t
                          int* iters);
 /* The adjoint vector of the last solve: [noc][4] and [nbf][5] (either may be NULL). */
 int uns_cc_adjoint_get(uns_cc_handle* h, double* lambda_q, double* lambda_g);
+/* Geometry.  prepare_geometry records what uns_cc_adjoint_prepare records
+ * plus the convective closure's Jacobians with respect to the face normal and
+ * length and the values of the start of the iteration (inviscid flows, and
+ * laminar flows with the GG-FC gradient; not a packed handle).
+ * uns_cc_adjoint_geometry then runs one transposed iteration like
+ * uns_cc_adjoint_vjp and writes G_X^T (wq, wg) + seed * J_X^T for every
+ * geometric array X of the handle's uns_cc_mesh into `out` (same layout;
+ * every array required): the explicit dependence of one iteration on the
+ * mesh at the recorded state.  With (wq, wg) the converged adjoint vector
+ * and seed 1 it is the total dJ/dX of the converged flow, which
+ * uns_host_cc_mesh_vjp carries to the node coordinates.  It overwrites the
+ * adjoint vector as uns_cc_adjoint_vjp does. */
+int uns_cc_adjoint_prepare_geometry(uns_cc_handle* h, double cfl, double* cl, double* cd);
+int uns_cc_adjoint_geometry(uns_cc_handle* h, int objective, double seed, const double* wq, const double* wg,
+                            uns_cc_mesh_adj* out);
 
 /* ==================================================== packed cases ====*/
 /* Many independent CCFVM cases in ONE index space (no reference

@@ -35,6 +35,16 @@ int uns_host_nc_airfoil(int ni, int nj, double thickness, double rfar, double dw
  * the adjoint's wall-node and Hicks-Henne derivatives. */
 int uns_host_cc_airfoil_dy(int ni, int nj, double thickness, double rfar, double dwall, const double* dy,
                            uns_host_cc** out);
+/* The mesh m with its nodes moved to (px, py) [nop]: same topology, cell
+ * centroids and areas of the moved triangles, then geometric (triangle cells
+ * only; UNS_ERR_MESH otherwise or for a degenerate cell). */
+int uns_host_cc_moved(const uns_host_cc* m, const double* px, const double* py, uns_host_cc** out);
+/* Transpose of geometric (cell_face_norm, face_co_volume, LSQR_Coeff,
+ * pseudo_Laplacian, the ghost mirror) and of the triangles' centroids and
+ * areas: given the adjoints `a` of m's mesh arrays (uns_cc_adjoint_geometry),
+ * writes dJ/dpx, dJ/dpy [nop].  UNS_ERR_MESH when m's arrays are not those of
+ * its triangles. */
+int uns_host_cc_mesh_vjp(const uns_host_cc* m, const uns_cc_mesh_adj* a, double* gpx, double* gpy);
 /* geometry.inp readers (CCFVM/read_input.F90:123-213, NCFVM/read_input.f90:
  * 479-512) followed by geometric. */
 int uns_host_cc_read(const char* path, uns_host_cc** out);

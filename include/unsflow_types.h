@@ -141,6 +141,18 @@ typedef struct {
     const double *v2c_wt;                  /* pseudo-Laplacian weights      */
 } uns_cc_mesh;
 
+/* Adjoints (dJ/d array) of the geometric arrays of a uns_cc_mesh, in the same
+ * layout: written by uns_cc_adjoint_geometry, read by uns_host_cc_mesh_vjp. */
+typedef struct {
+    double *px, *py;                       /* [nop]                         */
+    double *cx, *cy;                       /* [noc+nbf]                     */
+    double *cv, *cov;                      /* [noc]                         */
+    double *fnx, *fny, *farea;             /* [nfi+nbf]                     */
+    double *fcx, *fcy;                     /* [nfi+nbf]                     */
+    double *r11, *r12, *r22;               /* [noc]                         */
+    double *v2c_wt;                        /* [v2c_off[nop]]                */
+} uns_cc_mesh_adj;
+
 /* Vertex-centred median-dual mesh after the caller's geometric
  * preprocessing (NCFVM/geometric.f90:1-806).  Faces are mesh edges; the
  * dual-face unit normal points from fp1's dual cell to fp2's. */

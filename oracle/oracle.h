@@ -67,6 +67,13 @@ int oracle_cc_cs_set(oracle_cc_cs* o, int field, const double* re, const double*
 int oracle_cc_cs_get(oracle_cc_cs* o, int field, double* re, double* im);
 /* One RK3 main-loop iteration (as oracle_cc_iteration, without the norm). */
 int oracle_cc_cs_iteration(oracle_cc_cs* o, double cfl);
+/* Hold the RK update's dt / cv real (dt = real(dt / cv) * cv), as the
+   adjoint holds it fixed; off by default. */
+int oracle_cc_cs_freeze_dt(oracle_cc_cs* o, int on);
+/* Imaginary parts of one geometric array (field: index in uns_cc_mesh_adj
+   order px, py, cx, cy, cv, cov, fnx, fny, farea, fcx, fcy, r11, r12, r22,
+   v2c_wt), real parts kept. */
+int oracle_cc_cs_set_geometry_im(oracle_cc_cs* o, int field, const double* im);
 /* Fx1, Fy1 of the last residual: fx[0] + i fx[1], fy[0] + i fy[1]. */
 int oracle_cc_cs_forces(oracle_cc_cs* o, double* fx, double* fy);
 

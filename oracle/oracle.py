@@ -51,7 +51,8 @@ def lib() -> C.CDLL:
             "oracle_cc_cs_create": ([C.POINTER(abi.CCMeshView), C.POINTER(abi.Params), C.c_double], vp),
             "oracle_cc_cs_free": ([vp], None), "oracle_cc_cs_set": ([vp, i32, dp, dp], i32),
             "oracle_cc_cs_get": ([vp, i32, dp, dp], i32), "oracle_cc_cs_iteration": ([vp, C.c_double], i32),
-            "oracle_cc_cs_forces": ([vp, dp, dp], i32),
+            "oracle_cc_cs_forces": ([vp, dp, dp], i32), "oracle_cc_cs_freeze_dt": ([vp, i32], i32),
+            "oracle_cc_cs_set_geometry_im": ([vp, i32, dp], i32),
             "oracle_cc_find_cl_cd": ([vp, C.c_double, C.c_double, dp, dp, ip], i32),
             "oracle_cc_screen_minmax": ([vp, dp], i32), "oracle_cc_tecplt": ([vp, dp], i32),
             "oracle_nc_tecplt": ([vp, dp], i32), "oracle_nc_screen_minmax": ([vp, dp], i32),
@@ -261,6 +262,16 @@ class OracleCCComplexStep:
     def iteration(self, cfl: float) -> None:
         if self._L.oracle_cc_cs_iteration(self._h, C.c_double(cfl)):
             raise OracleError("oracle_cc_cs_iteration")
+
+    def freeze_dt(self, on: bool = True) -> None:
+        """Hold the RK update's dt / cv real (no derivative), as the adjoint does."""
+        self._L.oracle_cc_cs_freeze_dt(self._h, int(on))
+
+    def set_geometry_im(self, field: str, im: np.ndarray) -> None:
+        """Imaginary parts of one geometric mesh array (abi.CC_GEOM_FIELDS name)."""
+        a = np.ascontiguousarray(im, dtype=np.float64)
+        if self._L.oracle_cc_cs_set_geometry_im(self._h, abi.CC_GEOM_FIELDS.index(field), _dp(a)):
+            raise OracleError(f"oracle_cc_cs_set_geometry_im {field}")
 
     def forces(self) -> tuple[complex, complex]:
         fx, fy = np.zeros(2), np.zeros(2)

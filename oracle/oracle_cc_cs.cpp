@@ -60,7 +60,10 @@ using R = cs;
 
 }  // namespace
 
-struct oracle_cc_cs { CC s; };
+struct oracle_cc_cs {
+    CC s;
+    bool freeze_dt = false;
+};
 
 extern "C" {
 
@@ -97,6 +100,12 @@ int oracle_cc_cs_iteration(oracle_cc_cs* o, double cfl) {
     avg_c2v(s);
     s.cfl = cfl;
     time_step02(s, cfl);
+    // The adjoint holds the RK update's dt / cv at its recorded value (it
+    // multiplies the residual, which vanishes at a converged state); with
+    // freeze_dt the complex step does the same -- dt is replaced by
+    // real(dt / cv) * cv -- so that the two agree at any state.
+    if (o->freeze_dt)
+        for (int i = 0; i < s.noc; ++i) s.dt[i] = cs((s.dt[i].z / s.cv[i].z).real()) * s.cv[i];
     cc_save_old(s);
     if ((rc = gradient(s))) return rc;
     if (s.P.time_mode != UNS_TIME_RK3) return UNS_ERR_ARG;
@@ -104,6 +113,24 @@ int oracle_cc_cs_iteration(oracle_cc_cs* o, double cfl) {
         if ((rc = fvresidual(s))) return rc;
         cc_rk_stage(s, irk);
     }
+    return UNS_OK;
+}
+
+// Geometric arrays in uns_cc_mesh_adj order.
+int oracle_cc_cs_set_geometry_im(oracle_cc_cs* o, int field, const double* im) {
+    if (!o || !im) return UNS_ERR_ARG;
+    CC& s = o->s;
+    std::vector<cs>* tab[15] = {&s.px, &s.py, &s.cx, &s.cy, &s.cv, &s.cov, &s.fnx, &s.fny, &s.farea,
+                                &s.fcx, &s.fcy, &s.r11, &s.r12, &s.r22, &s.v2c_wt};
+    if (field < 0 || field >= 15) return UNS_ERR_ARG;
+    std::vector<cs>& v = *tab[field];
+    for (size_t k = 0; k < v.size(); ++k) v[k] = cs(v[k].z.real(), im[k]);
+    return UNS_OK;
+}
+
+int oracle_cc_cs_freeze_dt(oracle_cc_cs* o, int on) {
+    if (!o) return UNS_ERR_ARG;
+    o->freeze_dt = on != 0;
     return UNS_OK;
 }
 

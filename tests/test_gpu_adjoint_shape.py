@@ -1,7 +1,10 @@
 """Shape derivatives (unsflow2d_gb300.shape): dC_L/d(Hicks-Henne amplitude)
-from the adjoint vector plus one-iteration geometry partials, against central
-differences of C_L between solutions re-converged on meshes with the bump
-applied at +- 1e-5 (limiter frozen at the base phi in both)."""
+from the adjoint vector plus the transposed geometric linearisation
+(uns_cc_adjoint_geometry, then the transposed geometric preprocessing),
+against the same adjoint with one-iteration differenced geometry partials
+and against central differences of C_L between solutions re-converged on
+meshes with the bump applied at +- 1e-5 (limiter frozen at the base phi in
+both)."""
 import numpy as np
 import pytest
 
@@ -43,6 +46,10 @@ def test_bump_gradient_matches_reconverged_differences(name):
     lq, lg = a.adjoint_get()
     grad = case.bump_gradient("cl", lq, lg)
     assert grad.shape == (16,) and np.isfinite(grad).all()
+    grad_fd = case.bump_gradient("cl", lq, lg, method="differenced")
+    rel = np.max(np.abs(grad - grad_fd)) / np.max(np.abs(grad))
+    print(f"{name}: transposed vs one-iteration differences, max rel {rel:.2e}")
+    assert rel <= 1e-5, (grad, grad_fd)
     B = shape.bump_basis(NI)
     delta = 1e-5
     for k in (2, 12):  # upper-surface bump at x = 0.25, lower-surface bump at x = 0.5

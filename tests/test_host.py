@@ -301,3 +301,60 @@ def test_tecplt_writer_layout(tmp_path):
     assert np.array_equal(vals, table)
     elems = np.array([[int(x) for x in ln.split()] for ln in lines[4 + 2 * m.arrays["nop"]:]])
     assert np.array_equal(elems, cells + 1)
+
+
+def test_moved_mesh_at_the_same_nodes_is_the_mesh(cc):
+    a = cc.arrays
+    m = cc.moved(a["px"], a["py"]).arrays
+    for k in abi.CC_GEOM_FIELDS:  # centroids are recomputed as vertex means: rounding only
+        assert np.allclose(m[k], a[k], rtol=1e-13, atol=1e-13), k
+    for k in ("fp1", "fp2", "fin", "fout", "fbc", "c2f", "v2c"):
+        assert np.array_equal(m[k], a[k]), k
+
+
+def test_mesh_vjp_is_the_transpose_of_the_geometric_preprocessing(cc):
+    """uns_host_cc_mesh_vjp against central differences of the host geometry
+    (uns_host_cc_moved) in a random node direction, for random adjoints of
+    every geometric array: <abar, dA/dX dX> = <Xbar, dX>."""
+    a = cc.arrays
+    rng = np.random.default_rng(3)
+    sizes = abi.cc_geom_sizes(a)
+    abar = {k: rng.standard_normal(n) for k, n in sizes.items()}
+    gx, gy = cc.node_adjoint(abar)
+    dpx, dpy = 1e-3 * rng.standard_normal(a["nop"]), 1e-3 * rng.standard_normal(a["nop"])
+    rhs = np.dot(gx, dpx) + np.dot(gy, dpy)
+    h = 1e-5
+    mp = cc.moved(a["px"] + h * dpx, a["py"] + h * dpy).arrays
+    mm = cc.moved(a["px"] - h * dpx, a["py"] - h * dpy).arrays
+    terms = {k: np.dot(abar[k], (mp[k] - mm[k]) / (2 * h)) for k in sizes}
+    lhs = sum(terms.values())
+    assert abs(lhs - rhs) <= 1e-7 * abs(rhs), (lhs, rhs)
+    # and array by array, against the scale of the whole product
+    scale = sum(abs(t) for t in terms.values())
+    for k in sizes:
+        e = {kk: np.zeros(n) for kk, n in sizes.items()}
+        e[k] = abar[k]
+        x1, y1 = cc.node_adjoint(e)
+        assert abs(terms[k] - (np.dot(x1, dpx) + np.dot(y1, dpy))) <= 1e-7 * scale, k
+
+
+def test_mesh_vjp_rejects_a_mesh_whose_centroids_are_not_its_triangles(cc, tmp_path):
+    """A geometry.inp keeps the file's cell centroids; one moved off its
+    triangle's vertex mean makes the transposed geometry refuse the mesh."""
+    path = tmp_path / "g.inp"
+    cc.write(path)
+    text = path.read_text().splitlines()
+    nop, noc = (int(x) for x in text[0].split()[:2])
+    row = nop + noc  # the last cell: an outer one, large enough to keep its face co-volumes positive
+    parts = text[row].split()
+    parts[1] = repr(float(parts[1]) + 1e-6)
+    text[row] = " ".join(parts)
+    path.write_text("\n".join(text) + "\n")
+    m = mesh.CCMesh.read(path)
+    with pytest.raises(abi.UnsError) as e:
+        m.node_adjoint({k: np.zeros(n) for k, n in abi.cc_geom_sizes(m.arrays).items()})
+    assert e.value.code == abi.UNS_ERR_MESH
+    st, keep = abi.cc_mesh_adj(cc.arrays)
+    gx, gy = np.zeros(cc.arrays["nop"]), np.zeros(cc.arrays["nop"])
+    lib = abi.host_lib()
+    assert lib.uns_host_cc_mesh_vjp(cc._h, None, gx.ctypes.data_as(abi._D), gy.ctypes.data_as(abi._D)) == abi.UNS_ERR_ARG

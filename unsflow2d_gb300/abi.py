@@ -81,6 +81,34 @@ class NCMeshView(C.Structure):
                 ("wx", _D), ("wy", _D), ("v2f_off", _I), ("v2f", _I)]
 
 
+#: Geometric arrays of a CC mesh, in uns_cc_mesh_adj order, and their lengths.
+CC_GEOM_FIELDS = ("px", "py", "cx", "cy", "cv", "cov", "fnx", "fny", "farea", "fcx", "fcy", "r11", "r12", "r22",
+                  "v2c_wt")
+
+
+class CCMeshAdj(C.Structure):
+    _fields_ = [(k, _D) for k in CC_GEOM_FIELDS]
+
+
+def cc_geom_sizes(arr: dict) -> dict:
+    nop, noc, nof, ntot = arr["nop"], arr["noc"], arr["nfi"] + arr["nbf"], arr["noc"] + arr["nbf"]
+    n = {"px": nop, "py": nop, "cx": ntot, "cy": ntot, "cv": noc, "cov": noc, "r11": noc, "r12": noc, "r22": noc,
+         "v2c_wt": int(arr["v2c_off"][-1])}
+    n.update({k: nof for k in ("fnx", "fny", "farea", "fcx", "fcy")})
+    return n
+
+
+def cc_mesh_adj(arr: dict, values: dict | None = None) -> tuple[CCMeshAdj, dict]:
+    """A uns_cc_mesh_adj over numpy arrays sized for mesh `arr` (zeros, or
+    copies of `values`); returns the struct and the arrays it points into."""
+    out = {}
+    for k, n in cc_geom_sizes(arr).items():
+        out[k] = np.zeros(n) if values is None else np.ascontiguousarray(values[k], dtype=np.float64).copy()
+        assert out[k].shape == (n,), k
+    st = CCMeshAdj(**{k: out[k].ctypes.data_as(_D) for k in CC_GEOM_FIELDS})
+    return st, out
+
+
 def _arr(ptr, n, dtype):
     if n == 0:
         return np.zeros(0, dtype=dtype)
@@ -235,6 +263,8 @@ def gpu_lib() -> C.CDLL:
             "uns_cc_adjoint_vjp": ([vp, i32, C.c_double, dp, dp, dp, dp, dp], i32),
             "uns_cc_adjoint_solve": ([vp, i32, i32, C.c_double, dp, dp, C.POINTER(C.c_int)], i32),
             "uns_cc_adjoint_get": ([vp, dp, dp], i32),
+            "uns_cc_adjoint_prepare_geometry": ([vp, C.c_double, dp, dp], i32),
+            "uns_cc_adjoint_geometry": ([vp, i32, C.c_double, dp, dp, C.POINTER(CCMeshAdj)], i32),
         }
         for fn, (args, res) in sig.items():
             f = getattr(lib, fn)
@@ -254,6 +284,8 @@ def host_lib() -> C.CDLL:
             "uns_host_last_error": ([], C.c_char_p),
             "uns_host_cc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),
             "uns_host_cc_airfoil_dy": ([i32, i32, dp, dp, dp, _D, pp], i32),
+            "uns_host_cc_moved": ([vp, _D, _D, pp], i32),
+            "uns_host_cc_mesh_vjp": ([vp, C.POINTER(CCMeshAdj), _D, _D], i32),
             "uns_host_cc_plot3d": ([C.c_char_p, pp], i32), "uns_host_nc_plot3d": ([C.c_char_p, pp], i32),
             "uns_host_airfoil_plot3d": ([i32, i32, dp, dp, dp, C.c_char_p], i32),
             "uns_host_nc_airfoil": ([i32, i32, dp, dp, dp, pp], i32),

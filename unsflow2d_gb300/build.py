@@ -45,7 +45,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
              "-I", str(INCLUDE), "-I", str(CSRC / "host")]
 
 GPU_SOURCES = ["uns_api.cu", "uns_cc.cu", "uns_cc_adj.cu", "uns_cc_post.cu", "uns_nc.cu", "uns_noalloc.cu"]
-HOST_SOURCES = ["host/host_mesh.cpp", "host/host_api.cpp"]
+HOST_SOURCES = ["host/host_mesh.cpp", "host/host_api.cpp", "host/host_shape.cpp"]
 DRIVER_SOURCES = ["host/host_main.cpp"]
 
 

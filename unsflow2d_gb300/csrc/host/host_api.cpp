@@ -82,6 +82,26 @@ int uns_host_cc_airfoil_dy(int ni, int nj, double t, double rfar, double dwall, 
     return UNS_OK;
 }
 
+int uns_host_cc_moved(const uns_host_cc* m, const double* px, const double* py, uns_host_cc** out) {
+    if (!m || !px || !py || !out) return fail(UNS_ERR_ARG, "uns_host_cc_moved: null argument");
+    auto* o = new uns_host_cc();
+    std::string err;
+    int rc = moved_cc(m->raw, px, py, o->raw, err);
+    if (!rc) rc = geometric_cc(o->raw, o->mesh, err);
+    if (rc) { delete o; return fail(rc, err); }
+    *out = o;
+    return UNS_OK;
+}
+
+int uns_host_cc_mesh_vjp(const uns_host_cc* m, const uns_cc_mesh_adj* a, double* gpx, double* gpy) {
+    if (!m || !a || !gpx || !gpy || !a->px || !a->py || !a->cx || !a->cy || !a->cv || !a->cov || !a->fnx || !a->fny ||
+        !a->farea || !a->fcx || !a->fcy || !a->r11 || !a->r12 || !a->r22 || !a->v2c_wt)
+        return fail(UNS_ERR_ARG, "uns_host_cc_mesh_vjp: null argument");
+    std::string err;
+    int rc = mesh_vjp_cc(m->mesh, *a, gpx, gpy, err);
+    return rc ? fail(rc, err) : UNS_OK;
+}
+
 int uns_host_nc_airfoil(int ni, int nj, double t, double rfar, double dwall, uns_host_nc** out) {
     if (!out) return fail(UNS_ERR_ARG, "null out");
     AirfoilSpec s{ni, nj, t, rfar, dwall};

@@ -101,6 +101,11 @@ int write_geometry_nc(const std::string& path, const RawNC& m, std::string& err)
 int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err);
 int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err);
 
+// Shape derivatives (host_shape.cpp): raw rebuilt at moved nodes, and the
+// transpose of geometric_cc onto the node coordinates.
+int moved_cc(const RawCC& raw, const double* px, const double* py, RawCC& out, std::string& err);
+int mesh_vjp_cc(const MeshCC& m, const uns_cc_mesh_adj& a, double* gpx, double* gpy, std::string& err);
+
 // flo.inp readers (CCFVM/read_input.F90:4-121, NCFVM/read_input.f90:4-86).
 int read_flo_inp_cc(const std::string& path, uns_params& p, std::string& gridfile, std::string& err);
 int read_flo_inp_nc(const std::string& path, uns_params& p, std::string& gridfile, std::string& err);

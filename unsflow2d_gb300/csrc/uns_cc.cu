@@ -2166,6 +2166,9 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
         }
         lsw[f] = make_double4(wx0, wy0, wx1, wy1);
     }
+    h->lsq_r.resize((size_t)noc * 3);
+    for (int i = 0; i < noc; ++i) { h->lsq_r[3 * i] = m->r11[i]; h->lsq_r[3 * i + 1] = m->r12[i]; h->lsq_r[3 * i + 2] = m->r22[i]; }
+    h->fnb_host = fnb;
     // FP32 geometry of the mixed form, rounded once from the FP64 values.
     std::vector<float4> fgeof(nof), fnaf(nof), lswf(nof);
     for (int f = 0; f < nof; ++f) {

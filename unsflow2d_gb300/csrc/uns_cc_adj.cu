@@ -70,6 +70,23 @@ struct AdjView {
     double jx, jy;      // seed * dJ/dFx1, dJ/dFy1
     double jalpha;      // seed * explicit dJ/dalpha
     double dua, dva;    // d u_inf / d alpha, d v_inf / d alpha
+    // Geometry (uns_cc_adjoint_prepare_geometry): the convective closure's
+    // Jacobians with respect to the face normal and length, the values of the
+    // start of the iteration that the geometric partials read, and the
+    // adjoints of the view's geometric arrays that one transposed iteration
+    // accumulates.  Allocated only when geo is set.
+    int geo;             // 1 while the transposed iteration accumulates them
+    const double4* JG;   // [3][3][nfi]: dF/d(nx, ny, area) of interior faces
+    const double* BG;    // [3][nbf][3 in][9 out]: d(F, ghost prim, ghost T)/d(nx, ny, area)
+    const double4 *s_qp, *s_gx, *s_gy, *s_pp, *s_fq, *s_fgx, *s_fgy;
+    const double *s_qT, *s_ppT, *s_fas;
+    const double2* s_fgT;
+    double4 *fls, *frs;  // reconstruction adjoints summed over the stages (ql, qr; boundary qcl)
+    double2 *gfn, *gfcen, *gci, *gco, *gp1, *gp2;  // per face: normal, centre, parts for its cells and end points
+    double* garea;
+    double4* glsw;       // LSQ weights
+    double2 *gpxy, *gcen;
+    double *gcv, *gcov, *gv2c;
 };
 
 struct CCAdj {
@@ -77,7 +94,9 @@ struct CCAdj {
     std::vector<void*> allocs;
     double cfl = 0.0, fx = 0.0, fy = 0.0;
     bool recorded = false;
+    bool geo_alloc = false, geo_recorded = false;
     int nparts = 0;
+    int nv2c = 0;
 };
 
 void cc_adj_free(uns_cc_handle* h) {
@@ -148,6 +167,14 @@ __global__ void k_rec_conv(CCView v, AdjView a, int s) {
             face_flux<Tan>(v.g, Tan(n.x), Tan(n.y), Tan(area), L, R, F);
             ((double4*)a.JF)[((size_t)s * 8 + dir) * v.nfi + f] = make_double4(F[0].d, F[1].d, F[2].d, F[3].d);
         }
+        if (a.geo) {
+            for (int dir = 0; dir < 3; ++dir) {
+                V4<Tan> L, R, F;
+                for (int j = 0; j < 4; ++j) { L[j] = Tan(ql[j]); R[j] = Tan(qr[j]); }
+                face_flux<Tan>(v.g, Tan(n.x, dir == 0), Tan(n.y, dir == 1), Tan(area, dir == 2), L, R, F);
+                ((double4*)a.JG)[((size_t)s * 3 + dir) * v.nfi + f] = make_double4(F[0].d, F[1].d, F[2].d, F[3].d);
+            }
+        }
         return;
     }
     const int b = f - v.nfi, bc = v.fbc[f];
@@ -167,6 +194,35 @@ __global__ void k_rec_conv(CCView v, AdjView a, int s) {
         double* row = J + dir * 9;
         for (int k = 0; k < 4; ++k) { row[k] = o.F[k].d; row[4 + k] = o.gp[k].d; }
         row[8] = o.gT.d;
+    }
+    if (a.geo) {
+        double* G = (double*)a.BG + ((size_t)s * v.nbf + b) * 27;
+        for (int dir = 0; dir < 3; ++dir) {
+            V4<Tan> L, C;
+            for (int j = 0; j < 4; ++j) { L[j] = Tan(qcl[j]); C[j] = Tan(at(c, j)); }
+            CCBnd<Tan> o = cc_boundary<Tan, Tan, Tan>(v.g, bc, Tan(n.x, dir == 0), Tan(n.y, dir == 1),
+                                                      Tan(area, dir == 2), L, C, Tan(v.g.u_inf), Tan(v.g.v_inf));
+            double* row = G + dir * 9;
+            for (int k = 0; k < 4; ++k) { row[k] = o.F[k].d; row[4 + k] = o.gp[k].d; }
+            row[8] = o.gT.d;
+        }
+    }
+}
+
+// Values of the start of the iteration that the geometric partials read
+// (after the gradient; the stages leave them unchanged for the flows whose
+// geometry is differentiated: inviscid, and laminar with Gradient_GG_FC).
+__global__ void k_rec_geo(CCView v, AdjView a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < v.ntot) { ((double4*)a.s_qp)[i] = v.qp[i]; ((double*)a.s_qT)[i] = v.qT[i]; }
+    if (i < v.noc) { ((double4*)a.s_gx)[i] = v.gx[i]; ((double4*)a.s_gy)[i] = v.gy[i]; }
+    if (i < v.nop) { ((double4*)a.s_pp)[i] = v.pp[i]; ((double*)a.s_ppT)[i] = v.ppT[i]; }
+    if (i < v.nof) {
+        ((double4*)a.s_fq)[i] = v.fq[i];
+        ((double4*)a.s_fgx)[i] = v.fgx[i];
+        ((double4*)a.s_fgy)[i] = v.fgy[i];
+        ((double2*)a.s_fgT)[i] = v.fgT[i];
+        ((double*)a.s_fas)[i] = v.fasum[i];
     }
 }
 
@@ -214,6 +270,12 @@ __global__ void k_adj_init(CCView v, AdjView a) {
         a.sgx[i] = z4(); a.sgy[i] = z4(); a.sgT[i] = make_double2(0.0, 0.0);
     }
     if (i < v.nbf) a.falpha[i] = 0.0;
+    if (a.geo && i < v.nof) {
+        const double2 z = make_double2(0.0, 0.0);
+        a.fls[i] = z4(); a.frs[i] = z4(); a.glsw[i] = z4();
+        a.gfn[i] = z; a.gfcen[i] = z; a.gci[i] = z; a.gco[i] = z; a.gp1[i] = z; a.gp2[i] = z;
+        a.garea[i] = 0.0;
+    }
 }
 
 // RK update q = a*qold + b*(q - dt/cv * res) of stage irk, transposed.
@@ -271,6 +333,14 @@ __global__ void k_adj_visc(CCView v, AdjView a, int s, int last, int stage_grad)
     GX[f] = gx; GY[f] = gy;
     double2 t = GT[f];
     GT[f] = make_double2(t.x + txb, t.y + tyb);
+    if (a.geo) {  // flux*area = area*mr*(S1, 0, txx nx + txy ny, txy nx + tyy ny): its normal and length
+        const double A = u * txx + vv * txy - qx, B = u * txy + vv * tyy - qy;
+        const double t1 = txx * n.x + txy * n.y, t2 = txy * n.x + tyy * n.y;
+        a.garea[f] = a.garea[f] + mr * (b.x * S1 + b.z * t1 + b.w * t2);
+        const double2 gn = a.gfn[f];
+        a.gfn[f] = make_double2(gn.x + area * mr * (b.x * A + b.z * txx + b.w * txy),
+                                gn.y + area * mr * (b.x * B + b.z * txy + b.w * tyy));
+    }
 }
 
 // Sutherland viscosity transposed onto this stage's state.
@@ -363,6 +433,14 @@ __global__ void k_adj_conv(CCView v, AdjView a, int s, int last) {
         for (int dir = 0; dir < 8; ++dir) l[dir] = dot(a.JF[((size_t)s * 8 + dir) * v.nfi + f], Fb);
         a.fl[f] = make_double4(l[0], l[1], l[2], l[3]);
         a.fr[f] = make_double4(l[4], l[5], l[6], l[7]);
+        if (a.geo) {
+            const double2 gn = a.gfn[f];
+            a.gfn[f] = make_double2(gn.x + dot(a.JG[((size_t)s * 3 + 0) * v.nfi + f], Fb),
+                                    gn.y + dot(a.JG[((size_t)s * 3 + 1) * v.nfi + f], Fb));
+            a.garea[f] = a.garea[f] + dot(a.JG[((size_t)s * 3 + 2) * v.nfi + f], Fb);
+            a.fls[f] = add(a.fls[f], a.fl[f]);
+            a.frs[f] = add(a.frs[f], a.fr[f]);
+        }
         return;
     }
     const int b = f - v.nfi, g = nb.y;
@@ -380,6 +458,15 @@ __global__ void k_adj_conv(CCView v, AdjView a, int s, int last) {
     a.fl[f] = make_double4(x[0], x[1], x[2], x[3]);
     a.fr[f] = make_double4(x[4], x[5], x[6], x[7]);
     a.falpha[b] = a.falpha[b] + x[8];
+    if (a.geo) {
+        const double* G = a.BG + ((size_t)s * v.nbf + b) * 27;
+        double gx = 0.0, gy = 0.0, ga = 0.0;
+        for (int k = 0; k < 9; ++k) { gx = gx + G[k] * y[k]; gy = gy + G[9 + k] * y[k]; ga = ga + G[18 + k] * y[k]; }
+        const double2 gn = a.gfn[f];
+        a.gfn[f] = make_double2(gn.x + gx, gn.y + gy);
+        a.garea[f] = a.garea[f] + ga;
+        a.fls[f] = add(a.fls[f], make_double4(x[0], x[1], x[2], x[3]));
+    }
     a.qp[g] = z4();
     a.qT[g] = 0.0;
 }
@@ -583,6 +670,156 @@ __global__ void k_adj_reduce(CCView v, AdjView a, int nparts, double* hist, int 
     }
 }
 
+// ------------------------------------------------ geometric partials
+// After the transposed stages and the start gradient's transpose (a.gx, a.gy:
+// the adjoint of the gradient of the start of the iteration; a.fgx, a.fgy,
+// a.fgT: of the diamond-path face gradient), per face:
+//  * reconstruction (fvresidual.F90:235-247, boundary :38-43): ql depends on
+//    the face centre minus the cell centroid through the limited gradient;
+//  * Gradient_GG (gradient.F90:95-156): g_i = sum sigma q_f n_f area_f / cv_i
+//    (sigma -1 on the out side and on boundary faces);
+//  * Gradient_LSQR (gradient.F90:2-93): the adjoints of the face's weights;
+//  * Gradient_GG_FC (gradient.F90:159-323): the face gradient is T_f / s_f,
+//    T_f the contour sum over the diamond (p1, cell out, p2, cell in) of the
+//    edge means times the edge normals (the shared edge p1-p2 of the two
+//    triangles cancels) and s_f the diamond's area; the cell gradient is
+//    sum_f T_f / cov_i.  Contributions to the diamond's four points go to
+//    gp1, gco, gp2, gci (gathered per node and cell afterwards).
+__device__ __forceinline__ double dot5x(double4 a, double aT, double4 b, double bT) { return dot(a, b) + aT * bT; }
+
+__global__ void k_geo_face(CCView v, AdjView a, int use_ggfc) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= v.nof) return;
+    const int2 nb = v.fnb[f];
+    const bool interior = f < v.nfi;
+    const double zhi = 1.0 / 3.0;
+    double2 gfc = make_double2(0.0, 0.0), gci = make_double2(0.0, 0.0), gco = make_double2(0.0, 0.0);
+    {  // reconstruction
+        const double4 ph = v.phi[nb.x], gx = a.s_gx[nb.x], gy = a.s_gy[nb.x], L = a.fls[f];
+        const double c = interior ? 0.5 * (1.0 - zhi) : 1.0;
+        double d0 = 0.0, d1 = 0.0;
+        for (int j = 0; j < 4; ++j) {
+            d0 = d0 + at(L, j) * c * at(ph, j) * at(gx, j);
+            d1 = d1 + at(L, j) * c * at(ph, j) * at(gy, j);
+        }
+        gfc = make_double2(d0, d1);
+        gci = make_double2(-d0, -d1);
+        if (interior) {
+            const double4 po = v.phi[nb.y], hx = a.s_gx[nb.y], hy = a.s_gy[nb.y], Rr = a.frs[f];
+            double e0 = 0.0, e1 = 0.0;
+            for (int j = 0; j < 4; ++j) {
+                e0 = e0 + at(Rr, j) * c * at(po, j) * at(hx, j);
+                e1 = e1 + at(Rr, j) * c * at(po, j) * at(hy, j);
+            }
+            gfc = make_double2(gfc.x + e0, gfc.y + e1);
+            gco = make_double2(-e0, -e1);
+        }
+    }
+    a.gfcen[f] = gfc;
+    if (v.grad_type == UNS_GRAD_GG) {
+        const double4 q = a.s_fq[f];
+        const double2 n = v.fn[f];
+        const double area = v.farea[f];
+        const double si = interior ? 1.0 : -1.0;
+        double ddx = si * dot(q, a.gx[nb.x]) / v.cv[nb.x], ddy = si * dot(q, a.gy[nb.x]) / v.cv[nb.x];
+        if (interior) {
+            ddx = ddx - dot(q, a.gx[nb.y]) / v.cv[nb.y];
+            ddy = ddy - dot(q, a.gy[nb.y]) / v.cv[nb.y];
+        }
+        const double2 gn = a.gfn[f];
+        a.gfn[f] = make_double2(gn.x + ddx * area, gn.y + ddy * area);
+        a.garea[f] = a.garea[f] + ddx * n.x + ddy * n.y;
+    } else if (v.grad_type == UNS_GRAD_LSQR) {
+        const double4 var = sub(a.s_qp[nb.y], a.s_qp[nb.x]);
+        a.glsw[f] = make_double4(dot(var, a.gx[nb.x]), dot(var, a.gy[nb.x]),
+                                 interior ? -dot(var, a.gx[nb.y]) : 0.0, interior ? -dot(var, a.gy[nb.y]) : 0.0);
+    }
+    double2 g1 = make_double2(0.0, 0.0), g2 = make_double2(0.0, 0.0);
+    if (use_ggfc) {
+        const double s = a.s_fas[f];
+        const double4 bx = a.fgx[f], by = a.fgy[f], fx = a.s_fgx[f], fy = a.s_fgy[f];
+        const double2 bT = a.fgT[f], fT = a.s_fgT[f];
+        // fg = T / s: the adjoint of T, and of s through fg
+        double sb = -(dot5x(bx, bT.x, fx, fT.x) + dot5x(by, bT.y, fy, fT.y)) / s;
+        if (v.grad_type == UNS_GRAD_GGFC) {  // the cell gradient's explicit s: sum fg s / cov
+            sb = sb + (dot(fx, a.gx[nb.x]) + dot(fy, a.gy[nb.x])) / v.cov[nb.x];
+            if (interior) sb = sb + (dot(fx, a.gx[nb.y]) + dot(fy, a.gy[nb.y])) / v.cov[nb.y];
+        }
+        const double4 tx = scl(1.0 / s, bx), ty = scl(1.0 / s, by);
+        const double tTx = bT.x / s, tTy = bT.y / s;
+        const int2 p = v.fpt[f];
+        const double2 X[4] = {v.pxy[p.x], v.cen[nb.y], v.pxy[p.y], v.cen[nb.x]};
+        const double4 Q[4] = {a.s_pp[p.x], a.s_qp[nb.y], a.s_pp[p.y], a.s_qp[nb.x]};
+        const double QT[4] = {a.s_ppT[p.x], a.s_qT[nb.y], a.s_ppT[p.y], a.s_qT[nb.x]};
+        double2 g[4];
+        for (int k = 0; k < 4; ++k) {
+            const int km = (k + 3) & 3, kp = (k + 1) & 3;
+            // d T_x / d y_k = 0.5 (v_{k-1} - v_{k+1}),  d T_y / d x_k = -0.5 (v_{k-1} - v_{k+1})
+            const double4 dv = sub(Q[km], Q[kp]);
+            const double dT = QT[km] - QT[kp];
+            const double gxk = -0.5 * dot5x(ty, tTy, dv, dT) + sb * 0.5 * (X[kp].y - X[km].y);
+            const double gyk = 0.5 * dot5x(tx, tTx, dv, dT) + sb * 0.5 * (X[km].x - X[kp].x);
+            g[k] = make_double2(gxk, gyk);
+        }
+        g1 = g[0];
+        g2 = g[2];
+        gco = make_double2(gco.x + g[1].x, gco.y + g[1].y);
+        gci = make_double2(gci.x + g[3].x, gci.y + g[3].y);
+    }
+    a.gci[f] = gci;
+    a.gco[f] = gco;
+    a.gp1[f] = g1;
+    a.gp2[f] = g2;
+}
+
+// avg_c2v vertex part transposed onto its weights: pp_k = sum w q_c / sum w.
+__global__ void k_geo_vertex(CCView v, AdjView a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.nop) return;
+    double W = 0.0;
+    for (int e = v.v2c_off[k]; e < v.v2c_off[k + 1]; ++e) W = W + v.v2c_wt[e];
+    const double4 pk = a.s_pp[k], pb = a.pp[k];
+    const double pkT = a.s_ppT[k], pbT = a.ppT[k];
+    for (int e = v.v2c_off[k]; e < v.v2c_off[k + 1]; ++e) {
+        const int c = v.v2c[e];
+        a.gv2c[e] = dot5x(pb, pbT, sub(a.s_qp[c], pk), a.s_qT[c] - pkT) / W;
+    }
+}
+
+// Node coordinates: the diamond-path parts of the faces at each node.
+__global__ void k_geo_nodes(CCView v, AdjView a) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= v.nop) return;
+    double2 g = make_double2(0.0, 0.0);
+    for (int e = a.v2f_off[k]; e < a.v2f_off[k + 1]; ++e) {
+        const int x = a.v2f[e], f = x & ~V2F_P2;
+        const double2 t = (x & V2F_P2) ? a.gp2[f] : a.gp1[f];
+        g = make_double2(g.x + t.x, g.y + t.y);
+    }
+    a.gpxy[k] = g;
+}
+
+// Cell centroids (ghosts included) from their faces' parts; cv (Gradient_GG)
+// and cov (Gradient_GG_FC) from the start gradient g = S / cv.
+__global__ void k_geo_cells(CCView v, AdjView a) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.ntot) return;
+    double2 g = make_double2(0.0, 0.0);
+    if (i < v.noc) {
+        for (int k = v.cf_off[i]; k < v.cf_off[i + 1]; ++k) {
+            const int e = v.cf[k], f = e & FACE_MASK;
+            const double2 t = (e & SIDE_BIT) ? a.gco[f] : a.gci[f];
+            g = make_double2(g.x + t.x, g.y + t.y);
+        }
+        const double d = -(dot(a.gx[i], a.s_gx[i]) + dot(a.gy[i], a.s_gy[i]));
+        a.gcv[i] = v.grad_type == UNS_GRAD_GG ? d / v.cv[i] : 0.0;
+        a.gcov[i] = v.grad_type == UNS_GRAD_GGFC ? d / v.cov[i] : 0.0;
+    } else {
+        g = a.gco[v.nfi + (i - v.noc)];
+    }
+    a.gcen[i] = g;
+}
+
 #define LAUNCH(kern, n, ...)                                                         \
     do {                                                                             \
         kern<<<std::max(1, nblocks(n)), kBlock, 0, h->stream>>>(__VA_ARGS__);        \
@@ -610,8 +847,14 @@ int enqueue_vjp(uns_cc_handle* h, double* hist, int k) {
     LAUNCH(k_adj_start_grad, v.nof, v, a);
     const bool use_ggfc = lam || v.grad_type == UNS_GRAD_GGFC;
     const bool use_lsq = v.grad_type == UNS_GRAD_LSQR;
+    if (a.geo) LAUNCH(k_geo_face, v.nof, v, a, use_ggfc ? 1 : 0);
     if (use_ggfc) LAUNCH(k_adj_ggfc, v.nof, v, a);
     LAUNCH(k_adj_vertex, v.nop, v, a, use_ggfc ? 1 : 0);
+    if (a.geo) {
+        LAUNCH(k_geo_vertex, v.nop, v, a);
+        LAUNCH(k_geo_nodes, v.nop, v, a);
+        LAUNCH(k_geo_cells, v.ntot, v, a);
+    }
     LAUNCH(k_adj_final, v.ntot, v, a, use_ggfc ? 1 : 0, use_lsq ? 1 : 0);
     k_adj_reduce<<<1, kBlock, 0, h->stream>>>(v, a, h->adj->nparts, hist, k);
     UNS_CUDA(cudaGetLastError());
@@ -623,7 +866,10 @@ int rec_hook(uns_cc_handle* h, int point, int stage, void*) {
     const AdjView& a = h->adj->a;
     const int s = stage - 1;
     switch (point) {
-        case REC_AFTER_START: LAUNCH(k_rec_start, v.noc, v, a); break;
+        case REC_AFTER_START:
+            LAUNCH(k_rec_start, v.noc, v, a);
+            if (a.geo) LAUNCH(k_rec_geo, std::max(std::max(v.ntot, v.nof), v.nop), v, a);
+            break;
         case REC_BEFORE_FACE_CONV: LAUNCH(k_rec_conv, v.nof, v, a, s); break;
         case REC_BEFORE_CELL_MUL: LAUNCH(k_rec_mul, v.noc, v, a, s); break;
         case REC_AFTER_FACE_VISC: LAUNCH(k_rec_visc, v.nof, v, a, s); break;
@@ -719,6 +965,50 @@ int adj_setup(uns_cc_handle* h) {
 #undef AA
 }
 
+// Arrays of the geometric linearisation, created on the first
+// uns_cc_adjoint_prepare_geometry.
+int geo_setup(uns_cc_handle* h) {
+    CCAdj& A = *h->adj;
+    if (A.geo_alloc) return UNS_OK;
+    const CCView& v = h->v;
+    AdjView& a = A.a;
+    const size_t noc = v.noc, nof = v.nof, nfi = v.nfi, nbf = v.nbf, nop = v.nop, ntot = v.ntot;
+    int nnz = 0;
+    UNS_CUDA(cudaMemcpyAsync(&nnz, v.v2c_off + nop, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    A.nv2c = nnz;
+    int rc;
+#define AA(field, n) if ((rc = adj_alloc(h, a.field, (n)))) return rc
+    AA(JG, 3 * 3 * nfi); AA(BG, 3 * nbf * 27);
+    AA(s_qp, ntot); AA(s_qT, ntot); AA(s_gx, noc); AA(s_gy, noc); AA(s_pp, nop); AA(s_ppT, nop);
+    AA(s_fq, nof); AA(s_fgx, nof); AA(s_fgy, nof); AA(s_fgT, nof); AA(s_fas, nof);
+    AA(fls, nof); AA(frs, nof); AA(gfn, nof); AA(gfcen, nof); AA(gci, nof); AA(gco, nof); AA(gp1, nof); AA(gp2, nof);
+    AA(garea, nof); AA(glsw, nof); AA(gpxy, nop); AA(gcen, ntot); AA(gcv, noc); AA(gcov, noc); AA(gv2c, (size_t)nnz);
+#undef AA
+    A.geo_alloc = true;
+    return UNS_OK;
+}
+
+// Host part of the LSQ weights' transpose (the weights are formed on the
+// host from the centroids and r11, r12, r22 at create, gradient.F90:27-44,
+// 72-78): one side's (wx, wy) = (a1 - a2 r12 / r11, a2) with
+// a1 = dx / r11^2, a2 = (dy - dx r12 / r11) / r22^2.
+void lsw_side_vjp(double dx, double dy, double r11, double r12, double r22, double wxb, double wyb, double& dxb,
+                  double& dyb, double& r11b, double& r12b, double& r22b) {
+    const double num = dy - dx * r12 / r11, a2 = num / (r22 * r22);
+    const double a1b = wxb, a2b = wyb - wxb * r12 / r11;
+    r12b = -wxb * a2 / r11;
+    r11b = wxb * a2 * r12 / (r11 * r11);
+    dxb = a1b / (r11 * r11);
+    r11b = r11b - 2.0 * a1b * dx / (r11 * r11 * r11);
+    const double numb = a2b / (r22 * r22);
+    r22b = -2.0 * a2b * num / (r22 * r22 * r22);
+    dyb = numb;
+    dxb = dxb - numb * r12 / r11;
+    r12b = r12b - numb * dx / r11;
+    r11b = r11b + numb * dx * r12 / (r11 * r11);
+}
+
 int fail_adj(const char* msg, int code) {
     set_last_error(msg);
     return code;
@@ -744,8 +1034,23 @@ void objective_seeds(uns_cc_handle* h, int obj, double seed, AdjView& a) {
 // ====================================================================== C-ABI
 extern "C" {
 
+static int adjoint_prepare_impl(uns_cc_handle* h, double cfl, double* cl, double* cd, bool geo);
+
 int uns_cc_adjoint_prepare(uns_cc_handle* h, double cfl, double* cl, double* cd) {
+    return adjoint_prepare_impl(h, cfl, cl, cd, false);
+}
+
+int uns_cc_adjoint_prepare_geometry(uns_cc_handle* h, double cfl, double* cl, double* cd) {
+    return adjoint_prepare_impl(h, cfl, cl, cd, true);
+}
+
+static int adjoint_prepare_impl(uns_cc_handle* h, double cfl, double* cl, double* cd, bool geo) {
     if (!h || !(cfl > 0.0)) return fail_adj("uns_cc_adjoint_prepare: bad argument", UNS_ERR_ARG);
+    if (geo && h->v.ninst > 0)
+        return fail_adj("uns_cc_adjoint_prepare_geometry: one case per handle (not a packed handle)", UNS_ERR_ARG);
+    if (geo && h->P.flow_type != UNS_FLOW_INVISCID && h->P.grad_type != UNS_GRAD_GGFC)
+        return fail_adj("uns_cc_adjoint_prepare_geometry: a laminar flow's geometry is differentiated with the GG-FC "
+                        "gradient only (the others recompute the gradient inside each stage)", UNS_ERR_ARG);
     ++h->flux_gen;  // the recorded iterations overwrite the step's arrays
     if (h->P.time_mode != UNS_TIME_RK3)
         return fail_adj("uns_cc_adjoint_prepare: the adjoint follows the RK3 iteration (time_mode = RK3)", UNS_ERR_ARG);
@@ -756,10 +1061,12 @@ int uns_cc_adjoint_prepare(uns_cc_handle* h, double cfl, double* cl, double* cd)
     int rc = adj_setup(h);
     if (rc) return rc;
     CCAdj& A = *h->adj;
+    if (geo && (rc = geo_setup(h))) return rc;
     const double al = h->P.aoa_deg * (4.0 * std::atan(1.0)) / 180.0;
     A.a.dua = -std::sin(al);
     A.a.dva = std::cos(al);
     A.recorded = false;
+    A.geo_recorded = false;
     // The local time step of a viscous flow reads the face viscosity of the
     // previous iteration (spectral02's viscous term), which is not part of
     // the state vector: one plain iteration first makes it the converged
@@ -767,13 +1074,17 @@ int uns_cc_adjoint_prepare(uns_cc_handle* h, double cfl, double* cl, double* cd)
     if (h->P.flow_type != UNS_FLOW_INVISCID &&
         (rc = cc_record_iteration(h, cfl, [](uns_cc_handle*, int, int, void*) { return (int)UNS_OK; }, nullptr)))
         return rc;
-    if ((rc = cc_record_iteration(h, cfl, rec_hook, nullptr))) return rc;
+    A.a.geo = geo ? 1 : 0;
+    rc = cc_record_iteration(h, cfl, rec_hook, nullptr);
+    A.a.geo = 0;
+    if (rc) return rc;
     double fx = 0.0, fy = 0.0;
     if ((rc = uns_cc_forces(h, &fx, &fy))) return rc;
     A.fx = fx;
     A.fy = fy;
     A.cfl = cfl;
     A.recorded = true;
+    A.geo_recorded = geo;
     if (cl) *cl = 2.0 * (fy * std::cos(al) - fx * std::sin(al));
     if (cd) *cd = 2.0 * (fx * std::cos(al) + fy * std::sin(al));
     return cc_check_dev_err(h);
@@ -810,6 +1121,77 @@ int uns_cc_adjoint_vjp(uns_cc_handle* h, int objective, double seed, const doubl
     }
     if (oalpha) *oalpha = out[0];
     return cc_check_dev_err(h);
+}
+
+int uns_cc_adjoint_geometry(uns_cc_handle* h, int objective, double seed, const double* wq, const double* wg,
+                            uns_cc_mesh_adj* out) {
+    if (!h || !wq || !wg || !out || (objective != UNS_OBJ_CL && objective != UNS_OBJ_CD))
+        return fail_adj("uns_cc_adjoint_geometry: bad argument", UNS_ERR_ARG);
+    if (!h->adj || !h->adj->geo_recorded)
+        return fail_adj("uns_cc_adjoint_geometry: call uns_cc_adjoint_prepare_geometry first", UNS_ERR_ARG);
+    const uns_cc_mesh_adj& o = *out;
+    if (!o.px || !o.py || !o.cx || !o.cy || !o.cv || !o.cov || !o.fnx || !o.fny || !o.farea || !o.fcx || !o.fcy ||
+        !o.r11 || !o.r12 || !o.r22 || !o.v2c_wt)
+        return fail_adj("uns_cc_adjoint_geometry: every output array is required", UNS_ERR_ARG);
+    ++h->flux_gen;
+    CCAdj& A = *h->adj;
+    const CCView& v = h->v;
+    AdjView& a = A.a;
+    const int noc = v.noc, nof = v.nof, nbf = v.nbf, nop = v.nop, ntot = v.ntot;
+    objective_seeds(h, objective, seed, a);
+    std::vector<double4> g(nbf);
+    std::vector<double> gT(nbf);
+    for (int b = 0; b < nbf; ++b) {
+        g[b] = make_double4(wg[5 * b], wg[5 * b + 1], wg[5 * b + 2], wg[5 * b + 3]);
+        gT[b] = wg[5 * b + 4];
+    }
+    UNS_CUDA(cudaMemcpyAsync(a.lq, wq, sizeof(double4) * noc, cudaMemcpyHostToDevice, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(a.lg, g.data(), sizeof(double4) * nbf, cudaMemcpyHostToDevice, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(a.lgT, gT.data(), sizeof(double) * nbf, cudaMemcpyHostToDevice, h->stream));
+    a.geo = 1;
+    int rc = enqueue_vjp(h, nullptr, 0);
+    a.geo = 0;
+    if (rc) return rc;
+    std::vector<double2> pxy(nop), cen(ntot), fn(nof), fc(nof), cen_val(ntot);
+    std::vector<double4> lsw(nof);
+    std::vector<double> cv(noc), cov(noc), area(nof), wv(A.nv2c);
+    UNS_CUDA(cudaMemcpyAsync(pxy.data(), a.gpxy, sizeof(double2) * nop, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(cen.data(), a.gcen, sizeof(double2) * ntot, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(fn.data(), a.gfn, sizeof(double2) * nof, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(fc.data(), a.gfcen, sizeof(double2) * nof, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(lsw.data(), a.glsw, sizeof(double4) * nof, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(cv.data(), a.gcv, sizeof(double) * noc, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(cov.data(), a.gcov, sizeof(double) * noc, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(area.data(), a.garea, sizeof(double) * nof, cudaMemcpyDeviceToHost, h->stream));
+    if (A.nv2c) UNS_CUDA(cudaMemcpyAsync(wv.data(), a.gv2c, sizeof(double) * A.nv2c, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaMemcpyAsync(cen_val.data(), v.cen, sizeof(double2) * ntot, cudaMemcpyDeviceToHost, h->stream));
+    UNS_CUDA(cudaStreamSynchronize(h->stream));
+    if ((rc = cc_check_dev_err(h))) return rc;
+    for (int k = 0; k < nop; ++k) { o.px[k] = pxy[k].x; o.py[k] = pxy[k].y; }
+    for (int i = 0; i < ntot; ++i) { o.cx[i] = cen[i].x; o.cy[i] = cen[i].y; }
+    for (int i = 0; i < noc; ++i) { o.cv[i] = cv[i]; o.cov[i] = cov[i]; o.r11[i] = 0.0; o.r12[i] = 0.0; o.r22[i] = 0.0; }
+    for (int f = 0; f < nof; ++f) {
+        o.fnx[f] = fn[f].x; o.fny[f] = fn[f].y; o.farea[f] = area[f]; o.fcx[f] = fc[f].x; o.fcy[f] = fc[f].y;
+    }
+    for (int e = 0; e < A.nv2c; ++e) o.v2c_wt[e] = wv[e];
+    if (v.grad_type == UNS_GRAD_LSQR) {  // the weights' adjoints onto the centroids and r11, r12, r22
+        const std::vector<double>& r = h->lsq_r;
+        for (int f = 0; f < nof; ++f) {
+            const int in = h->fnb_host[f].x, ot = h->fnb_host[f].y;
+            const double dx = cen_val[ot].x - cen_val[in].x, dy = cen_val[ot].y - cen_val[in].y;
+            double dxb, dyb, r11b, r12b, r22b;
+            lsw_side_vjp(dx, dy, r[3 * in], r[3 * in + 1], r[3 * in + 2], lsw[f].x, lsw[f].y, dxb, dyb, r11b, r12b, r22b);
+            o.cx[ot] += dxb; o.cx[in] -= dxb; o.cy[ot] += dyb; o.cy[in] -= dyb;
+            o.r11[in] += r11b; o.r12[in] += r12b; o.r22[in] += r22b;
+            if (f < v.nfi) {
+                lsw_side_vjp(-dx, -dy, r[3 * ot], r[3 * ot + 1], r[3 * ot + 2], lsw[f].z, lsw[f].w, dxb, dyb, r11b, r12b,
+                             r22b);
+                o.cx[in] += dxb; o.cx[ot] -= dxb; o.cy[in] += dyb; o.cy[ot] -= dyb;
+                o.r11[ot] += r11b; o.r12[ot] += r12b; o.r22[ot] += r22b;
+            }
+        }
+    }
+    return UNS_OK;
 }
 
 int uns_cc_adjoint_solve(uns_cc_handle* h, int objective, int max_iter, double tol, double* dj_dalpha, double* hist,

@@ -168,6 +168,10 @@ struct uns_cc_handle {
     uns::CCAdj* adj = nullptr;  // discrete-adjoint state, created by uns_cc_adjoint_prepare
     double* d_post = nullptr;   // post-processing scratch (uns_cc_post.cu), created on first use
     double* d_tec = nullptr;    // tecplt vertex table (uns_cc_post.cu), created on first use
+    // Host copies the geometry adjoint transposes through (the LSQ weights are
+    // formed on the host from them): r11, r12, r22 per cell, fin/fout per face.
+    std::vector<double> lsq_r;  // [noc][3]
+    std::vector<int2> fnb_host; // [nof]
 
     template <class T>
     int alloc(T*& p, size_t n) {

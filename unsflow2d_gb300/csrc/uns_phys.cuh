@@ -353,8 +353,10 @@ struct CCBnd {
     S gT;
     bool ok, upd;
 };
-template <class S, class R>
-__device__ __forceinline__ CCBnd<S> cc_boundary(const Gas& g, int bc, double nx, double ny, double area,
+// N is the type of the face geometry: double, or a tangent type when the
+// adjoint differentiates the closure with respect to the normal and length.
+template <class S, class R, class N = double>
+__device__ __forceinline__ CCBnd<S> cc_boundary(const Gas& g, int bc, N nx, N ny, N area,
                                                 const V4<S>& qcl, const V4<S>& cin, S uinf, S vinf) {
     CCBnd<S> o;
     o.ok = true;

@@ -87,6 +87,30 @@ class CCMesh(_HostMesh):
                                              C.byref(h)), lib, "cc airfoil dy")
         return cls(h.value)
 
+    def moved(self, px, py) -> "CCMesh":
+        """This mesh with its nodes at (px, py): same topology, the moved
+        triangles' centroids and areas, then the geometric preprocessing."""
+        x = np.ascontiguousarray(px, dtype=np.float64)
+        y = np.ascontiguousarray(py, dtype=np.float64)
+        n = self.arrays["nop"]
+        assert x.shape == (n,) and y.shape == (n,)
+        h = C.c_void_p()
+        abi.check(self._lib.uns_host_cc_moved(self._h, x.ctypes.data_as(abi._D), y.ctypes.data_as(abi._D), C.byref(h)),
+                  self._lib, "cc moved")
+        return CCMesh(h.value)
+
+    def node_adjoint(self, geom: dict) -> tuple[np.ndarray, np.ndarray]:
+        """dJ/d(px, py) from the adjoints of this mesh's geometric arrays
+        (solver.CCSolver.adjoint_geometry): the transposed geometric
+        preprocessing (uns_host_cc_mesh_vjp)."""
+        st, keep = abi.cc_mesh_adj(self.arrays, geom)
+        n = self.arrays["nop"]
+        gx, gy = np.zeros(n), np.zeros(n)
+        abi.check(self._lib.uns_host_cc_mesh_vjp(self._h, C.byref(st), gx.ctypes.data_as(abi._D),
+                                                 gy.ctypes.data_as(abi._D)), self._lib, "cc mesh vjp")
+        del keep
+        return gx, gy
+
     @property
     def ncells(self) -> int:
         return self.arrays["noc"]

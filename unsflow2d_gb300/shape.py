@@ -7,16 +7,22 @@ the total derivative with respect to the mesh coordinates X is
     dJ/dX = dJ^/dX + lambda^T dG/dX        (state s* held fixed),
 
 where G is one main-loop iteration and J^ the objective computed inside it.
-Here the state dependence comes from the adjoint and the explicit geometry
-partials from central differences of ONE forward iteration at s* on meshes
-whose wall nodes are displaced (no re-convergence): a wall node moves its
-whole radial line (weight 1 - s along it), which changes the geometry of the
-two cell columns beside the line, and one iteration's output depends on the
-geometry within three columns of a cell.  So wall nodes eight columns apart
+
+method="transposed" (default): one transposed iteration with the geometric
+linearisation (uns_cc_adjoint_geometry) gives lambda^T G_A + J_A for every
+geometric array A of the mesh, and the transposed geometric preprocessing
+(uns_host_cc_mesh_vjp) carries them to the node coordinates; a wall node's
+y moves its radial line with weight 1 - s, so dJ/d(wall y_i) is the sum of
+dJ/dy over the line's nodes times those weights.  Exact to rounding.
+
+method="differenced": the explicit geometry partials from central
+differences of ONE forward iteration at s* on meshes whose wall nodes are
+displaced (no re-convergence).  One iteration's output depends on the
+geometry within three columns of a cell, so wall nodes eight columns apart
 are displaced together (eight colours), each cell's lambda-weighted change is
 credited to the nearest displaced line, and 16 forward iterations give the
-derivative for every wall node.  The displacement step h is a small fraction
-of the first wall spacing.
+derivative for every wall node; the step h is a small fraction of the first
+wall spacing.
 
 This module is the caller side of the adjoint (Python over the C-ABI); the
 limiter is frozen at the state's phi, as in the adjoint.
@@ -121,9 +127,20 @@ class ShapeCase:
         s.close()
         return out
 
-    def wall_gradient(self, objective: str, lam_q: np.ndarray, lam_g: np.ndarray, h: float = None,
-                      spacing: int = 8) -> np.ndarray:
+    def line_weights(self) -> np.ndarray:
+        """[nop] weight 1 - s of every node along its radial line (the
+        displacement of node (i, j) per unit displacement of wall node i)."""
+        base = self.mesh().arrays["py"]
+        moved = self.mesh(np.ones(self.ni)).arrays["py"]
+        return moved - base
+
+    def wall_gradient(self, objective: str, lam_q: np.ndarray, lam_g: np.ndarray, method: str = "transposed",
+                      h: float = None, spacing: int = 8) -> np.ndarray:
         """dJ/dy of every wall node (ni values)."""
+        if method == "transposed":
+            return self._wall_gradient_transposed(objective, lam_q, lam_g)
+        if method != "differenced":
+            raise ValueError(method)
         ni = self.ni
         dwall = self.mesh_kw.get("dwall", 1e-3)
         h = 1e-4 * dwall if h is None else h
@@ -152,6 +169,16 @@ class ShapeCase:
             grad += np.bincount(near[col], weights=phi_c, minlength=ni)
             grad += np.bincount(near[bcol], weights=phi_g + phi_j, minlength=ni)
         return grad
+
+    def _wall_gradient_transposed(self, objective: str, lam_q: np.ndarray, lam_g: np.ndarray) -> np.ndarray:
+        s = self.solver()
+        s.adjoint_prepare_geometry(self.cfl)
+        geom = s.adjoint_geometry(objective, 1.0, lam_q, lam_g)
+        s.close()
+        _, gy = self.mesh().node_adjoint(geom)
+        w = self.line_weights()
+        node = np.arange(len(w))
+        return np.bincount(node % self.ni, weights=gy * w, minlength=self.ni)
 
     def bump_gradient(self, objective: str, lam_q: np.ndarray, lam_g: np.ndarray, **kw) -> np.ndarray:
         """dJ/d(amplitude) of the 16 Hicks-Henne bumps (bump_basis order)."""

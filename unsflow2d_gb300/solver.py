@@ -219,6 +219,21 @@ class CCSolver(_Solver):
         self._call("adjoint_get", _dp(lq), _dp(lg))
         return lq, lg
 
+    def adjoint_prepare_geometry(self, cfl: float) -> tuple[float, float]:
+        """adjoint_prepare plus the geometric linearisation (uns_cc_adjoint_prepare_geometry)."""
+        cl, cd = C.c_double(), C.c_double()
+        self._call("adjoint_prepare_geometry", C.c_double(cfl), C.byref(cl), C.byref(cd))
+        return cl.value, cd.value
+
+    def adjoint_geometry(self, objective: str, seed: float, wq: np.ndarray, wg: np.ndarray) -> dict:
+        """G_X^T w + seed J_X^T for every geometric array X of the mesh
+        (uns_cc_adjoint_geometry): a dict of arrays shaped like the mesh's."""
+        wq = np.ascontiguousarray(wq, dtype=np.float64).reshape(self.noc, 4)
+        wg = np.ascontiguousarray(wg, dtype=np.float64).reshape(self.nbf, 5)
+        st, out = abi.cc_mesh_adj(self.m)
+        self._call("adjoint_geometry", abi.OBJ[objective], C.c_double(seed), _dp(wq), _dp(wg), C.byref(st))
+        return out
+
     def iteration(self, cfl: float) -> float:
         """One main-loop iteration (CCFVM/main.F90:60-115) through the per-routine entry points."""
         self.con2prim()
