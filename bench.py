@@ -129,8 +129,9 @@ def adjoint_cost(solver, w: dict, cfl: float, prof: dict) -> dict:
         t[n] = time.perf_counter() - t0
     per = (t[250] - t[50]) / 200 * 1e3
     # dC_L / d(wall-node y) of all wall nodes and the 16 Hicks-Henne amplitudes:
-    # one-iteration geometry partials on 16 displaced meshes, weighted by the
-    # adjoint vector (unsflow2d_gb300.shape)
+    # one transposed iteration with the geometric linearisation at the adjoint
+    # vector, then the transposed geometric preprocessing on the host
+    # (unsflow2d_gb300.shape, method "transposed")
     from unsflow2d_gb300 import shape
     lq, lg = solver.adjoint_get()
     case = shape.ShapeCase(w["ni"], w["nj"], w["params"], (solver.get_state(), solver.get("qp"), solver.get("phi")), cfl,
@@ -146,7 +147,8 @@ def adjoint_cost(solver, w: dict, cfl: float, prof: dict) -> dict:
             "ms_per_residual_evaluation": round(resid, 4),
             "ratio_to_forward_iteration": round(per / fwd, 3), "ratio_to_residual_evaluation": round(per / resid, 3),
             "prepare_s": round(prep, 3), "objective": "C_L", "CL": cl, "CD": cd,
-            "shape_gradient_s": round(shape_s, 2), "n_bumps": int(len(bumps)), "wall_nodes": int(w["ni"]),
+            "shape_gradient_s": round(shape_s, 2), "shape_method": "transposed", "n_bumps": int(len(bumps)),
+            "wall_nodes": int(w["ni"]),
             "timing": "host clock around uns_cc_adjoint_solve graphs of 50 and 250 transposed iterations (difference); "
                       "forward phases from CUDA events; a residual evaluation = con2prim, averages, gradient once + "
                       "one stage of flux, viscous flux and gather"}
