@@ -296,9 +296,10 @@ int uns_nc_debug_unpublish(uns_nc_handle* h, int entity, int pass);
  * whose every slot a call writes before reading it, so nothing needs to start
  * at zero.  ncells > UNS_RMS_NOALLOC_MAX_CELLS, NULL pointers or a misaligned
  * array give UNS_ERR_ARG before any device work.  The first call on each
- * device looks up the scratch address; make it before any stream capture.
- * The address belongs to the context it was looked up in: the first call in
- * a new context of the device (after cudaDeviceReset) looks it up again.
+ * device looks up the scratch address (cudaGetSymbolAddress, which allocates
+ * nothing).  The address belongs to the context it was looked up in: the
+ * first call in a new context of the device (after cudaDeviceReset) looks it
+ * up again.
  * Every call synchronises `stream` before it returns.
  * Calls that overlap on one device (other threads or streams) share the
  * scratch and race: serialise them. */
