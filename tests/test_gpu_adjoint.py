@@ -395,3 +395,22 @@ def test_geometry_rejects_a_laminar_flow_with_a_stage_gradient():
     with pytest.raises(abi.UnsError) as e:
         a.adjoint_prepare_geometry(CFL)
     assert e.value.code == abi.UNS_ERR_ARG
+
+
+def test_geometry_entry_points_check_their_preconditions():
+    kw = CASES["euler_roe_gg"]
+    m = mesh.CCMesh.airfoil(16, 8)
+    a = _frozen(m, kw)
+    noc, nbf = a.noc, a.nbf
+    with pytest.raises(abi.UnsError) as e:  # no geometric linearisation recorded
+        a.adjoint_geometry("cl", 1.0, np.zeros((noc, 4)), np.zeros((nbf, 5)))
+    assert e.value.code == abi.UNS_ERR_ARG
+    a.adjoint_prepare(CFL)  # the state linearisation alone is not enough
+    with pytest.raises(abi.UnsError) as e:
+        a.adjoint_geometry("cl", 1.0, np.zeros((noc, 4)), np.zeros((nbf, 5)))
+    assert e.value.code == abi.UNS_ERR_ARG
+    import ctypes as C
+    from unsflow2d_gb300.solver import CCPacked
+    p = abi.make_params(ilimit=0, **kw)
+    pk = CCPacked([m, m], [p, p])  # one case per handle: a packed handle is refused
+    assert pk._lib.uns_cc_adjoint_prepare_geometry(pk._h, C.c_double(CFL), None, None) == abi.UNS_ERR_ARG

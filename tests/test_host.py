@@ -358,3 +358,13 @@ def test_mesh_vjp_rejects_a_mesh_whose_centroids_are_not_its_triangles(cc, tmp_p
     gx, gy = np.zeros(cc.arrays["nop"]), np.zeros(cc.arrays["nop"])
     lib = abi.host_lib()
     assert lib.uns_host_cc_mesh_vjp(cc._h, None, gx.ctypes.data_as(abi._D), gy.ctypes.data_as(abi._D)) == abi.UNS_ERR_ARG
+
+
+def test_moved_mesh_with_a_collapsed_cell_is_a_mesh_error(cc):
+    a = cc.arrays
+    px, py = a["px"].copy(), a["py"].copy()
+    # put node 1 of the wall (the corner of triangles behind it) onto node 0
+    px[1], py[1] = px[0], py[0]
+    with pytest.raises(abi.UnsError) as e:
+        cc.moved(px, py)
+    assert e.value.code == abi.UNS_ERR_MESH
