@@ -18,10 +18,11 @@ import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
 INDEX = json.loads((ROOT / "tests" / "golden" / "reference_index.json").read_text())
-# Files written about this repository by others (the survey and reviews) cite
+CODE = (".py", ".cu", ".cuh", ".cpp", ".hpp", ".h", ".inc")
+# Documents are checked when they carry this marker: the repository's own
+# documentation does; documents written about the repository by others cite
 # the reference in their own way and are not part of the product.
-SKIP = {"SURVEY.md", "VERDICT.md", "ADVICE.md", "BASELINE.json", "BASELINE.md"}
-TEXT = (".py", ".cu", ".cuh", ".cpp", ".hpp", ".h", ".inc", ".md", ".txt")
+MARK = "<!-- reference citations in this file are checked by tests/test_citations.py -->"
 
 FULL = re.compile(r"((?:CCFVM|NCFVM|MeshGen)/[A-Za-z0-9_/.]+?\.(?:[fF]90|f|inp)|(?:CCFVM|NCFVM|MeshGen)/makefile)"
                   r":(\d+(?:-\d+)?(?:,\s?\d+(?:-\d+)?)*)")
@@ -49,7 +50,13 @@ def _tracked():
     else:
         files = [str(f.relative_to(ROOT)) for f in ROOT.rglob("*")
                  if f.is_file() and not (set(f.relative_to(ROOT).parts[:-1]) & NOT_SOURCE)]
-    return sorted(f for f in files if f not in SKIP and f.endswith(TEXT) and not f.startswith("_work/"))
+    def checked(f):
+        if f.startswith("_work/"):
+            return False
+        if f.endswith(CODE):
+            return True
+        return f.endswith(".md") and MARK in (ROOT / f).read_text(errors="replace")
+    return sorted(f for f in files if checked(f))
 
 
 def _citations():
@@ -71,6 +78,12 @@ def _citations():
 
 
 CITES = list(_citations())
+
+
+def test_the_documentation_is_checked():
+    docs = [f for f in _tracked() if f.endswith(".md")]
+    assert len(docs) >= 3 and any("/" not in f for f in docs), docs
+    assert any(c[0].endswith(".md") for c in CITES)
 
 
 def test_some_citations_found():
