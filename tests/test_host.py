@@ -368,3 +368,13 @@ def test_moved_mesh_with_a_collapsed_cell_is_a_mesh_error(cc):
     with pytest.raises(abi.UnsError) as e:
         cc.moved(px, py)
     assert e.value.code == abi.UNS_ERR_MESH
+
+
+def test_mesh_vjp_accepts_the_plot3d_triangulation(tmp_path):
+    path = tmp_path / "g.x"
+    mesh.write_airfoil_plot3d(str(path), 24, 12)
+    m = mesh.CCMesh.plot3d(str(path))
+    rng = np.random.default_rng(5)
+    abar = {k: rng.standard_normal(n) for k, n in abi.cc_geom_sizes(m.arrays).items()}
+    gx, gy = m.node_adjoint(abar)
+    assert np.isfinite(gx).all() and np.isfinite(gy).all()
