@@ -1817,10 +1817,23 @@ int enqueue_minmax(uns_cc_handle* h, CCView& v) {
         UNS_CUDA(cudaGetLastError());                                                              \
     } while (0)
 
+// Block size of a per-element kernel whose threads are independent (no
+// block-level reduction): kBlock, halved down to one warp while the launch
+// would have fewer than two blocks per SM, so that a small mesh spreads its
+// FP64 work over every SM sub-partition instead of stacking warps on a few
+// SMs (meshes above about 2 x 256 x SMs elements keep kBlock).  The
+// per-element arithmetic, and so every result, is the same at any width.
+inline int spread_bs(const uns_cc_handle* h, int n) {
+    int bs = kBlock;
+    while (bs > 32 && (n + bs - 1) / bs < 2 * h->nsm) bs >>= 1;
+    return bs;
+}
+#define LAUNCH_SPREAD(kern, n, ...) LAUNCH_BS(kern, (n), spread_bs(h, (n)), __VA_ARGS__)
+
 #define LAUNCH_CELL_GRAD(v, flags, cfl)                                                 \
     do {                                                                               \
         if ((v).mixed) LAUNCH(k_cell_grad_mixed, (v).noc, (v), (int)(flags), (cfl));   \
-        else LAUNCH(k_cell_grad, (v).noc, (v), (int)(flags), (cfl));                   \
+        else LAUNCH_SPREAD(k_cell_grad, (v).noc, (v), (int)(flags), (cfl));            \
     } while (0)
 
 int enqueue_gradient(uns_cc_handle* h, CCView& v, int extra_flags, double cfl, bool do_reduce) {
@@ -1962,7 +1975,7 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
     if (grad_by_sides(h, v)) {
         LAUNCH_BS(k_cell_grad_side, v.noc, v.blk_grad, v, gflags, 0.0);
     } else {
-        LAUNCH(k_face_prim_spec, v.nof, v);
+        LAUNCH_SPREAD(k_face_prim_spec, v.nof, v);
         if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
         LAUNCH_CELL_GRAD(v, gflags, 0.0);
     }
@@ -2020,9 +2033,9 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
     int rc;
     LAUNCH(k_begin, v.ntot, v, (int)(BEGIN_PRIM | BEGIN_OLD | BEGIN_POS));
     LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v);
-    LAUNCH(k_face_prim_spec, v.nof, v);
+    LAUNCH_SPREAD(k_face_prim_spec, v.nof, v);
     if (v.grad_type == UNS_GRAD_GGFC) LAUNCH(k_face_ggfc, v.nof, v);
-    LAUNCH(k_cell_grad, v.noc, v, (int)(CG_DT | CG_GRAD), cfl);
+    LAUNCH_SPREAD(k_cell_grad, v.noc, v, (int)(CG_DT | CG_GRAD), cfl);
     if ((rc = hook(h, REC_AFTER_START, 0, ctx))) return rc;
     for (int irk = 1; irk <= 3; ++irk) {
         if ((rc = hook(h, REC_BEFORE_FACE_CONV, irk, ctx))) return rc;
@@ -2034,7 +2047,7 @@ int cc_record_iteration(uns_cc_handle* h, double cfl, CCRecHook hook, void* ctx)
                 CCView w = v;
                 w.grad_type = UNS_GRAD_GGFC;
                 LAUNCH(k_face_ggfc, w.nof, w);
-                LAUNCH(k_cell_grad, w.noc, w, (int)CG_GRAD, cfl);
+                LAUNCH_SPREAD(k_cell_grad, w.noc, w, (int)CG_GRAD, cfl);
             }
             LAUNCH(k_face_visc, v.nof, v);
             if ((rc = hook(h, REC_AFTER_FACE_VISC, irk, ctx))) return rc;
@@ -2123,6 +2136,12 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
         set_last_error("uns_cc_create: cudaStreamCreate failed (no usable GPU?)");
         delete h;
         return UNS_ERR_CUDA;
+    }
+    {
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            nsm > 0)
+            h->nsm = nsm;
     }
     Gas& g = h->g;
     g = make_gas(p, &h->qinf);
@@ -2363,7 +2382,7 @@ int uns_cc_get_field(uns_cc_handle* h, int field, double* out) {
     const CCView& v = h->v;
     if (v.mixed && (field == UNS_CC_GRAD || field == UNS_CC_PHI)) LAUNCH(k_unpack_f32, v.noc, v);
     // the graph step of this form forms the face radii inside k_cell_grad_side
-    if (v.mixed && v.sideg && field == UNS_CC_FLA) LAUNCH(k_face_prim_spec, v.nof, v);
+    if (v.mixed && v.sideg && field == UNS_CC_FLA) LAUNCH_SPREAD(k_face_prim_spec, v.nof, v);
     auto d2h = [&](void* dst, const void* src, size_t bytes) {
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream);
     };
@@ -2481,7 +2500,7 @@ int uns_cc_avg_c2v(uns_cc_handle* h) {
     ++h->flux_gen;
     CCView v = h->v;
     LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v);
-    LAUNCH(k_face_prim_spec, v.nof, v);
+    LAUNCH_SPREAD(k_face_prim_spec, v.nof, v);
     return UNS_OK;
 }
 
@@ -3005,7 +3024,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
         });
         if (!rc) rc = timed(1, [&]() -> int { LAUNCH_BS(k_vertex_avg, v.nop, v.blk_vert, v); return UNS_OK; });
         const bool sides = grad_by_sides(h, v);
-        if (!rc && !sides) rc = timed(2, [&]() -> int { LAUNCH(k_face_prim_spec, v.nof, v); return UNS_OK; });
+        if (!rc && !sides) rc = timed(2, [&]() -> int { LAUNCH_SPREAD(k_face_prim_spec, v.nof, v); return UNS_OK; });
         if (!rc && v.grad_type == UNS_GRAD_GGFC) rc = timed(3, [&]() -> int { LAUNCH(k_face_ggfc, v.nof, v); return UNS_OK; });
         if (!rc) rc = timed(4, [&]() -> int {
             const int gflags = CG_DT | CG_GRAD | (v.ilimit ? CG_LIM : 0) | (rk3 ? 0 : CG_DIAG);

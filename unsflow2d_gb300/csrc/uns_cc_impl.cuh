@@ -146,6 +146,7 @@ struct uns_cc_handle {
     // LU-SGS levels
     int* woff = nullptr;   // LU-SGS warp schedule: per-warp ranges of v.sched
     int coop_blocks = 0;
+    int nsm = 1;           // SMs of the device (launch widths of small meshes)
     double4 qinf;
     // graph fast path
     cudaGraphExec_t graph = nullptr;
