@@ -925,13 +925,15 @@ def run_reference(args, w) -> dict:
 # The other benchmark configurations, measured in the same default run after
 # the headline (one GPU): key -> workload.  "3_fp64" is configuration 3's mesh
 # in the plain FP64 form, the denominator of the mixed and batched speed-ups.
-CONFIG_RUNS = [("1", "cc_small"), ("3_fp64", "cc"), ("3", "cc_mixed"), ("4", "cc_batched"), ("5", "cc_adjoint")]
+CONFIG_RUNS = [("1", "cc_small"), ("2_mixed_sweep", "nc_mixed_sweep"), ("2_mixed", "nc_mixed"), ("3_fp64", "cc"),
+               ("3", "cc_mixed"), ("4", "cc_batched"), ("5", "cc_adjoint")]
 SUMMARY_KEYS = ("value", "unit", "ms_per_step", "steps", "dtype", "gpu_launches", "clocks", "roofline",
                 "accuracy_vs_fp64", "adjoint", "time_to_1e-8", "convergence", "convergence_to_1e-8")
 
 
 def run_configs(args, dist, rank, local_rank) -> dict:
-    """Configurations 1, 3, 4 and 5 (and configuration 3's mesh in plain FP64),
+    """Configurations 1, 3, 4 and 5, configuration 2's mixed forms (FP32 sweeps;
+    FP32 residual and sweeps) and configuration 3's mesh in plain FP64,
     each timed like the headline: CUDA events on the library stream around
     `--steps` graph-replayed iterations after the warm-up, clocks sampled
     during the timed region.  No end-to-end leg and no CPU baseline here."""

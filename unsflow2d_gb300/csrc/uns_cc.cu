@@ -1175,6 +1175,9 @@ __global__ void __launch_bounds__(kBlock) k_cell_rk23(CCView v) {
             t = warp_sum(t);
             if (threadIdx.x == 0) v.partial[blockIdx.x] = t;
         }
+    } else if (v.wpart) {  // one partial per warp (v.ninst == 0)
+        rr = warp_sum(rr);
+        if ((threadIdx.x & 31) == 0) v.partial[i >> 5] = rr;
     } else {  // k_cell_res's
         __shared__ double s[kBlock / 32];
         rr = warp_sum(rr);
@@ -1244,6 +1247,18 @@ __global__ void __launch_bounds__(kBlock) k_res_partial(CCView v) {
 // Deterministic final sum of the block partials; in the graph path it also
 // records the history, the first-iteration normalisation and the stop flag
 // (solution.F90:159-166, main.F90:57).
+// Block partial k: stored, or the sum of its eight warp partials in warp
+// order (v.wpart), the warps past the last cell counting zero as they do in
+// a block's own sum.
+__device__ __forceinline__ double block_partial(const CCView& v, int k) {
+    if (!v.wpart) return v.partial[k];
+    const int nw = (v.noc + 31) >> 5;
+    double t = 0.0;
+#pragma unroll
+    for (int u = 0; u < kBlock / 32; ++u) t = t + (8 * k + u < nw ? v.partial[8 * k + u] : 0.0);
+    return t;
+}
+
 __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, double* out) {
     const int inst = blockIdx.x;  // one block per instance
     if (stopped(v, inst)) return;
@@ -1256,11 +1271,11 @@ __global__ void __launch_bounds__(kBlock) k_res_final(CCView v, int nparts, doub
     for (; k + 7 * kBlock < n; k += 8 * kBlock) {
         double p[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) p[u] = v.partial[k0 + k + u * kBlock];
+        for (int u = 0; u < 8; ++u) p[u] = block_partial(v, k0 + k + u * kBlock);
 #pragma unroll
         for (int u = 0; u < 8; ++u) t = t + p[u];
     }
-    for (; k < n; k += kBlock) t = t + v.partial[k0 + k];
+    for (; k < n; k += kBlock) t = t + block_partial(v, k0 + k);
     s[threadIdx.x] = t;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -1886,6 +1901,19 @@ int enqueue_wall_res(uns_cc_handle* h, CCView& v) {
 }
 
 // The wall cells' stages: 2-3 in the FP64 form, 1-3 in the mixed form.
+// Whether the FP64 k_cell_rk23 of this handle runs spread over the SMs with
+// per-warp norm partials: one case (no packed instances) on a small mesh.
+inline bool rk23_warp_partials(const uns_cc_handle* h, const CCView& v) {
+    return v.ninst == 0 && spread_bs(h, v.noc) < kBlock;
+}
+
+// k_res_final's view after the FP64 one-pass RK stages.
+inline CCView final_view(const uns_cc_handle* h, const CCView& v) {
+    CCView w = v;
+    w.wpart = rk23_warp_partials(h, v) ? 1 : 0;
+    return w;
+}
+
 int enqueue_wall_rk(uns_cc_handle* h, CCView& v) {
     if (v.nwcell == 0) return UNS_OK;
     const int nb = (v.nwcell + 31) / 32;
@@ -1900,7 +1928,13 @@ int enqueue_wall_rk(uns_cc_handle* h, CCView& v) {
 int enqueue_rk23(uns_cc_handle* h, CCView& v) {
     int rc = enqueue_wall_rk(h, v);
     if (rc) return rc;
-    LAUNCH(k_cell_rk23<double>, v.noc, v);
+    if (rk23_warp_partials(h, v)) {
+        CCView w = v;
+        w.wpart = 1;
+        LAUNCH_SPREAD(k_cell_rk23<double>, v.noc, w);
+    } else {
+        LAUNCH(k_cell_rk23<double>, v.noc, v);
+    }
     return UNS_OK;
 }
 
@@ -1925,7 +1959,8 @@ int enqueue_fvresidual(uns_cc_handle* h, CCView& v, double cfl, int irk, int par
     bool smooth = v.irs && eps > 0.0;
     *fused = !smooth && irk > 0;
     if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0, 0);
-    else LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    else if ((partial && !smooth) || v.ninst) LAUNCH(k_cell_res, v.noc, v, *fused ? irk : 0, (partial && !smooth) ? 1 : 0);
+    else LAUNCH_SPREAD(k_cell_res, v.noc, v, *fused ? irk : 0, 0);
     if (smooth) {
         UNS_CUDA(cudaMemcpyAsync(v.res0, v.res, sizeof(double4) * v.noc, cudaMemcpyDeviceToDevice, h->stream));
         LAUNCH(k_cirs, v.noc, v, (const double4*)v.res0, v.restmp, eps);
@@ -1997,6 +2032,9 @@ int enqueue_iteration(uns_cc_handle* h, CCView& v, double cfl_for_eps) {
         bool fused = false;
         if ((rc = enqueue_fvresidual(h, v, cfl_for_eps, 1, 0, &fused))) return rc;
         if ((rc = enqueue_rk23(h, v))) return rc;
+        k_res_final<<<std::max(1, v.ninst), kBlock, 0, h->stream>>>(final_view(h, v), h->nparts, nullptr);
+        UNS_CUDA(cudaGetLastError());
+        return UNS_OK;
     } else if (h->P.time_mode == UNS_TIME_RK3) {
         for (int irk = 1; irk <= 3; ++irk) {
             bool fused = false;
@@ -2278,7 +2316,7 @@ static int create_impl(const uns_cc_mesh* m, const uns_params* p, bool lusgs_sch
     h->v.wait_cycles = kWaitCycles;
     h->v.skip_code = -1;
     h->nparts = nblocks(noc);
-    AL(partial, h->nparts);
+    AL(partial, 8 * (size_t)h->nparts);  // per-warp partials of a small mesh's spread RK pass
     if ((rc = h->alloc(h->d_scalar, 4))) return fail(rc);
     if ((rc = h->alloc(h->d_iter, 1))) return fail(rc);
     if ((rc = h->alloc(h->d_done, 1))) return fail(rc);
@@ -3069,7 +3107,7 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
         if (!rc && one_pass && !v.mixed) rc = timed(11, [&]() -> int { return enqueue_rk23(h, v); });
         if (!rc && !rk3) rc = timed(9, [&]() -> int { return enqueue_lusgs(h, v); });
         if (!rc) rc = timed(10, [&]() -> int {
-            k_res_final<<<1, kBlock, 0, h->stream>>>(v, h->nparts, h->d_scalar);
+            k_res_final<<<1, kBlock, 0, h->stream>>>(one_pass && !v.mixed ? final_view(h, v) : v, h->nparts, h->d_scalar);
             UNS_CUDA(cudaGetLastError());
             return UNS_OK;
         });

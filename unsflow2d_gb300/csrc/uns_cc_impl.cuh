@@ -118,6 +118,10 @@ struct CCView {
     // instance are padded to a multiple of kBlock (padding: instance -1), so
     // every block of cells belongs to one instance.
     int ninst, cfl_stride;
+    // 1 when `partial` holds one sum per warp of 32 cells (a small mesh's
+    // spread k_cell_rk23): k_res_final adds each 8 of them in warp order,
+    // which is the 256-cell block partial bit for bit.
+    int wpart;
     const int* cinst;       // [ntot] instance of each cell, ghosts included
     const int* finst;       // [nof]
     const int* pinst;       // [nop]
