@@ -796,7 +796,8 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(secs * 1e3 / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "gpu_library": abi.gpu_library_name(),
-        "dtype": "f64" if p.precision == abi.PREC["fp64"] else "f32-face/f64-accumulate",
+        "dtype": ("f64" if p.precision == abi.PREC["fp64"] else
+                  "f64-residual/f32-sweep" if p.precision == abi.PREC["mixed_sweep"] else "f32-face/f64-accumulate"),
         "data": "synthetic: seeded analytic-airfoil O-mesh, uniform freestream start",
         "config": {"workload": w["desc"], "units": units, "edges_or_faces": int(m["nof"] if kind == "nc" else m["nfi"] + m["nbf"]),
                    "global_batch": units, "seq_len": 1, "parallelism": f"replicas x{args.gpus}",
