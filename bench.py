@@ -178,8 +178,9 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = Fal
             "edge": 144 * N + 80 * E + 80 * B,
             "node_res": 60 * N + 56 * E + 80 * B,
             # per taken edge record R (2 per interior edge): 12 B of indices,
-            # normal 16, length 8, la 8, qold 32 read; 96 B written
-            "sweep_prep": 172 * 2 * E,
+            # normal 16, length 8, la 8, qold 32 and its primitives 32 read;
+            # 96 B written; per node the primitives of qold: 32 read, 32 written
+            "sweep_prep": 204 * 2 * E + 64 * N,
             # per node: two items (schedule 16, diag 8, qold 32), res 32,
             # records written 2 x 64, qc 32; per record: 96 B read plus the
             # neighbour's 64 B record polled
@@ -805,7 +806,9 @@ def run_ours(args, w, dist, rank, local_rank) -> dict | None:
                    "setup_s": round(setup_s, 2), "block_sizes": blocks},
         "e2e": e2e,
         "gpu_launches": (cc_launches(p) if kind == "cc" else
-                         LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")]) * args.steps,
+                         LAUNCHES[(kind, "lusgs" if p.time_mode == abi.TIME["lusgs"] else "rk3")]
+                         + (1 if (kind, p.time_mode, p.precision) == ("nc", abi.TIME["lusgs"], abi.PREC["fp64"]) else 0))
+                        * args.steps,
         "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,

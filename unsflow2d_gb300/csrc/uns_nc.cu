@@ -56,6 +56,7 @@ struct NCView {
     const float2* wxyf;   // FP32 LSQ weights per v2v entry
     const float2* edf;    // FP32 edge vector X(fp2) - X(fp1) per edge
     double4* qold;
+    double4* qoldp;  // (u, v, p, e*rho) of qold per node, for the FP64 sweep records
     double4* res;
     double4* gx;
     double4* gy;
@@ -609,6 +610,31 @@ constexpr double kOmega = 1.5;  // lusgs.f90:26
 //   rec[3r]   normalflux(qold(nb)) on the edge (lusgs.f90:137-155)
 //   rec[3r+1] (nx, ny, ds, omega * la)
 //   rec[3r+2] (qold(nb).rho, sign, nb as integer bits, 0)
+// con2prim of qold once per node (a node has about six records): the
+// records' normalflux then reads (u, v, p, e*rho) instead of dividing again,
+// with the same operations on the same values.
+__global__ void __launch_bounds__(kBlock) k_nc_qold_prim(NCView v) {
+    if (stopped(v)) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.nop) return;
+    const double4 q = v.qold[i];
+    Prim P = con2prim(v.g, q.x, q.y, q.z, q.w);
+    v.qoldp[i] = make_double4(P.u, P.v, P.p, P.e * P.rho);
+}
+
+// normalflux_nc from the node's precomputed primitives (rho = qold.rho).
+__device__ __forceinline__ void normalflux_nc_p(const double4& P, double rho, double nx, double ny, double ds,
+                                                double o[4]) {
+    const double u = P.x, vv = P.y, p = P.z, et = P.w;
+    double un = u * nx + vv * ny;
+    o[0] = (et + p) * un;
+    o[1] = rho * un;
+    o[2] = o[1] * u + p * nx;
+    o[3] = o[1] * vv + p * ny;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = o[k] * ds;
+}
+
 __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     if (stopped(v)) return;
     int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -618,7 +644,7 @@ __global__ void __launch_bounds__(kBlock) k_nc_sweep_prep(NCView v) {
     const double ds = v.farea[c];
     const double4 q = v.qold[nb];
     double o[4];
-    normalflux_nc(v.g, q, n.x, n.y, ds, o);
+    normalflux_nc_p(v.qoldp[nb], q.y, n.x, n.y, ds, o);
     v.rec[3 * (size_t)r] = m4(o);
     v.rec[3 * (size_t)r + 1] = make_double4(n.x, n.y, ds, kOmega * v.fla[c]);
     v.rec[3 * (size_t)r + 2] = make_double4(q.y, (double)v.rec_sign[r], __longlong_as_double((long long)nb), 0.0);
@@ -1150,8 +1176,12 @@ int launch_sweeps_nc(uns_nc_handle* h, NCView& v) {
 
 int enqueue_sweep_prep_nc(uns_nc_handle* h, NCView& v) {
     if (v.nrec <= 0) return UNS_OK;
-    if (h->P.precision != UNS_PREC_FP64) NLAUNCH(k_nc_sweep_prep_mixed, v.nrec, v);
-    else NLAUNCH(k_nc_sweep_prep, v.nrec, v);
+    if (h->P.precision != UNS_PREC_FP64) {
+        NLAUNCH(k_nc_sweep_prep_mixed, v.nrec, v);
+    } else {
+        NLAUNCH(k_nc_qold_prim, v.nop, v);
+        NLAUNCH(k_nc_sweep_prep, v.nrec, v);
+    }
     return UNS_OK;
 }
 
@@ -1275,7 +1305,7 @@ int uns_nc_create(const uns_nc_mesh* m, const uns_params* p, uns_nc_handle** out
     UPN(v2f_off, cnt); UPN(v2f, vf);
     { std::vector<int> t(m->v2f_off, m->v2f_off + nop + 1); UPN(rv2f_off, t); }
     { std::vector<int> t(m->v2f, m->v2f + m->v2f_off[nop]); UPN(rv2f, t); }
-    ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(packn, 3 * (size_t)nop); ALN(qold, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
+    ALN(qc, nop); ALN(qp, nop); ALN(qpf, nop); ALN(packn, 3 * (size_t)nop); ALN(qold, nop); ALN(qoldp, nop); ALN(res, nop); ALN(gx, nop); ALN(gy, nop); ALN(phi, nop);
     ALN(dt, nop); ALN(la, nop); ALN(fla, nof); ALN(fF, nof); ALN(bres1, nbnd); ALN(bres2, nbnd); ALN(bla, nbnd);
     ALN(diag, nop); ALN(diaginv, nop); ALN(rec_a, 2 * (size_t)nop); ALN(rec_b, 2 * (size_t)nop); ALN(rec_r, 2 * (size_t)nop);
     ALN(err, 1);
