@@ -249,7 +249,7 @@ def algorithmic_bytes(kind: str, m: dict, mixed: bool = False, sides: bool = Fal
 # quarter-size case, whose reads grow in proportion to the units; see the
 # summaries under profiles/): scaled here to the benchmark's size.
 TRAFFIC_PER_UNIT = {
-    ("nc", "lusgs_sweeps", False): ((454.23e6 + 75.36e6) / 525312, "nodes", "profiles/nc_lusgs_1024x512_launches.md"),
+    ("nc", "lusgs_sweeps", False): ((457.42e6 + 75.82e6) / 525312, "nodes", "profiles/nc_lusgs_1024x512_launches.md"),
     ("cc", "face_conv", False): (58.58e6 / 393728, "faces", "profiles/cc_fp64_512x256_full.md"),
     ("cc", "face_conv", True): (156.96e6 / 1573888, "faces", "profiles/cc_mixed_1024x512_full.md"),
     ("cc", "cell_res", True): (138.34e6 / 1048576, "cells", "profiles/cc_mixed_1024x512_full.md"),
