@@ -3092,7 +3092,8 @@ int uns_cc_profile(uns_cc_handle* h, double cfl, int reps, double* ms, const cha
             if (!rc && one_pass && v.mixed) rc = timed(11, [&]() -> int { return enqueue_wall_rk(h, v); });
             if (!rc) rc = timed(7, [&]() -> int {
                 if (v.mixed) LAUNCH(k_cell_res_mixed, v.noc, v, fuse, smooth ? 0 : 1, one_pass ? 1 : 0);
-                else LAUNCH(k_cell_res, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
+                else if (!(smooth || one_pass) || v.ninst) LAUNCH(k_cell_res, v.noc, v, fuse, (smooth || one_pass) ? 0 : 1);
+                else LAUNCH_SPREAD(k_cell_res, v.noc, v, fuse, 0);  // as the iteration launches it
                 return UNS_OK;
             });
             if (!rc && smooth) rc = timed(8, [&]() -> int {
