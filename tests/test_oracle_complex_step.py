@@ -87,3 +87,55 @@ def test_complex_step_matches_oracle_and_differences(name):
     d_fd = (a_qc - b_qc)[:noc] / (2 * np.deg2rad(1e-4))
     d_cs = c_qc.imag[:noc] / H
     assert np.max(np.abs(d_cs - d_fd)) <= 1e-6 * np.max(np.abs(d_cs))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_geometric_complex_step_matches_differences_of_the_oracle(name):
+    """An imaginary perturbation of one geometric mesh array
+    (oracle_cc_cs_set_geometry_im) against central differences of the oracle
+    on meshes whose array is perturbed: Im(G)/h equals (G(A + eps d) -
+    G(A - eps d)) / (2 eps), array by array: two iterations from a developed
+    state, the second from the first's state with its imaginary part
+    dropped, the geometry perturbed in both (the time step of the second
+    reads the first's face viscosity)."""
+    m = mesh.CCMesh.airfoil(16, 8)
+    kw = CASES[name]
+    p = abi.make_params(ilimit=0, min_res=1e-30, **kw)
+    qc, qp, phi = _developed(m, abi.make_params(min_res=1e-30, **kw))
+    noc = m.arrays["noc"]
+    rng = np.random.default_rng(17)
+    eps = 1e-7
+    for field in ("fnx", "farea", "fcx", "cx", "cv", "r12", "v2c_wt", "px") + (("cov",) if kw["grad"] == "ggfc" else ()):
+        x = np.asarray(m.arrays[field], dtype=np.float64)
+        d = rng.standard_normal(x.shape) * (np.abs(x) + 1e-3 * np.mean(np.abs(x)))
+        o = OracleCCComplexStep(m, p)
+        o.set_geometry_im(field, H * d)  # before both iterations, as the differences perturb both
+        o.set("phi", phi)
+        o.set("qc", qc)
+        o.set("qp", qp)
+        o.iteration(CFL)  # sets the face viscosity the next time step reads
+        q1, g1 = o.get("qc").real, o.get("qp").real
+        o.set("qc", q1)
+        o.set("qp", g1)
+        o.iteration(CFL)
+        cs = o.get("qc")[:noc].imag / H
+        out = []
+        for sgn in (1, -1):
+            arr = dict(m.arrays)
+            arr[field] = x + sgn * eps * d
+            r = OracleCC(arr, p)
+            r.set("phi", phi)
+            r.set("qc", qc)
+            r.set("qp", qp)
+            r.iteration(CFL)
+            r.set("qc", q1)
+            r.set("qp", g1)
+            r.iteration(CFL)
+            out.append(r.get("qc")[:noc])
+        fd = (out[0] - out[1]) / (2 * eps)
+        # the differences' rounding floor is about ulp(q) / eps, 1e-9 of the state;
+        # an array the iteration does not depend on (cv under GG-FC, where dt / cv
+        # cancels the volume) has a zero derivative that the differences see as that
+        scale = np.max(np.abs(cs))
+        floor = 1e-8 * np.max(np.abs(q1))
+        assert np.max(np.abs(cs - fd)) <= 1e-5 * scale + floor, (field, np.max(np.abs(cs - fd)), scale)
