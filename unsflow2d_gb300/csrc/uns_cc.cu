@@ -1592,7 +1592,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
             const int nr = min(8, ntake - base);
-            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
+            int e = 0;
+            if (base == 0) { cres = zero_plus(__shfl_sync(full, t, k)); e = 1; }  // 0.0 + t0, exact
+            for (; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
         }
         // next item's inputs (independent of the sweep), issued once this
         // item's polls are done so they do not queue ahead of them
@@ -1721,7 +1723,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs_mixed(CCView v, const 
             }
             if (__ballot_sync(full, !ok)) return;
             const int nr = min(8, ntake - base);
-            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
+            int e = 0;
+            if (base == 0) { cres = zero_plus(__shfl_sync(full, t, k)); e = 1; }  // 0.0 + t0, exact
+            for (; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
         }
         if (kk + 1 < kend) sweep_load_m(v, Sn, lane, Xn);
         double r = X.r;

@@ -45,6 +45,14 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// 0.0 + x exactly as the FP64 addition rounds it (x itself; -0.0 becomes
+// +0.0), on the integer pipe: the first term of a sum that starts from zero,
+// one FP64 instruction less on a sweep item's dependent chain.
+__device__ __forceinline__ double zero_plus(double x) {
+    const long long b = __double_as_longlong(x);
+    return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+
 // Default bound on every spin-wait in the library's kernels (~2 s at
 // 2 GHz); a handle may set a shorter one (uns_*_set_wait_limit).
 constexpr long long kWaitCycles = 4000000000LL;

@@ -832,11 +832,13 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
                 t = 0.5 * ((__double_as_longlong(E.sgn) < 0 ? -diff : diff) - E.ol * dqk);
             }
             if (__ballot_sync(full, !ok)) return;  // a wait gave up; the error is recorded
-            // the terms in edge order
+            // the terms in edge order, from 0.0 (the first addition is exact)
             const int nr = min(8, ntake - base);
             wx[lane] = t;
             __syncwarp();
-            for (int e = 0; e < nr; ++e) cres = cres + wx[4 * e + k];
+            int e = 0;
+            if (base == 0) { cres = zero_plus(wx[k]); e = 1; }
+            for (; e < nr; ++e) cres = cres + wx[4 * e + k];
             __syncwarp();
         }
         // next item's inputs (independent of the sweep), issued once this
@@ -981,7 +983,9 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
             }
             if (__ballot_sync(full, !ok)) return;
             const int nr = min(8, ntake - base);
-            for (int e = 0; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
+            int e = 0;
+            if (base == 0) { cres = zero_plus(__shfl_sync(full, t, k)); e = 1; }  // 0.0 + t0, exact
+            for (; e < nr; ++e) cres = cres + __shfl_sync(full, t, 4 * e + k);
         }
         if (kk + 1 < kend) sweep_load_m(v, Sn, lane, Xn);
         double r = X.r;
