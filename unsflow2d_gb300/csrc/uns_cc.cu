@@ -1618,28 +1618,41 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_lusgs(CCView v, const int* _
         const double rho = __shfl_sync(full, q, 1);
         const double quo = q / rho;
         const double E0 = __shfl_sync(full, q, 0), Q2 = __shfl_sync(full, q, 2), Q3 = __shfl_sync(full, q, 3);
-        const double e = __shfl_sync(full, quo, 0), u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
-        const double qq = u * u + vv * vv;
-        const double p = gm1 * (E0 - 0.5 * rho * qq);
+        // the four products of the pressure and the record as one
+        // multiplication: lane 0 e*rho, lane 1 0.5*rho, lane 2 u*u, lane 3 v*v
+        // (an FP64 instruction costs the warp the same for one lane or four)
+        const double ma = lane == 1 ? 0.5 : quo, mb = lane < 2 ? rho : quo;
+        const double pr = ma * mb;
+        const double u = __shfl_sync(full, quo, 2), vv = __shfl_sync(full, quo, 3);
+        const double erho = __shfl_sync(full, pr, 0), hrho = __shfl_sync(full, pr, 1);
+        const double qq = __shfl_sync(full, pr, 2) + __shfl_sync(full, pr, 3);  // u*u + v*v
+        const double p = gm1 * (E0 - hrho * qq);                                  // gm1*(E - 0.5*rho*qq)
         L0 = __shfl_sync(full, d, 0);
         L1 = __shfl_sync(full, d, 1);
         L2 = __shfl_sync(full, d, 2);
         L3 = __shfl_sync(full, d, 3);
-        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
+        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = erho;
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
         if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
             last = -1;
-        } else if (lane == 0) {
-            double2* a = reinterpret_cast<double2*>(v.rec_a + slotr);
-            st_relaxed2(a, Lu, Lv);
-            st_relaxed2(a + 1, Lp, Le);
-        } else if (lane == 1) {
-            double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
-            st_relaxed2(b, L0, L1);
-            st_relaxed2(b + 1, L2, L3);
-        } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(E0, rho, Q2, Q3);
+        } else {
+            // Lane 0 stores (u, v, p, e*rho), lane 1 dq, as predicated stores
+            // of one instruction sequence (lane-divergent branches around the
+            // stores cost the sweep's critical path more than the stores).
+            double2* dst = reinterpret_cast<double2*>(lane == 0 ? v.rec_a + slotr : v.rec_b + slotr);
+            const double x0 = lane == 0 ? Lu : L0, x1 = lane == 0 ? Lv : L1;
+            const double x2 = lane == 0 ? Lp : L2, x3 = lane == 0 ? Le : L3;
+            const int st_ab = lane < 2;
+            asm volatile(
+                "{\n\t.reg .pred pa;\n\t"
+                "setp.ne.s32 pa, %0, 0;\n\t"
+                "@pa st.relaxed.gpu.global.v2.f64 [%1], {%2, %3};\n\t"
+                "@pa st.relaxed.gpu.global.v2.f64 [%4], {%5, %6};\n\t}"
+                :
+                : "r"(st_ab), "l"(dst), "d"(x0), "d"(x1), "l"(dst + 1), "d"(x2), "d"(x3)
+                : "memory");
+            if (pass == 1 && lane == 2) v.qc[it] = make_double4(E0, rho, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;

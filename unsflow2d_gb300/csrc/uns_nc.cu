@@ -867,15 +867,21 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs(NCView v, const int
         const double2 qa = reinterpret_cast<const double2*>(wx)[0], qb = reinterpret_cast<const double2*>(wx)[1];
         const double E0 = qa.x, rho = qa.y, Q2 = qb.x, Q3 = qb.y;
         const double quo = q / rho;
-        if (lane < 4) wx[8 + lane] = quo;
+        // the four products of the pressure and the record as one
+        // multiplication: lane 0 e*rho, lane 1 0.5*rho, lane 2 u*u, lane 3 v*v
+        // (an FP64 instruction costs the warp the same for one lane or four)
+        const double ma = lane == 1 ? 0.5 : quo, mb = lane < 2 ? rho : quo;
+        const double pr = ma * mb;
+        if (lane < 4) { wx[8 + lane] = quo; wx[12 + lane] = pr; }
         __syncwarp();
         const double2 da = reinterpret_cast<const double2*>(wx)[2], db = reinterpret_cast<const double2*>(wx)[3];
-        const double e = wx[8], u = wx[10], vv = wx[11];
+        const double2 pa = reinterpret_cast<const double2*>(wx)[6], pb = reinterpret_cast<const double2*>(wx)[7];
+        const double u = wx[10], vv = wx[11];
         L0 = da.x; L1 = da.y; L2 = db.x; L3 = db.y;
         __syncwarp();
-        const double qq = u * u + vv * vv;
-        const double p = gm1 * (E0 - 0.5 * rho * qq);
-        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = e * rho;
+        const double qq = pb.x + pb.y;                // u*u + v*v
+        const double p = gm1 * (E0 - pa.y * qq);      // gm1*(E - 0.5*rho*qq)
+        Lrho = rho; Lu = u; Lv = vv; Lp = p; Le = pa.x;
         last = (it << 1) | pass;
         const size_t slotr = (size_t)pass * n + it;
         if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
