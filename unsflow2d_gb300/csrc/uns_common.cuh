@@ -171,10 +171,26 @@ __device__ __forceinline__ float dflux_k(const Rec& e, float gm1, const float dq
     return df1 * v2 + run * dv + dp * e.ny;
 }
 
-__device__ __forceinline__ void st_relaxed4f(float4* p, float a, float b, float c, float d) {
-    asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" : : "l"(p), "f"(a), "f"(b), "f"(c), "f"(d)
-                 : "memory");
+// Publishes a mixed-form sweep record: lane 0 the FP32 dq (one float4
+// slot), lane 1 the FP64 dq (two double2), as predicated stores of one
+// instruction sequence; lane-divergent branches around the stores cost a
+// sweep's critical path more than the stores themselves (measured).
+__device__ __forceinline__ void publish_mixed(int lane, float4* a, double2* b, const float f[4], double d0, double d1,
+                                              double d2, double d3) {
+    const int p0 = lane == 0, p1 = lane == 1;
+    asm volatile(
+        "{\n\t.reg .pred q0, q1;\n\t"
+        "setp.ne.s32 q0, %0, 0;\n\t"
+        "setp.ne.s32 q1, %1, 0;\n\t"
+        "@q0 st.relaxed.gpu.global.v4.f32 [%2], {%3, %4, %5, %6};\n\t"
+        "@q1 st.relaxed.gpu.global.v2.f64 [%7], {%8, %9};\n\t"
+        "@q1 st.relaxed.gpu.global.v2.f64 [%10], {%11, %12};\n\t}"
+        :
+        : "r"(p0), "r"(p1), "l"(a), "f"(f[0]), "f"(f[1]), "f"(f[2]), "f"(f[3]), "l"(b), "d"(d0), "d"(d1), "l"(b + 1),
+          "d"(d2), "d"(d3)
+        : "memory");
 }
+
 static __global__ void __launch_bounds__(kBlock) k_fill_unset_f(float4* p, long long n4) {
     const float u = __int_as_float((int)kUnsetF);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x)

@@ -1023,14 +1023,10 @@ __global__ void __launch_bounds__(kSweepBlock, 1) k_nc_lusgs_mixed(NCView v, con
         const size_t slotr = (size_t)pass * n + it;
         if (last == v.skip_code) {  // test hook: this item publishes nothing and hands nothing on
             last = -1;
-        } else if (lane == 0) {
-            st_relaxed4f(reinterpret_cast<float4*>(v.rec_a) + slotr, LF[0], LF[1], LF[2], LF[3]);
-        } else if (lane == 1) {
-            double2* b = reinterpret_cast<double2*>(v.rec_b + slotr);
-            st_relaxed2(b, L0, L1);
-            st_relaxed2(b + 1, L2, L3);
-        } else if (lane == 2 && pass == 1) {
-            v.qc[it] = make_double4(Q0, Q1, Q2, Q3);
+        } else {
+            publish_mixed(lane, reinterpret_cast<float4*>(v.rec_a) + slotr, reinterpret_cast<double2*>(v.rec_b + slotr), LF,
+                          L0, L1, L2, L3);
+            if (pass == 1 && lane == 2) v.qc[it] = make_double4(Q0, Q1, Q2, Q3);
         }
         S = Sn;
         Sn = Snn;
