@@ -70,6 +70,17 @@ int uns_host_nc_newnum(const uns_host_nc* m, int32_t* out);  /* [nop] */
 void uns_host_cc_free(uns_host_cc* m);
 void uns_host_nc_free(uns_host_nc* m);
 
+/* Test hook (no reference counterpart): the LU-SGS sweeps' warp schedule as
+ * uns_cc_create / uns_nc_create build it (the forward and backward sweeps of
+ * CCFVM/lusgs.F90:245-318 and NCFVM/lusgs.f90:48-124 as one dependency
+ * graph), for n entities with CSR neighbour lists nbr_off[n+1] / nbr
+ * (entries outside [0, n) ignored) on nwarps warps: off[nwarps+1] offsets
+ * into items[2n], each item (entity << 1) | pass (pass 0 forward, 1
+ * backward), in each warp's execution order; levels[2] = the dependency
+ * levels of the forward and backward sweeps. */
+int uns_host_sweep_schedule(int n, const int32_t* nbr_off, const int32_t* nbr, int nwarps, int32_t* off, int32_t* items,
+                            int32_t* levels);
+
 /* flo.inp readers.  `grid` receives the GridFile value (up to gridlen-1
  * characters). */
 int uns_host_read_flo_cc(const char* path, uns_params* p, char* grid, int gridlen);

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "../uns_sched.hpp"
 #include "host_mesh.hpp"
 #include "unsflow_host.h"
 
@@ -272,6 +273,21 @@ int uns_host_read_flow(const char* path, double* qc, int n) {
         }
     }
     std::fclose(f);
+    return UNS_OK;
+}
+
+int uns_host_sweep_schedule(int n, const int32_t* nbr_off, const int32_t* nbr, int nwarps, int32_t* off, int32_t* items,
+                            int32_t* levels) {
+    if (n < 0 || nwarps < 1 || !nbr_off || (n > 0 && !nbr) || !off || (n > 0 && !items) || !levels)
+        return fail(UNS_ERR_ARG, "uns_host_sweep_schedule: bad argument");
+    if (nbr_off[0] != 0) return fail(UNS_ERR_ARG, "uns_host_sweep_schedule: nbr_off[0] != 0");
+    for (int i = 0; i < n; ++i)
+        if (nbr_off[i + 1] < nbr_off[i]) return fail(UNS_ERR_ARG, "uns_host_sweep_schedule: nbr_off decreases");
+    const uns::WarpSchedule ws = uns::list_schedule(n, nbr_off, nbr, nwarps);
+    std::copy(ws.off.begin(), ws.off.end(), off);
+    std::copy(ws.items.begin(), ws.items.end(), items);
+    levels[0] = ws.nlev_fwd;
+    levels[1] = ws.nlev_bwd;
     return UNS_OK;
 }
 

@@ -136,7 +136,7 @@ inline WarpSchedule list_schedule(int n, const int* nbr_off, const int* nbr, int
         place(2 * i + 1);
     }
     WarpSchedule out;
-    out.makespan = *std::max_element(fin.begin(), fin.end());
+    out.makespan = fin.empty() ? 0.0 : *std::max_element(fin.begin(), fin.end());
     out.nlev_fwd = nlev;
     out.nlev_bwd = nlevb;
     out.off.assign(nwarps + 1, 0);
