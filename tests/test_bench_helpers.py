@@ -53,3 +53,30 @@ def test_algorithmic_bytes_cover_each_form(bench):
     n = mesh.NCMesh.airfoil(32, 16).arrays
     nc = bench.algorithmic_bytes("nc", n)
     assert {"grad_lim", "edge", "node_res", "lusgs_sweeps"} <= set(nc)
+
+
+def _reference_arm(env_extra=None):
+    import json
+    import os
+    import subprocess
+    import sys
+    env = dict(os.environ, **(env_extra or {}))
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--mesh", "48x24", "--steps", "3",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_prints_one_line_with_the_contract_keys(bench):
+    (d,) = _reference_arm()
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["higher_is_better"] is True and d["dtype"] == "f64" and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["steps"] >= 1 and d["ms_per_step"] > 0 and "48x24" in d["config"]["workload"]
+
+
+def test_reference_arm_runs_on_rank_0_only():
+    assert _reference_arm({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"}) == []
