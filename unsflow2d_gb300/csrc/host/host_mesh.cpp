@@ -421,11 +421,6 @@ bool triarea(const double xy[2][3], double& area) {
     return area > 0.0;
 }
 
-void append_unique(std::vector<int>& v, int x) {
-    for (int y : v) if (y == x) return;
-    v.push_back(x);
-}
-
 template <class VV>
 void to_csr(const VV& lists, std::vector<int>& off, std::vector<int>& idx) {
     off.assign(lists.size() + 1, 0);
@@ -511,12 +506,26 @@ int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
         m.fny[i] = m.fny[i] / m.farea[i];
     }
 
+    // The connectivity below is built in flat CSR arrays (a count pass, then a
+    // fill pass in the reference's loop order) rather than one growing list
+    // per cell or node: the same entries in the same order, without millions
+    // of small allocations on a 4 M-cell mesh.
+    // appends x to the list seg[0..cnt) unless it is there already
+    auto add_unique = [](int* seg, int& cnt, int x) {
+        for (int k = 0; k < cnt; ++k)
+            if (seg[k] == x) return;
+        seg[cnt++] = x;
+    };
+
     // cell_2_cell (geometric.F90:200-245): interior faces only, face order.
-    std::vector<std::vector<int>> c2c(noc);
+    std::vector<int> cc_off(noc + 1, 0), cc_n(noc, 0);
+    for (int i = 0; i < nfi; ++i) { ++cc_off[m.fin[i] + 1]; ++cc_off[m.fout[i] + 1]; }
+    for (int i = 0; i < noc; ++i) cc_off[i + 1] += cc_off[i];
+    std::vector<int> cc_idx(cc_off[noc], -1);
     for (int i = 0; i < nfi; ++i) {
         int in = m.fin[i], out = m.fout[i];
-        append_unique(c2c[in], out);
-        append_unique(c2c[out], in);
+        add_unique(&cc_idx[cc_off[in]], cc_n[in], out);
+        add_unique(&cc_idx[cc_off[out]], cc_n[out], in);
     }
 
     // renumber (geometric.F90:247-356): breadth-first from cell 1.
@@ -526,8 +535,10 @@ int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
     for (int i = 0; i < noc; ++i) {
         int it = oldnum[i];
         if (it < 0) { err = "renumber: mesh is not connected"; return UNS_ERR_MESH; }
-        for (int t1 : c2c[it])
+        for (int k = cc_off[it]; k < cc_off[it] + cc_n[it]; ++k) {
+            int t1 = cc_idx[k];
             if (t1 >= 0 && t1 < noc && newnum[t1] < 0) { ++c; oldnum[c] = t1; newnum[t1] = c; }
+        }
     }
     if (c + 1 != noc) { err = "renumber: count does not match no. of cells"; return UNS_ERR_MESH; }
     for (int i = 0; i < nof; ++i) {
@@ -536,66 +547,95 @@ int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
     }
     {
         std::vector<double> ncx(m.cx), ncy(m.cy), ncv(noc);
-        std::vector<std::vector<int>> nc2c(noc);
+        m.nc2c.resize(noc);
+        m.c2c_off.assign(noc + 1, 0);
         for (int i = 0; i < noc; ++i) {
             int it = oldnum[i];
             ncx[i] = m.cx[it]; ncy[i] = m.cy[it]; ncv[i] = cv[it];
-            for (int t1 : c2c[it]) nc2c[i].push_back((t1 >= 0 && t1 < noc) ? newnum[t1] : t1);
+            m.nc2c[i] = cc_n[it];
+            m.c2c_off[i + 1] = m.c2c_off[i] + cc_n[it];
         }
-        m.cx.swap(ncx); m.cy.swap(ncy); cv.swap(ncv); c2c.swap(nc2c);
+        m.c2c.resize(m.c2c_off[noc]);
+        for (int i = 0; i < noc; ++i) {
+            int it = oldnum[i];
+            for (int k = 0; k < cc_n[it]; ++k) {
+                int t1 = cc_idx[cc_off[it] + k];
+                m.c2c[m.c2c_off[i] + k] = (t1 >= 0 && t1 < noc) ? newnum[t1] : t1;
+            }
+        }
+        m.cx.swap(ncx); m.cy.swap(ncy); cv.swap(ncv);
     }
     m.newnum = newnum;
     m.cv = cv;
-    m.nc2c.resize(noc);
-    for (int i = 0; i < noc; ++i) m.nc2c[i] = (int)c2c[i].size();
-    to_csr(c2c, m.c2c_off, m.c2c);
 
     // cell_2_face (geometric.F90:425-457).
-    std::vector<std::vector<int>> c2f(noc);
+    m.c2f_off.assign(noc + 1, 0);
     for (int i = 0; i < nof; ++i) {
         int in = m.fin[i], out = m.fout[i];
-        if (in >= 0) c2f[in].push_back(i);
-        if (out >= 0 && out < noc) c2f[out].push_back(i);
+        if (in >= 0) ++m.c2f_off[in + 1];
+        if (out >= 0 && out < noc) ++m.c2f_off[out + 1];
+    }
+    for (int i = 0; i < noc; ++i) m.c2f_off[i + 1] += m.c2f_off[i];
+    m.c2f.assign(m.c2f_off[noc], -1);
+    {
+        std::vector<int> cur(m.c2f_off.begin(), m.c2f_off.end() - 1);
+        for (int i = 0; i < nof; ++i) {
+            int in = m.fin[i], out = m.fout[i];
+            if (in >= 0) m.c2f[cur[in]++] = i;
+            if (out >= 0 && out < noc) m.c2f[cur[out]++] = i;
+        }
     }
 
     // vertex_2_cell (geometric.F90:459-531): ghosts included.
-    std::vector<std::vector<int>> v2c(nop);
-    for (int i = 0; i < nof; ++i) {
-        int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
-        if (in < 0) { err = "v2c:in"; return UNS_ERR_MESH; }
-        append_unique(v2c[p1], in);
-        append_unique(v2c[p2], in);
-        if (out < 0) { err = "v2c:out"; return UNS_ERR_MESH; }
-        append_unique(v2c[p1], out);
-        append_unique(v2c[p2], out);
+    {
+        std::vector<int> vo(nop + 1, 0), vn(nop, 0);
+        for (int i = 0; i < nof; ++i) { vo[m.fp1[i] + 1] += 2; vo[m.fp2[i] + 1] += 2; }
+        for (int i = 0; i < nop; ++i) vo[i + 1] += vo[i];
+        std::vector<int> vi(vo[nop], -1);
+        for (int i = 0; i < nof; ++i) {
+            int p1 = m.fp1[i], p2 = m.fp2[i], in = m.fin[i], out = m.fout[i];
+            if (in < 0) { err = "v2c:in"; return UNS_ERR_MESH; }
+            add_unique(&vi[vo[p1]], vn[p1], in);
+            add_unique(&vi[vo[p2]], vn[p2], in);
+            if (out < 0) { err = "v2c:out"; return UNS_ERR_MESH; }
+            add_unique(&vi[vo[p1]], vn[p1], out);
+            add_unique(&vi[vo[p2]], vn[p2], out);
+        }
+        m.v2c_off.assign(nop + 1, 0);
+        for (int i = 0; i < nop; ++i) m.v2c_off[i + 1] = m.v2c_off[i] + vn[i];
+        m.v2c.resize(m.v2c_off[nop]);
+        for (int i = 0; i < nop; ++i) std::copy(vi.begin() + vo[i], vi.begin() + vo[i] + vn[i], m.v2c.begin() + m.v2c_off[i]);
     }
 
     // cell_2_vertex (geometric.F90:533-616): walks the faces of each cell and
     // reorders its c2f list as it goes (LU-SGS later loops over c2f).
-    std::vector<std::vector<int>> c2v(noc);
+    m.c2v_off.assign(noc + 1, 0);
+    m.c2v.clear();
+    m.c2v.reserve(m.c2f.size() + noc);
     for (int i = 0; i < noc; ++i) {
         double xc = m.cx[i], yc = m.cy[i];
-        auto& F = c2f[i];
-        auto& V = c2v[i];
-        int nf = (int)F.size();
+        int* F = m.c2f.data() + m.c2f_off[i];
+        int nf = m.c2f_off[i + 1] - m.c2f_off[i];
+        if (nf < 1) { err = "cell without faces"; return UNS_ERR_MESH; }
+        const size_t v0 = m.c2v.size();
         int p1 = m.fp1[F[0]], p2 = m.fp2[F[0]];
-        if (dotprod(px, py, p1, p2, xc, yc) < 0.0) { V.push_back(p1); V.push_back(p2); }
-        else { V.push_back(p2); V.push_back(p1); }
+        if (dotprod(px, py, p1, p2, xc, yc) < 0.0) { m.c2v.push_back(p1); m.c2v.push_back(p2); }
+        else { m.c2v.push_back(p2); m.c2v.push_back(p1); }
         for (int k = 1; k < nf - 1; ++k) {
-            int last = V.back();
+            int last = m.c2v.back();
             for (int j = k; j < nf; ++j) {
                 int m1 = m.fp1[F[j]], m2 = m.fp2[F[j]];
                 if (m1 == last || m2 == last) {
-                    if (dotprod(px, py, m1, m2, xc, yc) < 0.0) V.push_back(m2);
-                    else V.push_back(m1);
+                    if (dotprod(px, py, m1, m2, xc, yc) < 0.0) m.c2v.push_back(m2);
+                    else m.c2v.push_back(m1);
                     std::swap(F[j], F[k]);
                 }
             }
         }
-        V.push_back(V[0]);
+        const int first = m.c2v[v0];
+        m.c2v.push_back(first);
+        m.c2v_off[i + 1] = (int)m.c2v.size();
     }
-    to_csr(c2f, m.c2f_off, m.c2f);
-    to_csr(c2v, m.c2v_off, m.c2v);
 
     // face_co_volume (geometric.F90:619-674).
     m.fcov.assign(nof, 0.0);
@@ -641,7 +681,6 @@ int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
     }
 
     // pseudo_Laplacian (geometric.F90:962-1013).
-    to_csr(v2c, m.v2c_off, m.v2c);
     m.v2c_wt.assign(m.v2c.size(), 0.0);
     for (int i = 0; i < nop; ++i) {
         double ixx = 0, iyy = 0, ixy = 0, rx = 0, ry = 0;
