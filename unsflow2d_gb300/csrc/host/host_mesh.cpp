@@ -421,14 +421,6 @@ bool triarea(const double xy[2][3], double& area) {
     return area > 0.0;
 }
 
-template <class VV>
-void to_csr(const VV& lists, std::vector<int>& off, std::vector<int>& idx) {
-    off.assign(lists.size() + 1, 0);
-    for (size_t i = 0; i < lists.size(); ++i) off[i + 1] = off[i] + (int)lists[i].size();
-    idx.resize(off.back());
-    for (size_t i = 0; i < lists.size(); ++i) std::copy(lists[i].begin(), lists[i].end(), idx.begin() + off[i]);
-}
-
 }  // namespace
 
 int geometric_cc(const RawCC& raw, MeshCC& m, std::string& err) {
@@ -728,11 +720,18 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
     m.cx = raw.cx; m.cy = raw.cy; m.ccv = raw.cv;
     m.fp1 = raw.fp1; m.fp2 = raw.fp2; m.fin = raw.fin; m.fout = raw.fout; m.fbc = raw.fbc;
 
-    // vertex_2_vertex (NCFVM/geometric.f90:52-81): face order, no dedup.
-    std::vector<std::vector<int>> v2v(nop);
-    for (int i = 0; i < nof; ++i) {
-        v2v[m.fp1[i]].push_back(m.fp2[i]);
-        v2v[m.fp2[i]].push_back(m.fp1[i]);
+    // vertex_2_vertex (NCFVM/geometric.f90:52-81): face order, no dedup; a
+    // flat CSR array (count pass, fill pass) rather than a list per node.
+    std::vector<int> vv_off(nop + 1, 0);
+    for (int i = 0; i < nof; ++i) { ++vv_off[m.fp1[i] + 1]; ++vv_off[m.fp2[i] + 1]; }
+    for (int i = 0; i < nop; ++i) vv_off[i + 1] += vv_off[i];
+    std::vector<int> vv(vv_off[nop]);
+    {
+        std::vector<int> cur(vv_off.begin(), vv_off.end() - 1);
+        for (int i = 0; i < nof; ++i) {
+            vv[cur[m.fp1[i]]++] = m.fp2[i];
+            vv[cur[m.fp2[i]]++] = m.fp1[i];
+        }
     }
     // renumber (NCFVM/geometric.f90:85-180): breadth-first from node 1.
     std::vector<int> oldnum(nop, -1), newnum(nop, -1);
@@ -741,20 +740,30 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
     for (int i = 0; i < nop; ++i) {
         int it = oldnum[i];
         if (it < 0) { err = "renumber: mesh is not connected"; return UNS_ERR_MESH; }
-        for (int t1 : v2v[it])
+        for (int k = vv_off[it]; k < vv_off[it + 1]; ++k) {
+            int t1 = vv[k];
             if (t1 >= 0 && newnum[t1] < 0) { ++c; oldnum[c] = t1; newnum[t1] = c; }
+        }
     }
     if (c + 1 != nop) { err = "renumber: count does not match nt"; return UNS_ERR_MESH; }
     {
         std::vector<double> nx(nop), ny(nop);
         std::vector<int> nbc(nop);
-        std::vector<std::vector<int>> nv(nop);
+        m.v2v_off.assign(nop + 1, 0);
         for (int i = 0; i < nop; ++i) {
             int it = oldnum[i];
             nx[i] = raw.px[it]; ny[i] = raw.py[it]; nbc[i] = raw.pbc[it];
-            for (int t1 : v2v[it]) nv[i].push_back(t1 >= 0 ? newnum[t1] : t1);
+            m.v2v_off[i + 1] = m.v2v_off[i] + (vv_off[it + 1] - vv_off[it]);
         }
-        m.px.swap(nx); m.py.swap(ny); m.pbc.swap(nbc); v2v.swap(nv);
+        m.v2v.resize(m.v2v_off[nop]);
+        for (int i = 0; i < nop; ++i) {
+            int it = oldnum[i];
+            for (int k = vv_off[it]; k < vv_off[it + 1]; ++k) {
+                int t1 = vv[k];
+                m.v2v[m.v2v_off[i] + (k - vv_off[it])] = t1 >= 0 ? newnum[t1] : t1;
+            }
+        }
+        m.px.swap(nx); m.py.swap(ny); m.pbc.swap(nbc);
     }
     for (int i = 0; i < nof; ++i) { m.fp1[i] = newnum[m.fp1[i]]; m.fp2[i] = newnum[m.fp2[i]]; }
     m.newnum = newnum;
@@ -827,8 +836,14 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
         if (!(m.cv[i] > 0.0)) { err = "non-positive dual volume"; return UNS_ERR_MESH; }
 
     // vertex_2_face (NCFVM/geometric.f90:347-379): face order.
-    std::vector<std::vector<int>> v2f(nop);
-    for (int i = 0; i < nof; ++i) { v2f[m.fp1[i]].push_back(i); v2f[m.fp2[i]].push_back(i); }
+    m.v2f_off.assign(nop + 1, 0);
+    for (int i = 0; i < nof; ++i) { ++m.v2f_off[m.fp1[i] + 1]; ++m.v2f_off[m.fp2[i] + 1]; }
+    for (int i = 0; i < nop; ++i) m.v2f_off[i + 1] += m.v2f_off[i];
+    m.v2f.resize(m.v2f_off[nop]);
+    {
+        std::vector<int> cur(m.v2f_off.begin(), m.v2f_off.end() - 1);
+        for (int i = 0; i < nof; ++i) { m.v2f[cur[m.fp1[i]]++] = i; m.v2f[cur[m.fp2[i]]++] = i; }
+    }
 
     // face_co_volume (NCFVM/geometric.f90:657-758): consistency check only.
     m.fcov.assign(nof, 0.0);
@@ -857,7 +872,6 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
     }
 
     // LSQR_Coeff (NCFVM/geometric.f90:760-806): weights per v2v entry.
-    to_csr(v2v, m.v2v_off, m.v2v);
     m.wx.assign(m.v2v.size(), 0.0); m.wy.assign(m.v2v.size(), 0.0);
     for (int i = 0; i < nop; ++i) {
         double xc = px[i], yc = py[i];
@@ -879,7 +893,6 @@ int geometric_nc(const RawNC& raw, MeshNC& m, std::string& err) {
             m.wy[k] = alfa2;
         }
     }
-    to_csr(v2f, m.v2f_off, m.v2f);
     return UNS_OK;
 }
 
